@@ -1,0 +1,235 @@
+"""ctypes binding of the engine's C ABI (include/igaos_pdhg.h).
+
+This is the reference-facing boundary seen from Python: the same calls a
+cgo/JNI/ctypes user makes. There is no CPU fallback: if the native library
+is missing or fails to load, every call raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libigaos_pdhg.so")
+
+OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_NODEVICE, ERR_NUMERIC, ERR_TIMEOUT = range(7)
+FP64, FP32_REFINE, FP32 = 0, 1, 2
+PRECISIONS = {"fp64": FP64, "fp32-refine": FP32_REFINE, "fp32": FP32}
+STATUS_NAMES = ["optimal", "near-optimal", "feasible", "infeasible", "unbounded",
+                "iteration-limit", "time-limit", "error"]
+
+_dp = C.POINTER(C.c_double)
+_ip = C.POINTER(C.c_int)
+
+
+class Options(C.Structure):
+    _fields_ = [
+        ("time_limit_s", C.c_double), ("tolerance", C.c_double),
+        ("max_iterations", C.c_int64), ("seed", C.c_int), ("presolve", C.c_int),
+        ("restarts", C.c_int), ("verbosity", C.c_int), ("precision", C.c_int),
+        ("check_period", C.c_int), ("inner_tolerance", C.c_double),
+        ("max_refinements", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("status", C.c_int), ("error_code", C.c_int), ("objective", C.c_double),
+        ("pinf", C.c_double), ("dinf", C.c_double), ("rel_gap", C.c_double),
+        ("prow", C.c_double), ("iterations", C.c_int64), ("attempts", C.c_int64),
+        ("kkt_checks", C.c_int64), ("restarts", C.c_int64), ("kkt_passes", C.c_int64),
+        ("refinements", C.c_int), ("solve_time_ms", C.c_double),
+        ("setup_time_ms", C.c_double), ("device_time_ms", C.c_double),
+        ("attempt_time_ms", C.c_double), ("message", C.c_char * 160),
+    ]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_}
+        d["message"] = self.message.decode(errors="replace")
+        d["status_name"] = STATUS_NAMES[self.status] if 0 <= self.status < 8 else "?"
+        return d
+
+
+_LIB = None
+
+
+def lib():
+    """Loads libigaos_pdhg.so (raises if absent -- never falls back)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"{LIB_PATH} is not built; run igaos_gb300.build.build()")
+        L = C.CDLL(LIB_PATH)
+        L.igaos_pdhg_create.argtypes = [
+            C.POINTER(C.c_void_p), C.c_int, C.c_int, C.c_int64, _ip, _ip, _dp, _ip, _ip, _dp,
+            _dp, _dp, _dp, _dp, _dp, C.c_double, C.POINTER(Options)]
+        L.igaos_pdhg_solve.argtypes = [C.c_void_p, C.POINTER(Options), C.POINTER(Result), _dp, _dp]
+        L.igaos_pdhg_destroy.argtypes = [C.c_void_p]
+        L.igaos_pdhg_destroy.restype = None
+        L.igaos_pdhg_default_options.argtypes = [C.POINTER(Options)]
+        L.igaos_pdhg_default_options.restype = None
+        L.igaos_pdhg_last_error.argtypes = [C.c_char_p, C.c_size_t]
+        L.igaos_pdhg_solve_csr.argtypes = [
+            C.c_int, C.c_int, C.c_int64, _ip, _ip, _dp, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp,
+            C.c_double, C.POINTER(Options), C.POINTER(Result), _dp, _dp]
+        L.igaos_pdhg_get_scaling.argtypes = [C.c_void_p, _dp, _dp]
+        L.igaos_pdhg_get_step_init.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.igaos_pdhg_get_transpose.argtypes = [C.c_void_p, _ip, _ip, _dp]
+        L.igaos_pdhg_iterate.argtypes = [C.c_void_p, C.c_int, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.igaos_pdhg_evaluate.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.igaos_pdhg_spmv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp]
+        _LIB = L
+    return _LIB
+
+
+def last_error() -> str:
+    buf = C.create_string_buffer(512)
+    lib().igaos_pdhg_last_error(buf, 512)
+    return buf.value.decode(errors="replace")
+
+
+class EngineError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"igaos_pdhg error {code}: {msg}")
+        self.code = code
+
+
+def _check(rc):
+    if rc != OK:
+        raise EngineError(rc, last_error())
+
+
+def _d(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def _i(a):
+    return None if a is None else a.ctypes.data_as(_ip)
+
+
+def default_options(**kw) -> Options:
+    o = Options()
+    lib().igaos_pdhg_default_options(C.byref(o))
+    for k, v in kw.items():
+        if k == "precision" and isinstance(v, str):
+            v = PRECISIONS[v]
+        if not hasattr(o, k):
+            raise TypeError(f"unknown option {k!r}")
+        setattr(o, k, v)
+    return o
+
+
+def _arrays(lp, with_transpose=True):
+    f = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    i = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    a = dict(ap=i(lp.ap), ai=i(lp.ai), ax=f(lp.ax), c=f(lp.c), cl=f(lp.cl), cu=f(lp.cu),
+             rmin=f(lp.rmin), rmax=f(lp.rmax))
+    if with_transpose and getattr(lp, "cp", None) is not None:
+        a.update(cp=i(lp.cp), ci=i(lp.ci), acx=f(lp.acx))
+    else:
+        a.update(cp=None, ci=None, acx=None)
+    return a
+
+
+class Problem:
+    """An LP uploaded to the GPU (igaos_pdhg_create / _destroy)."""
+
+    def __init__(self, lp, with_transpose=True, **opts):
+        self.m, self.n = int(lp.m), int(lp.n)
+        a = _arrays(lp, with_transpose)
+        self._keep = a
+        self.nnz = int(a["ap"][self.m])
+        h = C.c_void_p()
+        o = default_options(**opts)
+        rc = lib().igaos_pdhg_create(
+            C.byref(h), self.m, self.n, self.nnz, _i(a["ap"]), _i(a["ai"]), _d(a["ax"]),
+            _i(a["cp"]), _i(a["ci"]), _d(a["acx"]), _d(a["c"]), _d(a["cl"]), _d(a["cu"]),
+            _d(a["rmin"]), _d(a["rmax"]), float(getattr(lp, "obj_const", 0.0)), C.byref(o))
+        _check(rc)
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().igaos_pdhg_destroy(self.h)
+            self.h = None
+
+    __del__ = close
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def solve(self, **opts):
+        o = default_options(**opts)
+        r = Result()
+        x = np.zeros(self.n)
+        y = np.zeros(self.m)
+        rc = lib().igaos_pdhg_solve(self.h, C.byref(o), C.byref(r), _d(x), _d(y))
+        d = r.as_dict()
+        d["rc"] = rc
+        d["x"], d["y"] = x, y
+        return d
+
+    def scaling(self):
+        dr, dc = np.zeros(self.m), np.zeros(self.n)
+        _check(lib().igaos_pdhg_get_scaling(self.h, _d(dr), _d(dc)))
+        return dr, dc
+
+    def step_init(self):
+        v = [C.c_double() for _ in range(3)]
+        _check(lib().igaos_pdhg_get_step_init(self.h, *[C.byref(t) for t in v]))
+        return tuple(t.value for t in v)
+
+    def transpose(self):
+        cp = np.zeros(self.n + 1, np.int32)
+        ci = np.zeros(self.nnz, np.int32)
+        acx = np.zeros(self.nnz)
+        _check(lib().igaos_pdhg_get_transpose(self.h, _i(cp), _i(ci), _d(acx)))
+        return cp, ci, acx
+
+    def iterate(self, state: dict, iters: int, precision="fp64"):
+        st = {k: np.ascontiguousarray(state[k], dtype=np.float64).copy()
+              for k in ("x", "y", "xavg", "yavg", "axcur")}
+        s6 = np.array([state["eta"], state["omega"], state["k"], state["hn"], 0, 0], np.float64)
+        prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        _check(lib().igaos_pdhg_iterate(self.h, prec, int(iters), _d(st["x"]), _d(st["y"]),
+                                        _d(st["xavg"]), _d(st["yavg"]), _d(st["axcur"]), _d(s6)))
+        st.update(eta=s6[0], omega=s6[1], k=int(s6[2]), hn=int(s6[3]), attempts=int(s6[4]),
+                  parity=int(s6[5]))
+        return st
+
+    def evaluate(self, x, y):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.ascontiguousarray(y, np.float64)
+        out = np.zeros(6)
+        _check(lib().igaos_pdhg_evaluate(self.h, _d(x), _d(y), _d(out)))
+        return dict(zip(("pinf", "dinf", "gap", "op", "od", "prow"), out.tolist()))
+
+    def spmv(self, x, transpose=False, precision="fp64"):
+        x = np.ascontiguousarray(x, np.float64)
+        y = np.zeros(self.n if transpose else self.m)
+        prec = PRECISIONS[precision] if isinstance(precision, str) else precision
+        _check(lib().igaos_pdhg_spmv(self.h, int(bool(transpose)), prec, _d(x), _d(y)))
+        return y
+
+
+def solve_lp(lp, **opts):
+    """One-shot solve of an LP object (m, n, ap, ai, ax, [cp, ci, acx], c, cl,
+    cu, rmin, rmax, obj_const) through igaos_pdhg_solve_csr."""
+    a = _arrays(lp)
+    m, n = int(lp.m), int(lp.n)
+    o = default_options(**opts)
+    r = Result()
+    x, y = np.zeros(n), np.zeros(m)
+    rc = lib().igaos_pdhg_solve_csr(
+        m, n, int(a["ap"][m]), _i(a["ap"]), _i(a["ai"]), _d(a["ax"]), _i(a["cp"]), _i(a["ci"]),
+        _d(a["acx"]), _d(a["c"]), _d(a["cl"]), _d(a["cu"]), _d(a["rmin"]), _d(a["rmax"]),
+        float(getattr(lp, "obj_const", 0.0)), C.byref(o), C.byref(r), _d(x), _d(y))
+    d = r.as_dict()
+    d["rc"] = rc
+    d["x"], d["y"] = x, y
+    return d

@@ -1,0 +1,272 @@
+// C ABI of the GB300 PDHG engine (declared in include/igaos_pdhg.h).
+// No exception crosses this boundary: every failure becomes an
+// IGAOS_PDHG_ERR_* code plus a thread-local message.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "engine.hpp"
+
+struct igaos_pdhg_problem {
+    igx::Engine* eng;
+};
+
+namespace {
+thread_local int g_code = IGAOS_PDHG_OK;
+thread_local char g_msg[512] = "";
+
+int fail(int code, const char* msg) {
+    g_code = code;
+    std::snprintf(g_msg, sizeof(g_msg), "%s", msg);
+    return code;
+}
+int ok() {
+    g_code = IGAOS_PDHG_OK;
+    g_msg[0] = 0;
+    return IGAOS_PDHG_OK;
+}
+
+template <class F>
+int guarded(F&& f) {
+    try {
+        f();
+        return ok();
+    } catch (const igx::CudaError& e) {
+        return fail(e.code, e.what());
+    } catch (const std::bad_alloc&) {
+        return fail(IGAOS_PDHG_ERR_NOMEM, "host allocation failed");
+    } catch (const std::invalid_argument& e) {
+        return fail(IGAOS_PDHG_ERR_INVALID, e.what());
+    } catch (const std::exception& e) {
+        return fail(IGAOS_PDHG_ERR_CUDA, e.what());
+    }
+}
+
+// Structural and numeric validation of the input LP, before any upload.
+void validate(int m, int n, int64_t nnz, const int* ap, const int* ai, const double* ax,
+              const int* cp, const int* ci, const double* acx, const double* c,
+              const double* cl, const double* cu, const double* rmin, const double* rmax) {
+    auto bad = [](const char* s) { throw std::invalid_argument(s); };
+    if (m <= 0 || n <= 0) bad("problem must have at least one row and one column");
+    if (nnz < 0 || nnz > 0x7fffffffLL) bad("nnz must be in [0, 2^31)");
+    if (!ap || (nnz > 0 && (!ai || !ax))) bad("CSR arrays must not be NULL");
+    if (!c || !cl || !cu || !rmin || !rmax) bad("cost and bound arrays must not be NULL");
+    const bool have_t = cp || ci || acx;
+    if (have_t && (!cp || (nnz > 0 && (!ci || !acx))))
+        bad("pass all of cp, ci, acx or none of them");
+    if (ap[0] != 0 || ap[m] != nnz) bad("row pointer must start at 0 and end at nnz");
+    for (int i = 0; i < m; ++i)
+        if (ap[i + 1] < ap[i]) bad("row pointer must be non-decreasing");
+    for (int64_t p = 0; p < nnz; ++p) {
+        if (ai[p] < 0 || ai[p] >= n) bad("column index out of range");
+        if (!std::isfinite(ax[p])) bad("matrix values must be finite");
+    }
+    if (have_t) {
+        if (cp[0] != 0 || cp[n] != nnz) bad("column pointer must start at 0 and end at nnz");
+        for (int j = 0; j < n; ++j)
+            if (cp[j + 1] < cp[j]) bad("column pointer must be non-decreasing");
+        for (int64_t p = 0; p < nnz; ++p) {
+            if (ci[p] < 0 || ci[p] >= m) bad("row index out of range");
+            if (!std::isfinite(acx[p])) bad("matrix values must be finite");
+        }
+    }
+    for (int j = 0; j < n; ++j) {
+        if (!std::isfinite(c[j])) bad("cost must be finite");
+        if (std::isnan(cl[j]) || std::isnan(cu[j])) bad("column bounds must not be NaN");
+        if (cl[j] > cu[j]) bad("column lower bound above upper bound");
+    }
+    for (int i = 0; i < m; ++i) {
+        if (std::isnan(rmin[i]) || std::isnan(rmax[i])) bad("row bounds must not be NaN");
+        if (rmin[i] > rmax[i]) bad("row lower bound above upper bound");
+    }
+}
+
+// Stable counting sort of the CSR by column: the CSC orientation that
+// src/io/model.hpp:39-67 builds from row-ordered triplets.
+void transpose_host(int m, int n, const int* ap, const int* ai, const double* ax,
+                    std::vector<int>& cp, std::vector<int>& ci, std::vector<double>& acx) {
+    const int64_t nnz = ap[m];
+    cp.assign(n + 1, 0);
+    ci.resize(nnz);
+    acx.resize(nnz);
+    for (int64_t p = 0; p < nnz; ++p) cp[ai[p] + 1]++;
+    for (int j = 0; j < n; ++j) cp[j + 1] += cp[j];
+    std::vector<int> next(cp.begin(), cp.end() - 1);
+    for (int i = 0; i < m; ++i)
+        for (int p = ap[i]; p < ap[i + 1]; ++p) {
+            const int j = ai[p];
+            ci[next[j]] = i;
+            acx[next[j]] = ax[p];
+            ++next[j];
+        }
+}
+}  // namespace
+
+extern "C" {
+
+int igaos_pdhg_abi_version(void) { return IGAOS_PDHG_ABI_VERSION; }
+
+int igaos_pdhg_device_count(void) {
+    int c = 0;
+    if (cudaGetDeviceCount(&c) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return c;
+}
+
+void igaos_pdhg_default_options(igaos_pdhg_options* o) {
+    if (!o) return;
+    std::memset(o, 0, sizeof(*o));
+    o->time_limit_s = 120.0;
+    o->tolerance = 1e-4;
+    o->max_iterations = 500000;
+    o->seed = 0;
+    o->presolve = 1;
+    o->restarts = 0;
+    o->verbosity = 0;
+    o->precision = IGAOS_PDHG_FP64;
+    o->check_period = 64;
+    o->inner_tolerance = 1e-4;
+    o->max_refinements = 12;
+    o->use_graphs = 1;
+    o->device = -1;
+}
+
+int igaos_pdhg_last_error(char* buf, size_t len) {
+    if (buf && len > 0) {
+        std::strncpy(buf, g_msg, len - 1);
+        buf[len - 1] = 0;
+    }
+    return g_code;
+}
+
+int igaos_pdhg_create(igaos_pdhg_problem** out, int m, int n, int64_t nnz, const int* ap,
+                      const int* ai, const double* ax, const int* cp, const int* ci,
+                      const double* acx, const double* c, const double* cl, const double* cu,
+                      const double* rmin, const double* rmax, double obj_const,
+                      const igaos_pdhg_options* opt) {
+    if (!out) return fail(IGAOS_PDHG_ERR_INVALID, "out handle pointer is NULL");
+    *out = nullptr;
+    return guarded([&] {
+        validate(m, n, nnz, ap, ai, ax, cp, ci, acx, c, cl, cu, rmin, rmax);
+        if (igaos_pdhg_device_count() == 0)
+            throw igx::CudaError(IGAOS_PDHG_ERR_NODEVICE,
+                                 "no CUDA device: PDHG engine unavailable");
+        std::vector<int> tcp, tci;
+        std::vector<double> tacx;
+        if (!cp) {
+            transpose_host(m, n, ap, ai, ax, tcp, tci, tacx);
+            cp = tcp.data();
+            ci = tci.data();
+            acx = tacx.data();
+        }
+        const int dev = opt ? opt->device : -1;
+        auto* p = new igaos_pdhg_problem;
+        try {
+            p->eng = new igx::Engine(m, n, nnz, ap, ai, ax, cp, ci, acx, c, cl, cu, rmin, rmax,
+                                     obj_const, dev);
+        } catch (...) {
+            delete p;
+            throw;
+        }
+        *out = p;
+    });
+}
+
+int igaos_pdhg_solve(igaos_pdhg_problem* p, const igaos_pdhg_options* opt,
+                     igaos_pdhg_result* res, double* x, double* y) {
+    if (!p || !p->eng) return fail(IGAOS_PDHG_ERR_INVALID, "problem handle is NULL");
+    if (!res) return fail(IGAOS_PDHG_ERR_INVALID, "result pointer is NULL");
+    igaos_pdhg_options o;
+    if (opt) o = *opt;
+    else igaos_pdhg_default_options(&o);
+    if (!(o.tolerance > 0)) return fail(IGAOS_PDHG_ERR_INVALID, "tolerance must be positive");
+    if (o.precision < 0 || o.precision > 2) return fail(IGAOS_PDHG_ERR_INVALID, "unknown precision");
+    int rc = guarded([&] { p->eng->solve(o, *res, x, y); });
+    if (rc != IGAOS_PDHG_OK) {
+        std::memset(res, 0, sizeof(*res));
+        res->status = IGAOS_STATUS_ERROR;
+        res->error_code = rc;
+        std::snprintf(res->message, sizeof(res->message), "%.159s", g_msg);
+        return rc;
+    }
+    if (res->error_code != IGAOS_PDHG_OK) return fail(res->error_code, res->message);
+    return rc;
+}
+
+void igaos_pdhg_destroy(igaos_pdhg_problem* p) {
+    if (!p) return;
+    delete p->eng;
+    delete p;
+}
+
+int igaos_pdhg_solve_csr(int m, int n, int64_t nnz, const int* ap, const int* ai,
+                         const double* ax, const int* cp, const int* ci, const double* acx,
+                         const double* c, const double* cl, const double* cu,
+                         const double* rmin, const double* rmax, double obj_const,
+                         const igaos_pdhg_options* opt, igaos_pdhg_result* res, double* x,
+                         double* y) {
+    if (!res) return fail(IGAOS_PDHG_ERR_INVALID, "result pointer is NULL");
+    igaos_pdhg_problem* p = nullptr;
+    int rc = igaos_pdhg_create(&p, m, n, nnz, ap, ai, ax, cp, ci, acx, c, cl, cu, rmin, rmax,
+                               obj_const, opt);
+    if (rc != IGAOS_PDHG_OK) {
+        std::memset(res, 0, sizeof(*res));
+        res->status = IGAOS_STATUS_ERROR;
+        res->error_code = rc;
+        std::snprintf(res->message, sizeof(res->message), "%.159s", g_msg);
+        return rc;
+    }
+    rc = igaos_pdhg_solve(p, opt, res, x, y);
+    igaos_pdhg_destroy(p);
+    return rc;
+}
+
+int igaos_pdhg_get_scaling(const igaos_pdhg_problem* p, double* dr, double* dc) {
+    if (!p || !p->eng || !dr || !dc) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    std::memcpy(dr, p->eng->h_dr.data(), sizeof(double) * p->eng->m);
+    std::memcpy(dc, p->eng->h_dc.data(), sizeof(double) * p->eng->n);
+    return ok();
+}
+
+int igaos_pdhg_get_step_init(const igaos_pdhg_problem* p, double* lambda, double* eta0,
+                             double* omega0) {
+    if (!p || !p->eng) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (lambda) *lambda = p->eng->lam2;
+    if (eta0) *eta0 = p->eng->eta0;
+    if (omega0) *omega0 = p->eng->omega0;
+    return ok();
+}
+
+int igaos_pdhg_get_transpose(const igaos_pdhg_problem* p, int* cp, int* ci, double* acx) {
+    if (!p || !p->eng || !cp || !ci || !acx) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    return guarded([&] { p->eng->get_transpose(cp, ci, acx); });
+}
+
+int igaos_pdhg_iterate(igaos_pdhg_problem* p, int precision, int64_t iters, double* x, double* y,
+                       double* xavg, double* yavg, double* axcur, double* state6) {
+    if (!p || !p->eng || !x || !y || !xavg || !yavg || !axcur || !state6)
+        return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (iters < 0) return fail(IGAOS_PDHG_ERR_INVALID, "iters must be >= 0");
+    if (precision != IGAOS_PDHG_FP64 && precision != IGAOS_PDHG_FP32)
+        return fail(IGAOS_PDHG_ERR_INVALID, "precision must be FP64 or FP32");
+    return guarded([&] { p->eng->iterate(precision, iters, x, y, xavg, yavg, axcur, state6); });
+}
+
+int igaos_pdhg_evaluate(igaos_pdhg_problem* p, const double* x, const double* y, double* out6) {
+    if (!p || !p->eng || !x || !y || !out6) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    return guarded([&] { p->eng->evaluate(x, y, out6); });
+}
+
+int igaos_pdhg_spmv(igaos_pdhg_problem* p, int transpose, int precision, const double* x,
+                    double* y) {
+    if (!p || !p->eng || !x || !y) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (precision != IGAOS_PDHG_FP64 && precision != IGAOS_PDHG_FP32)
+        return fail(IGAOS_PDHG_ERR_INVALID, "precision must be FP64 or FP32");
+    return guarded([&] { p->eng->spmv(transpose, precision, x, y); });
+}
+
+}  // extern "C"

@@ -1,0 +1,840 @@
+// Host engine of the GB300 PDHG LP solver. Mirrors the control flow of the
+// reference engine (IGAOS src/pdhg/pdhg.cu:457-1156) with the per-iteration
+// work moved onto the device (kernels.cuh) and replayed from CUDA graphs.
+#include "engine.hpp"
+#include "kernels.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <type_traits>
+
+namespace igx {
+
+static const double kInf = std::numeric_limits<double>::infinity();
+
+void cuda_check(cudaError_t e, const char* what, int line) {
+    if (e == cudaSuccess) return;
+    char buf[400];
+    std::snprintf(buf, sizeof(buf), "CUDA error in PDHG engine: %s (%s, line %d)",
+                  cudaGetErrorString(e), what, line);
+    throw CudaError(e == cudaErrorMemoryAllocation ? IGAOS_PDHG_ERR_NOMEM : IGAOS_PDHG_ERR_CUDA,
+                    buf);
+}
+
+Arena::~Arena() {
+    for (void* p : ptrs_) cudaFree(p);
+}
+
+void* Arena::raw(size_t bytes) {
+    void* p = nullptr;
+    bytes = (bytes + 255) & ~size_t(255);
+    CU(cudaMalloc(&p, bytes));
+    ptrs_.push_back(p);
+    total_ += bytes;
+    return p;
+}
+
+// ---------------------------------------------------------- tile schedule
+// Lanes per row for one tile: the candidate width G minimising the busiest
+// group's work (rows are dealt round-robin to kThreads/G groups; a row costs
+// ceil(len/G) staged reads plus its shuffle tree and epilogue).
+static unsigned char pick_lanes(const int* ptr, int r0, int r1) {
+    long best = -1;
+    int best_lg = 0;
+    for (int lg = 0; lg <= 5; ++lg) {
+        const int G = 1 << lg, ngrp = kThreads >> lg;
+        long worst = 0;
+        for (int g = 0; g < ngrp && g < r1 - r0; ++g) {
+            long cost = 0;
+            for (int r = r0 + g; r < r1; r += ngrp) {
+                const int len = ptr[r + 1] - ptr[r];
+                cost += (len + G - 1) / G + lg + 2;
+            }
+            worst = std::max(worst, cost);
+        }
+        if (best < 0 || worst < best) {
+            best = worst;
+            best_lg = lg;
+        }
+    }
+    return (unsigned char)best_lg;
+}
+
+void build_tiles(const int* ptr, int rows, std::vector<int>& tile_row,
+                 std::vector<unsigned char>& tile_lg) {
+    tile_row.assign(1, 0);
+    tile_lg.clear();
+    int r = 0;
+    while (r < rows) {
+        const int len = ptr[r + 1] - ptr[r];
+        if (len > kTileNnz) {
+            tile_row.push_back(r + 1);
+            tile_lg.push_back(kLongTile);
+            ++r;
+            continue;
+        }
+        int e = r;
+        long cnt = 0;
+        while (e < rows && e - r < kTileRows) {
+            const int l = ptr[e + 1] - ptr[e];
+            if (l > kTileNnz || cnt + l > kTileNnz) break;
+            cnt += l;
+            ++e;
+        }
+        tile_row.push_back(e);
+        tile_lg.push_back(pick_lanes(ptr, r, e));
+        r = e;
+    }
+}
+
+static Sched upload_sched(Arena& ar, const int* ptr, int rows) {
+    std::vector<int> tr;
+    std::vector<unsigned char> tl;
+    build_tiles(ptr, rows, tr, tl);
+    Sched s;
+    s.ntiles = (int)tl.size();
+    s.row = ar.alloc<int>(tr.size());
+    s.lg = ar.alloc<unsigned char>(tl.size());
+    CU(cudaMemcpy(s.row, tr.data(), sizeof(int) * tr.size(), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(s.lg, tl.data(), tl.size(), cudaMemcpyHostToDevice));
+    return s;
+}
+
+static int grid_for(long long n, int per_block = kThreads, int cap = 152 * 16) {
+    long long g = (n + per_block - 1) / per_block;
+    if (g < 1) g = 1;
+    if (g > cap) g = cap;
+    return (int)g;
+}
+
+// ------------------------------------------------------------------ setup
+Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, const double* ax,
+               const int* cp, const int* ci, const double* acx, const double* c,
+               const double* cl, const double* cu, const double* rmin, const double* rmax,
+               double obj_const_, int device)
+    : m(m_), n(n_), nnz(nnz_), obj_const(obj_const_) {
+    auto t_setup = std::chrono::steady_clock::now();
+    if (device >= 0) CU(cudaSetDevice(device));
+    CU(cudaGetDevice(&device_));
+    CU(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
+    for (auto& e : ev_) CU(cudaEventCreate(&e));
+    // matrix, both orientations
+    ap_ = ar_.alloc<int>(m + 1);
+    ai_ = ar_.alloc<int>(nnz);
+    ax_ = ar_.alloc<double>(nnz);
+    cp_ = ar_.alloc<int>(n + 1);
+    ci_ = ar_.alloc<int>(nnz);
+    acx_ = ar_.alloc<double>(nnz);
+    ax32_ = ar_.alloc<float>(nnz);
+    acx32_ = ar_.alloc<float>(nnz);
+    CU(cudaMemcpyAsync(ap_, ap, sizeof(int) * (m + 1), cudaMemcpyHostToDevice, st_));
+    CU(cudaMemcpyAsync(ai_, ai, sizeof(int) * nnz, cudaMemcpyHostToDevice, st_));
+    CU(cudaMemcpyAsync(ax_, ax, sizeof(double) * nnz, cudaMemcpyHostToDevice, st_));
+    CU(cudaMemcpyAsync(cp_, cp, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st_));
+    CU(cudaMemcpyAsync(ci_, ci, sizeof(int) * nnz, cudaMemcpyHostToDevice, st_));
+    CU(cudaMemcpyAsync(acx_, acx, sizeof(double) * nnz, cudaMemcpyHostToDevice, st_));
+    sA_ = upload_sched(ar_, ap, m);
+    sAT_ = upload_sched(ar_, cp, n);
+    // vectors
+    auto vec = [&](const double* h, int len) {
+        double* d = ar_.alloc<double>(len);
+        CU(cudaMemcpyAsync(d, h, sizeof(double) * len, cudaMemcpyHostToDevice, st_));
+        return d;
+    };
+    base_.c = vec(c, n);
+    base_.cl = vec(cl, n);
+    base_.cu = vec(cu, n);
+    base_.rmin = vec(rmin, m);
+    base_.rmax = vec(rmax, m);
+    base_.cmax = 0.0;
+    for (int j = 0; j < n; ++j) base_.cmax = std::max(base_.cmax, std::fabs(c[j]));
+    base_.sc = ar_.alloc<double>(n);
+    base_.scl = ar_.alloc<double>(n);
+    base_.scu = ar_.alloc<double>(n);
+    base_.srmin = ar_.alloc<double>(m);
+    base_.srmax = ar_.alloc<double>(m);
+    base_.fc = ar_.alloc<float>(n);
+    base_.fcl = ar_.alloc<float>(n);
+    base_.fcu = ar_.alloc<float>(n);
+    base_.frmin = ar_.alloc<float>(m);
+    base_.frmax = ar_.alloc<float>(m);
+    dr_ = ar_.alloc<double>(m);
+    dc_ = ar_.alloc<double>(n);
+    // control + scratch
+    ctl_ = ar_.alloc<DevCtl>(1);
+    met_ = ar_.alloc<DevMetrics>(2);
+    CU(cudaMemsetAsync(ctl_, 0, sizeof(DevCtl), st_));
+    CU(cudaMallocHost(&h_ctl_, sizeof(DevCtl)));
+    CU(cudaMallocHost(&h_met_, 2 * sizeof(DevMetrics)));
+    CU(cudaMallocHost(&h_scal_, 16 * sizeof(double)));
+    std::memset(h_ctl_, 0, sizeof(DevCtl));
+    red_blocks_ = grid_for(std::max(m, n), kThreads, 152 * 4);
+    const int kkt_blocks = std::max(std::max(sA_.ntiles, sAT_.ntiles), red_blocks_);
+    kkt_part_ = ar_.alloc<double>((size_t)2 * kkt_blocks * 4);
+    red_part_ = ar_.alloc<double>((size_t)2 * red_blocks_ + 8);
+    scal_ = ar_.alloc<double>(16);
+    ticket_ = ar_.alloc<unsigned int>(4);
+    flag_ = ar_.alloc<int>(4);
+    CU(cudaMemsetAsync(ticket_, 0, 4 * sizeof(unsigned int), st_));
+    tmp_n_ = ar_.alloc<double>(n);
+    tmp_n2_ = ar_.alloc<double>(n);
+    tmp_m_ = ar_.alloc<double>(m);
+    tmp_m2_ = ar_.alloc<double>(m);
+
+    setup_scaling();
+    power_iteration();
+    // eta0, omega0 (src/pdhg/pdhg.cu:642-663), from the scaled cost and
+    // row bounds, in the reference's summation order.
+    eta0 = 1.2 / std::sqrt(lam2);
+    omega0 = 1.0;
+    {
+        double cn = 0.0, qn = 0.0;
+        for (int j = 0; j < n; ++j) {
+            const double s = c[j] * h_dc[j] / 1.0;
+            cn += s * s;
+        }
+        for (int i = 0; i < m; ++i) {
+            const double hi = rmax[i] / h_dr[i], lo = rmin[i] / h_dr[i];
+            const double q = std::isfinite(hi) ? hi : (std::isfinite(lo) ? lo : 0.0);
+            qn += q * q;
+        }
+        if (cn > 1e-24 && qn > 1e-24) omega0 = std::clamp(std::sqrt(cn / qn), 0.3, 3.0);
+    }
+    CU(cudaStreamSynchronize(st_));
+    setup_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() -
+                                                         t_setup).count();
+}
+
+Engine::~Engine() {
+    for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
+    for (auto& e : ev_)
+        if (e) cudaEventDestroy(e);
+    if (h_ctl_) cudaFreeHost(h_ctl_);
+    if (h_met_) cudaFreeHost(h_met_);
+    if (h_scal_) cudaFreeHost(h_scal_);
+    if (st_) cudaStreamDestroy(st_);
+}
+
+// Ruiz equilibration (src/pdhg/pdhg.cu:472-492) and the scaled problem
+// (:499-513), all on the device, bit-identical to the host loops.
+void Engine::setup_scaling() {
+    const int gr = grid_for((long long)m * 32), gc = grid_for((long long)n * 32);
+    const int gr_full = (int)(((long long)m * 32 + kThreads - 1) / kThreads);
+    const int gc_full = (int)(((long long)n * 32 + kThreads - 1) / kThreads);
+    (void)gr;
+    (void)gc;
+    k_fill<<<grid_for(m), kThreads, 0, st_>>>(m, 1.0, dr_);
+    k_fill<<<grid_for(n), kThreads, 0, st_>>>(n, 1.0, dc_);
+    for (int sweep = 0; sweep < 10; ++sweep) {
+        k_ruiz_rows<<<gr_full, kThreads, 0, st_>>>(m, ap_, ai_, ax_, dc_, dr_);
+        k_ruiz_cols<<<gc_full, kThreads, 0, st_>>>(n, cp_, ci_, acx_, dr_, dc_);
+    }
+    k_fix_scale<<<grid_for(m), kThreads, 0, st_>>>(m, dr_);
+    k_fix_scale<<<grid_for(n), kThreads, 0, st_>>>(n, dc_);
+    k_scale_matrix<<<gr_full, kThreads, 0, st_>>>(m, ap_, ai_, ax_, ax32_, dr_, dc_, 1);
+    k_scale_matrix<<<gc_full, kThreads, 0, st_>>>(n, cp_, ci_, acx_, acx32_, dr_, dc_, 0);
+    k_scale_vec<<<grid_for(m), kThreads, 0, st_>>>(m, base_.rmin, dr_, 0, base_.srmin, base_.frmin);
+    k_scale_vec<<<grid_for(m), kThreads, 0, st_>>>(m, base_.rmax, dr_, 0, base_.srmax, base_.frmax);
+    k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.c, dc_, 1, base_.sc, base_.fc);
+    k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cl, dc_, 0, base_.scl, base_.fcl);
+    k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cu, dc_, 0, base_.scu, base_.fcu);
+    CU(cudaGetLastError());
+    h_dr.resize(m);
+    h_dc.resize(n);
+    CU(cudaMemcpyAsync(h_dr.data(), dr_, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(h_dc.data(), dc_, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+    CU(cudaStreamSynchronize(st_));
+}
+
+template <> Csr<double> Engine::csrA<double>() const { return Csr<double>{ap_, ai_, ax_, m}; }
+template <> Csr<double> Engine::csrAT<double>() const { return Csr<double>{cp_, ci_, acx_, n}; }
+template <> Csr<float> Engine::csrA<float>() const { return Csr<float>{ap_, ai_, ax32_, m}; }
+template <> Csr<float> Engine::csrAT<float>() const { return Csr<float>{cp_, ci_, acx32_, n}; }
+
+template <typename T>
+void Engine::spmv_dev(bool transpose, const T* x, T* y) {
+    if (transpose)
+        k_spmv<T, T><<<sAT_.ntiles, kThreads, 0, st_>>>(sAT_.view(), csrAT<T>(), x, y);
+    else
+        k_spmv<T, T><<<sA_.ntiles, kThreads, 0, st_>>>(sA_.view(), csrA<T>(), x, y);
+    CU(cudaGetLastError());
+}
+
+// lambda ~ ||A~||_2^2 by 30 power iterations (src/pdhg/pdhg.cu:605-631),
+// norms and normalisation kept on the device.
+void Engine::power_iteration() {
+    double* v = tmp_n_;
+    double* w = tmp_n2_;
+    double* tm = tmp_m_;
+    k_fill<<<grid_for(n), kThreads, 0, st_>>>(n, 1.0 / std::sqrt((double)n), v);
+    CU(cudaMemsetAsync(flag_, 0, sizeof(int), st_));
+    for (int it = 0; it < 30; ++it) {
+        spmv_dev<double>(false, v, tm);
+        spmv_dev<double>(true, tm, w);
+        k_sumsq<<<red_blocks_, kThreads, 0, st_>>>(NormArgs{w, n, red_part_, scal_, ticket_ + 1}, 1);
+        k_power_normalise<<<grid_for(n), kThreads, 0, st_>>>(n, w, v, scal_, flag_);
+    }
+    spmv_dev<double>(false, v, tm);
+    k_sumsq<<<red_blocks_, kThreads, 0, st_>>>(NormArgs{tm, m, red_part_, scal_ + 1, ticket_ + 1}, 1);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(h_scal_, scal_, 2 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CU(cudaStreamSynchronize(st_));
+    const double na = h_scal_[1];
+    lam2 = na * na;
+    if (!(lam2 > 0) || !std::isfinite(lam2)) lam2 = 1.0;
+}
+
+// -------------------------------------------------------------- workspace
+template <> Work<double>& Engine::work<double>() { return w64_; }
+template <> Work<float>& Engine::work<float>() { return w32_; }
+
+template <typename T>
+void Engine::ensure_work() {
+    bool& have = std::is_same<T, double>::value ? have64_ : have32_;
+    if (have) return;
+    Work<T>& w = work<T>();
+    for (int s = 0; s < 2; ++s) {
+        w.x[s] = ar_.alloc<T>(n);
+        w.xavg[s] = ar_.alloc<T>(n);
+        w.y[s] = ar_.alloc<T>(m);
+        w.yavg[s] = ar_.alloc<T>(m);
+        w.axc[s] = ar_.alloc<T>(m);
+    }
+    w.xbar = ar_.alloc<T>(n);
+    w.xb = ar_.alloc<T>(n);
+    w.pesx = ar_.alloc<T>(n);
+    w.yb = ar_.alloc<T>(m);
+    w.pesy = ar_.alloc<T>(m);
+    w.part_p = ar_.alloc<double>(sAT_.ntiles);
+    w.part_d = ar_.alloc<double>(2 * (size_t)sA_.ntiles);
+    have = true;
+}
+
+template <typename T> struct VecSel;
+template <> struct VecSel<double> {
+    static const double* c(const Vecs& v) { return v.sc; }
+    static const double* l(const Vecs& v) { return v.scl; }
+    static const double* u(const Vecs& v) { return v.scu; }
+    static const double* rl(const Vecs& v) { return v.srmin; }
+    static const double* ru(const Vecs& v) { return v.srmax; }
+};
+template <> struct VecSel<float> {
+    static const float* c(const Vecs& v) { return v.fc; }
+    static const float* l(const Vecs& v) { return v.fcl; }
+    static const float* u(const Vecs& v) { return v.fcu; }
+    static const float* rl(const Vecs& v) { return v.frmin; }
+    static const float* ru(const Vecs& v) { return v.frmax; }
+};
+
+// Enqueues `count` line-search attempts (2 launches each). With graphs the
+// sequence is captured once per (precision, count, vector set) and replayed.
+template <typename T>
+void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
+    Work<T>& w = work<T>();
+    PrimalArgs<T> pa;
+    pa.ts = sAT_.view();
+    pa.AT = csrAT<T>();
+    pa.y[0] = w.y[0];
+    pa.y[1] = w.y[1];
+    pa.c = VecSel<T>::c(v);
+    pa.lo = VecSel<T>::l(v);
+    pa.hi = VecSel<T>::u(v);
+    for (int s = 0; s < 2; ++s) {
+        pa.x[s] = w.x[s];
+        pa.xavg[s] = w.xavg[s];
+    }
+    pa.xbar = w.xbar;
+    pa.part = w.part_p;
+    pa.ctl = ctl_;
+    DualArgs<T> da;
+    da.ts = sA_.view();
+    da.A = csrA<T>();
+    da.xbar = w.xbar;
+    da.rmin = VecSel<T>::rl(v);
+    da.rmax = VecSel<T>::ru(v);
+    for (int s = 0; s < 2; ++s) {
+        da.y[s] = w.y[s];
+        da.axc[s] = w.axc[s];
+        da.yavg[s] = w.yavg[s];
+    }
+    da.part = w.part_d;
+    da.part_primal = w.part_p;
+    da.n_primal = sAT_.ntiles;
+    da.ctl = ctl_;
+    auto enqueue = [&](int cnt) {
+        for (int a = 0; a < cnt; ++a) {
+            k_primal<T><<<sAT_.ntiles, kThreads, 0, st_>>>(pa);
+            k_dual<T><<<sA_.ntiles, kThreads, 0, st_>>>(da);
+        }
+    };
+    if (!graphs) {
+        enqueue(count);
+        CU(cudaGetLastError());
+        return;
+    }
+    // key: precision, attempt count, vector set
+    const GraphKey key{std::is_same<T, double>::value ? 1 : 2, count,
+                       (uintptr_t)VecSel<T>::c(v)};
+    auto it = graphs_.find(key);
+    if (it == graphs_.end()) {
+        cudaGraph_t g;
+        CU(cudaStreamBeginCapture(st_, cudaStreamCaptureModeThreadLocal));
+        enqueue(count);
+        CU(cudaStreamEndCapture(st_, &g));
+        cudaGraphExec_t ge;
+        CU(cudaGraphInstantiate(&ge, g, 0));
+        cudaGraphDestroy(g);
+        it = graphs_.emplace(key, ge).first;
+    }
+    CU(cudaGraphLaunch(it->second, st_));
+}
+
+void Engine::upload_ctl() {
+    CU(cudaMemcpyAsync(ctl_, h_ctl_, sizeof(DevCtl), cudaMemcpyHostToDevice, st_));
+}
+void Engine::download_ctl() {
+    CU(cudaMemcpyAsync(h_ctl_, ctl_, sizeof(DevCtl), cudaMemcpyDeviceToHost, st_));
+    CU(cudaStreamSynchronize(st_));
+}
+double Engine::elapsed() const {
+    return std::chrono::duration<double>(std::chrono::steady_clock::now() - t0_).count();
+}
+
+// Launch attempts until the device raises `stop` (iteration k_stop accepted
+// or NaN). The first batch covers the accepted iterations still needed plus
+// the rejections the history predicts; the rest are topped up in small
+// batches (a stopped launch is a no-op).
+template <typename T>
+void Engine::run_until_stop(const Vecs& v, bool graphs, LoopOut& out) {
+    for (;;) {
+        const long long need = h_ctl_->k_stop - (h_ctl_->k - 1);
+        const double rej = h_ctl_->accepted > 0
+                               ? (double)(h_ctl_->attempts - h_ctl_->accepted) / h_ctl_->attempts
+                               : 0.0;
+        long long want = (long long)std::ceil((double)need * (1.0 + 1.2 * rej)) + (rej > 0 ? 1 : 0);
+        int cnt = want <= 1 ? 1 : want <= 4 ? 4 : want <= 8 ? 8 : want <= 16 ? 16
+                  : want <= 32 ? 32 : want <= 64 ? 64 : want <= 72 ? 72 : want <= 80 ? 80 : 96;
+        CU(cudaEventRecord(ev_[2], st_));
+        launch_attempts<T>(cnt, v, graphs);
+        CU(cudaEventRecord(ev_[3], st_));
+        download_ctl();
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, ev_[2], ev_[3]));
+        attempt_ms_ += ms;
+        if (h_ctl_->stop) break;
+    }
+    out.attempts = h_ctl_->attempts;
+}
+
+template <typename T>
+void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* y1, int ncand) {
+    KktArgs<T> ka;
+    ka.tsA = sA_.view();
+    ka.tsAT = sAT_.view();
+    ka.A = csrA<T>();
+    ka.AT = csrAT<T>();
+    ka.x[0] = x0;
+    ka.y[0] = y0;
+    ka.x[1] = x1;
+    ka.y[1] = y1;
+    ka.dr = dr_;
+    ka.dc = dc_;
+    ka.c = v.c;
+    ka.cl = v.cl;
+    ka.cu = v.cu;
+    ka.rmin = v.rmin;
+    ka.rmax = v.rmax;
+    ka.cmax = v.cmax;
+    ka.part = kkt_part_;
+    ka.out = met_;
+    ka.ticket = ticket_ + 2;
+    k_kkt_rows<T><<<dim3(sA_.ntiles, ncand), kThreads, 0, st_>>>(ka);
+    k_kkt_cols<T><<<dim3(sAT_.ntiles, ncand), kThreads, 0, st_>>>(ka);
+    k_kkt_rowdual<T><<<dim3(red_blocks_, ncand), kThreads, 0, st_>>>(ka, m);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(h_met_, met_, ncand * sizeof(DevMetrics), cudaMemcpyDeviceToHost, st_));
+    CU(cudaStreamSynchronize(st_));
+}
+
+// The reference iteration loop with its 64-iteration checks: termination,
+// incumbent, rollback, restart and primal weight (src/pdhg/pdhg.cu:665-1085).
+template <typename T>
+LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
+    ensure_work<T>();
+    Work<T>& w = work<T>();
+    LoopOut out;
+    const size_t nb = sizeof(T) * n, mb = sizeof(T) * m;
+    CU(cudaMemsetAsync(w.x[0], 0, nb, st_));
+    CU(cudaMemsetAsync(w.xavg[0], 0, nb, st_));
+    CU(cudaMemsetAsync(w.y[0], 0, mb, st_));
+    CU(cudaMemsetAsync(w.yavg[0], 0, mb, st_));
+    CU(cudaMemsetAsync(w.axc[0], 0, mb, st_));
+    std::memset(h_ctl_, 0, sizeof(DevCtl));
+    h_ctl_->eta = o.eta_init;
+    h_ctl_->omega = o.omega_init;
+    h_ctl_->k = 1;
+    const int CHECK = o.check > 0 ? o.check : 64;
+    const long long MAXIT = o.maxit;
+    h_ctl_->k_stop = std::min<long long>(CHECK, MAXIT);
+    upload_ctl();
+
+    double epoch_kkt = -1.0, prev_cand = kInf;
+    long long epoch_start = 0, last_rollback = 0;
+    bool have_pe = false, have_last = false, have_inc = false;
+    double inc_op = 0.0;
+    DevMetrics inc{};
+    out.status = IGAOS_STATUS_ITERATION_LIMIT;
+    long long k_done = 0;
+    auto passes = [&](const DevMetrics& t) {
+        return t.pinf <= o.tol && t.dinf <= o.tol && t.prow <= o.tol && std::isfinite(t.gap) &&
+               t.gap <= o.tol;
+    };
+    while (k_done < MAXIT) {
+        run_until_stop<T>(v, o.graphs, out);
+        k_done = h_ctl_->k - 1;
+        out.spmvs = 2 * h_ctl_->attempts;
+        if (h_ctl_->nan_flag) {
+            out.numeric_failure = true;
+            out.status = IGAOS_STATUS_ERROR;
+            break;
+        }
+        if (k_done % CHECK == 0) {
+            ++out.checks;
+            const int p = h_ctl_->parity;
+            kkt<T>(v, w.x[p], w.y[p], w.xavg[p], w.yavg[p], 2);
+            const DevMetrics mc = h_met_[0], ma = h_met_[1];
+            const double ec = mc.finite ? mc.err : kInf;
+            const double ea = ma.finite ? ma.err : kInf;
+            out.last = (ec <= ea) ? mc : ma;
+            out.last_is_avg = (ea < ec);
+            have_last = true;
+            if (o.verbosity > 0 && k_done % (CHECK * 40) == 0)
+                std::fprintf(stderr, "[pdhg-gb300] k=%lld pinf=%.3e dinf=%.3e gap=%.3e\n", k_done,
+                             out.last.pinf, out.last.dinf, out.last.gap);
+            if (passes(mc)) { out.last = mc; out.last_is_avg = false; out.status = IGAOS_STATUS_NEAR_OPTIMAL; break; }
+            if (passes(ma)) { out.last = ma; out.last_is_avg = true; out.status = IGAOS_STATUS_NEAR_OPTIMAL; break; }
+            // incumbent (src/pdhg/pdhg.cu:937-958)
+            int inc_src = -1;
+            for (int cnd = 0; cnd < 2; ++cnd) {
+                const DevMetrics& t = cnd ? ma : mc;
+                if (t.pinf <= 1e-4 && std::isfinite(t.op) && (!have_inc || t.op < inc_op)) {
+                    have_inc = true;
+                    inc_op = t.op;
+                    inc = t;
+                    inc_src = cnd;
+                }
+            }
+            if (inc_src >= 0) {
+                CU(cudaMemcpyAsync(w.xb, inc_src ? w.xavg[p] : w.x[p], nb, cudaMemcpyDeviceToDevice, st_));
+                CU(cudaMemcpyAsync(w.yb, inc_src ? w.yavg[p] : w.y[p], mb, cudaMemcpyDeviceToDevice, st_));
+            }
+            // rollback (src/pdhg/pdhg.cu:965-988)
+            if (mc.pinf >= 0.5 && have_inc && k_done - last_rollback > 2000) {
+                CU(cudaMemcpyAsync(w.x[p], w.xb, nb, cudaMemcpyDeviceToDevice, st_));
+                CU(cudaMemcpyAsync(w.y[p], w.yb, mb, cudaMemcpyDeviceToDevice, st_));
+                CU(cudaMemcpyAsync(w.xavg[p], w.xb, nb, cudaMemcpyDeviceToDevice, st_));
+                CU(cudaMemcpyAsync(w.yavg[p], w.yb, mb, cudaMemcpyDeviceToDevice, st_));
+                h_ctl_->eta = std::min(h_ctl_->eta, 0.5 * o.eta0);
+                h_ctl_->hn = 0;
+                epoch_start = k_done;
+                epoch_kkt = -1.0;
+                prev_cand = kInf;
+                spmv_dev<T>(false, w.x[p], w.axc[p]);
+                ++out.spmvs;
+                last_rollback = k_done;
+            }
+            // restart + primal weight (src/pdhg/pdhg.cu:1001-1075)
+            const double cand = std::min(ec, ea);
+            if (epoch_kkt < 0.0) {
+                epoch_kkt = cand;
+                prev_cand = cand;
+            }
+            const long long t_epoch = k_done - epoch_start;
+            const bool restart_now =
+                (std::isfinite(cand) && std::isfinite(epoch_kkt) && epoch_kkt > 0.0 &&
+                 (cand <= 0.2 * epoch_kkt ||
+                  (cand <= 0.8 * epoch_kkt && std::isfinite(prev_cand) && cand > prev_cand))) ||
+                (double)t_epoch >= 0.36 * (double)k_done;
+            prev_cand = cand;
+            if (restart_now) {
+                ++out.restarts;
+                if (ea < ec) {
+                    CU(cudaMemcpyAsync(w.x[p], w.xavg[p], nb, cudaMemcpyDeviceToDevice, st_));
+                    CU(cudaMemcpyAsync(w.y[p], w.yavg[p], mb, cudaMemcpyDeviceToDevice, st_));
+                }
+                CU(cudaMemcpyAsync(w.xavg[p], w.x[p], nb, cudaMemcpyDeviceToDevice, st_));
+                CU(cudaMemcpyAsync(w.yavg[p], w.y[p], mb, cudaMemcpyDeviceToDevice, st_));
+                h_ctl_->hn = 0;
+                epoch_start = k_done;
+                epoch_kkt = cand;
+                prev_cand = kInf;
+                spmv_dev<T>(false, w.x[p], w.axc[p]);
+                ++out.spmvs;
+                if (have_pe) {
+                    k_diffnorms<T><<<red_blocks_, kThreads, 0, st_>>>(
+                        n, w.x[p], w.pesx, m, w.y[p], w.pesy, red_part_, scal_, ticket_ + 1);
+                    CU(cudaGetLastError());
+                    CU(cudaMemcpyAsync(h_scal_, scal_, 2 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+                    CU(cudaStreamSynchronize(st_));
+                    const double dxn = h_scal_[0], dyn = h_scal_[1];
+                    if (dxn > 1e-24 && dyn > 1e-24) {
+                        const double om = std::sqrt(h_ctl_->omega * std::sqrt(dyn / dxn));
+                        if (std::isfinite(om) && om > 0.0)
+                            h_ctl_->omega = std::clamp(om, 1e-6, 1e6);
+                    }
+                }
+                have_pe = true;
+                CU(cudaMemcpyAsync(w.pesx, w.x[p], nb, cudaMemcpyDeviceToDevice, st_));
+                CU(cudaMemcpyAsync(w.pesy, w.y[p], mb, cudaMemcpyDeviceToDevice, st_));
+                if (o.verbosity > 1)
+                    std::fprintf(stderr, "[pdhg-gb300] restart @k=%lld t=%lld r=%.3e eta=%.3e om=%.3e\n",
+                                 k_done, t_epoch, cand, h_ctl_->eta, h_ctl_->omega);
+            }
+            out.spmvs += 4;
+            if (o.deadline > 0 && elapsed() > o.deadline) {
+                out.status = IGAOS_STATUS_TIME_LIMIT;
+                break;
+            }
+        }
+        if (k_done >= MAXIT) break;
+        h_ctl_->k_stop = std::min<long long>((k_done / CHECK + 1) * CHECK, MAXIT);
+        h_ctl_->stop = 0;
+        upload_ctl();
+    }
+    out.iters = k_done;
+    out.attempts = h_ctl_->attempts;
+    out.eta = h_ctl_->eta;
+    out.omega = h_ctl_->omega;
+    out.parity = h_ctl_->parity;
+    if (!have_last && !out.numeric_failure) {
+        // no check ran (fewer than CHECK iterations): evaluate the last iterate
+        const int p = h_ctl_->parity;
+        kkt<T>(v, w.x[p], w.y[p], w.x[p], w.y[p], 1);
+        out.last = h_met_[0];
+        out.last_is_avg = false;
+        out.spmvs += 2;
+    }
+    auto certified = [&](const DevMetrics& t) {
+        return t.pinf <= o.tol && t.prow <= o.tol && std::isfinite(t.gap) && t.gap <= o.tol;
+    };
+    if (out.status == IGAOS_STATUS_ITERATION_LIMIT && certified(out.last))
+        out.status = IGAOS_STATUS_NEAR_OPTIMAL;
+    if (!certified(out.last) && have_inc && inc.pinf <= o.tol && std::isfinite(inc.op) &&
+        (inc.op < out.last.op || out.last.pinf > o.tol)) {
+        out.last = inc;
+        out.use_inc = true;
+        out.last_is_avg = false;
+    }
+    return out;
+}
+
+template <typename T>
+void Engine::fetch_scaled(const T* src, int len, double* dst) {
+    if (std::is_same<T, double>::value) {
+        CU(cudaMemcpyAsync(dst, src, sizeof(double) * len, cudaMemcpyDeviceToHost, st_));
+    } else {
+        double* staging = (len == n) ? tmp_n_ : tmp_m_;
+        k_convert<T, double><<<grid_for(len), kThreads, 0, st_>>>(len, src, staging);
+        CU(cudaGetLastError());
+        CU(cudaMemcpyAsync(dst, staging, sizeof(double) * len, cudaMemcpyDeviceToHost, st_));
+    }
+    CU(cudaStreamSynchronize(st_));
+}
+
+// -------------------------------------------------------------------- solve
+static void fill_message(igaos_pdhg_result& r, const char* s) {
+    std::snprintf(r.message, sizeof(r.message), "%s", s);
+}
+
+void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x, double* y) {
+    std::memset(&r, 0, sizeof(r));
+    r.status = IGAOS_STATUS_ERROR;
+    r.setup_time_ms = setup_ms;
+    if (o.precision == IGAOS_PDHG_FP32_REFINE) {
+        solve_refine(o, r, x, y);
+        return;
+    }
+    t0_ = std::chrono::steady_clock::now();
+    attempt_ms_ = 0;
+    CU(cudaEventRecord(ev_[0], st_));
+    LoopOpts lo;
+    lo.tol = o.tolerance;
+    const bool finite_tl = o.time_limit_s > 0 && o.time_limit_s < 1e6;
+    lo.deadline = finite_tl ? o.time_limit_s : 0.0;
+    lo.maxit = finite_tl ? 20000000LL : (long long)o.max_iterations;
+    lo.check = o.check_period > 0 ? o.check_period : 64;
+    lo.verbosity = o.verbosity;
+    lo.graphs = o.use_graphs != 0;
+    lo.eta_init = eta0;
+    lo.eta0 = eta0;
+    lo.omega_init = omega0;
+    LoopOut out;
+    std::vector<double> hx(n), hy(m);
+    if (o.precision == IGAOS_PDHG_FP32) {
+        out = loop<float>(base_, lo);
+        Work<float>& w = w32_;
+        const int p = out.parity;
+        const float* fx = out.use_inc ? w.xb : (out.last_is_avg ? w.xavg[p] : w.x[p]);
+        const float* fy = out.use_inc ? w.yb : (out.last_is_avg ? w.yavg[p] : w.y[p]);
+        fetch_scaled<float>(fx, n, hx.data());
+        fetch_scaled<float>(fy, m, hy.data());
+    } else {
+        out = loop<double>(base_, lo);
+        Work<double>& w = w64_;
+        const int p = out.parity;
+        const double* fx = out.use_inc ? w.xb : (out.last_is_avg ? w.xavg[p] : w.x[p]);
+        const double* fy = out.use_inc ? w.yb : (out.last_is_avg ? w.yavg[p] : w.y[p]);
+        fetch_scaled<double>(fx, n, hx.data());
+        fetch_scaled<double>(fy, m, hy.data());
+    }
+    const double secs = elapsed();
+    CU(cudaEventRecord(ev_[1], st_));
+    CU(cudaEventSynchronize(ev_[1]));
+    {
+        float ms = 0.f;
+        CU(cudaEventElapsedTime(&ms, ev_[0], ev_[1]));
+        r.device_time_ms = ms;
+        r.attempt_time_ms = attempt_ms_;
+    }
+    r.status = out.status;
+    r.objective = out.last.op + obj_const;
+    r.pinf = out.last.pinf;
+    r.dinf = out.last.dinf;
+    r.rel_gap = out.last.gap;
+    r.prow = out.last.prow;
+    r.iterations = out.iters;
+    r.attempts = out.attempts;
+    r.kkt_checks = out.checks;
+    r.restarts = out.restarts;
+    r.kkt_passes = out.spmvs / 2;
+    r.solve_time_ms = secs * 1000.0;
+    if (out.numeric_failure) {
+        r.error_code = IGAOS_PDHG_ERR_NUMERIC;
+        fill_message(r, "numerical failure: NaN/Inf in the PDHG iterates");
+    } else if (out.status == IGAOS_STATUS_NEAR_OPTIMAL) {
+        fill_message(r, "converged: residuals + duality gap @tol");
+    } else if (out.status == IGAOS_STATUS_TIME_LIMIT) {
+        fill_message(r, "wall-clock budget exhausted");
+    } else {
+        fill_message(r, out.last.pinf <= o.tolerance && out.last.dinf <= o.tolerance
+                            ? "iteration cap: residuals @tol but gap not certified (dual bound "
+                              "-inf or > tol)"
+                            : "iteration cap reached before tolerance");
+    }
+    if (x)
+        for (int j = 0; j < n; ++j) x[j] = hx[j] * h_dc[j];
+    if (y)
+        for (int i = 0; i < m; ++i) y[i] = 1.0 * hy[i] / h_dr[i];
+}
+
+// --------------------------------------------------------- inspection API
+void Engine::get_transpose(int* cp, int* ci, double* acx) {
+    CU(cudaMemcpyAsync(cp, cp_, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(ci, ci_, sizeof(int) * nnz, cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(acx, acx_, sizeof(double) * nnz, cudaMemcpyDeviceToHost, st_));
+    CU(cudaStreamSynchronize(st_));
+}
+
+template <typename T>
+static void upload_as(cudaStream_t st, T* dst, const double* src, int len, double* staging) {
+    if (std::is_same<T, double>::value) {
+        CU(cudaMemcpyAsync(dst, src, sizeof(double) * len, cudaMemcpyHostToDevice, st));
+    } else {
+        CU(cudaMemcpyAsync(staging, src, sizeof(double) * len, cudaMemcpyHostToDevice, st));
+        k_convert<double, T><<<grid_for(len), kThreads, 0, st>>>(len, staging, dst);
+        CU(cudaGetLastError());
+    }
+    CU(cudaStreamSynchronize(st));
+}
+
+void Engine::iterate(int precision, long long iters, double* x, double* y, double* xavg,
+                     double* yavg, double* axc, double* st6) {
+    auto run = [&](auto tag) {
+        using T = decltype(tag);
+        ensure_work<T>();
+        Work<T>& w = work<T>();
+        upload_as<T>(st_, w.x[0], x, n, tmp_n_);
+        upload_as<T>(st_, w.xavg[0], xavg, n, tmp_n_);
+        upload_as<T>(st_, w.y[0], y, m, tmp_m_);
+        upload_as<T>(st_, w.yavg[0], yavg, m, tmp_m_);
+        upload_as<T>(st_, w.axc[0], axc, m, tmp_m_);
+        std::memset(h_ctl_, 0, sizeof(DevCtl));
+        h_ctl_->eta = st6[0];
+        h_ctl_->omega = st6[1];
+        h_ctl_->k = (long long)st6[2];
+        h_ctl_->hn = (long long)st6[3];
+        h_ctl_->k_stop = h_ctl_->k + iters - 1;
+        upload_ctl();
+        LoopOut out;
+        if (iters > 0) run_until_stop<T>(base_, false, out);
+        else download_ctl();
+        const int p = h_ctl_->parity;
+        fetch_scaled<T>(w.x[p], n, x);
+        fetch_scaled<T>(w.xavg[p], n, xavg);
+        fetch_scaled<T>(w.y[p], m, y);
+        fetch_scaled<T>(w.yavg[p], m, yavg);
+        fetch_scaled<T>(w.axc[p], m, axc);
+        st6[0] = h_ctl_->eta;
+        st6[1] = h_ctl_->omega;
+        st6[2] = (double)h_ctl_->k;
+        st6[3] = (double)h_ctl_->hn;
+        st6[4] = (double)h_ctl_->attempts;
+        st6[5] = (double)p;
+    };
+    if (precision == IGAOS_PDHG_FP64) run(double());
+    else run(float());
+}
+
+void Engine::evaluate(const double* x, const double* y, double* out6) {
+    // scaled copies: x~ = x / dc, y~ = y * dr
+    std::vector<double> xs(n), ys(m);
+    for (int j = 0; j < n; ++j) xs[j] = x[j] / h_dc[j];
+    for (int i = 0; i < m; ++i) ys[i] = y[i] * h_dr[i];
+    CU(cudaMemcpyAsync(tmp_n2_, xs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st_));
+    CU(cudaMemcpyAsync(tmp_m2_, ys.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st_));
+    kkt<double>(base_, tmp_n2_, tmp_m2_, tmp_n2_, tmp_m2_, 1);
+    const DevMetrics& t = h_met_[0];
+    out6[0] = t.pinf;
+    out6[1] = t.dinf;
+    out6[2] = t.gap;
+    out6[3] = t.op;
+    out6[4] = t.od;
+    out6[5] = t.prow;
+}
+
+void Engine::spmv(int transpose, int precision, const double* x, double* y) {
+    const int lin = transpose ? m : n, lout = transpose ? n : m;
+    if (precision == IGAOS_PDHG_FP64) {
+        double* dx = transpose ? tmp_m_ : tmp_n_;
+        double* dy = transpose ? tmp_n2_ : tmp_m2_;
+        CU(cudaMemcpyAsync(dx, x, sizeof(double) * lin, cudaMemcpyHostToDevice, st_));
+        spmv_dev<double>(transpose != 0, dx, dy);
+        CU(cudaMemcpyAsync(y, dy, sizeof(double) * lout, cudaMemcpyDeviceToHost, st_));
+        CU(cudaStreamSynchronize(st_));
+    } else {
+        ensure_work<float>();
+        float* fx = transpose ? w32_.y[0] : w32_.x[0];
+        float* fy = transpose ? w32_.x[1] : w32_.y[1];
+        upload_as<float>(st_, fx, x, lin, transpose ? tmp_m_ : tmp_n_);
+        spmv_dev<float>(transpose != 0, fx, fy);
+        k_convert<float, double><<<grid_for(lout), kThreads, 0, st_>>>(lout, fy, transpose ? tmp_n2_ : tmp_m2_);
+        CU(cudaMemcpyAsync(y, transpose ? tmp_n2_ : tmp_m2_, sizeof(double) * lout,
+                           cudaMemcpyDeviceToHost, st_));
+        CU(cudaStreamSynchronize(st_));
+    }
+}
+
+}  // namespace igx
+
+namespace igx {
+// FP32 iterates with FP64 residual refinement: filled in below the basic
+// loops once they are validated on the device.
+void Engine::solve_refine(const igaos_pdhg_options&, igaos_pdhg_result& r, double*, double*) {
+    r.status = IGAOS_STATUS_ERROR;
+    r.error_code = IGAOS_PDHG_ERR_INVALID;
+    std::snprintf(r.message, sizeof(r.message), "FP32_REFINE precision is not available yet");
+}
+}  // namespace igx

@@ -1,0 +1,172 @@
+// Host side of the GB300 PDHG engine: owns the device copy of one LP and
+// drives the iteration loop. Only the C ABI (capi.cu) is exported.
+#pragma once
+
+#include <chrono>
+#include <map>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "igaos_pdhg.h"
+#include "device.cuh"
+
+namespace igx {
+
+struct CudaError : std::runtime_error {
+    int code;
+    CudaError(int c, const std::string& s) : std::runtime_error(s), code(c) {}
+};
+
+void cuda_check(cudaError_t e, const char* what, int line);
+#define CU(x) ::igx::cuda_check((x), #x, __LINE__)
+
+// Every device allocation of a problem, freed together.
+class Arena {
+   public:
+    ~Arena();
+    void* raw(size_t bytes);
+    template <typename T>
+    T* alloc(size_t n) { return static_cast<T*>(raw(sizeof(T) * (n ? n : 1))); }
+    size_t bytes() const { return total_; }
+
+   private:
+    std::vector<void*> ptrs_;
+    size_t total_ = 0;
+};
+
+struct Sched {
+    int* row = nullptr;
+    unsigned char* lg = nullptr;
+    int ntiles = 0;
+    TileSched view() const { return TileSched{row, lg, ntiles}; }
+};
+
+// Host-side tile schedule of a CSR row pointer (see device.cuh).
+void build_tiles(const int* ptr, int rows, std::vector<int>& tile_row,
+                 std::vector<unsigned char>& tile_lg);
+
+// Vectors defining one LP over the engine's shared matrix: original units
+// (FP64, for the KKT pass) and scaled units (FP64 and FP32, for iterating).
+struct Vecs {
+    double *c, *cl, *cu, *rmin, *rmax;      // original
+    double *sc, *scl, *scu, *srmin, *srmax; // scaled FP64
+    float *fc, *fcl, *fcu, *frmin, *frmax;  // scaled FP32
+    double cmax;
+};
+
+template <typename T>
+struct Work {
+    T *x[2], *y[2], *xavg[2], *yavg[2], *axc[2];
+    T *xbar, *xb, *yb, *pesx, *pesy;
+    double *part_p, *part_d;
+};
+
+struct GraphKey {
+    int prec, count;
+    uintptr_t vecs;
+    bool operator<(const GraphKey& o) const {
+        if (prec != o.prec) return prec < o.prec;
+        if (count != o.count) return count < o.count;
+        return vecs < o.vecs;
+    }
+};
+
+struct LoopOpts {
+    double tol = 1e-4;
+    double deadline = 0;    // seconds since solve start; <=0: none
+    long long maxit = 500000;
+    int check = 64;
+    int verbosity = 0;
+    bool graphs = true;
+    double eta_init = 1, omega_init = 1, eta0 = 1;
+};
+
+struct LoopOut {
+    int status = IGAOS_STATUS_ERROR;
+    DevMetrics last{};
+    bool last_is_avg = false, use_inc = false;
+    long long iters = 0, attempts = 0, checks = 0, restarts = 0, spmvs = 0;
+    double eta = 0, omega = 0;
+    int parity = 0;
+    bool numeric_failure = false;
+};
+
+class Engine {
+   public:
+    Engine(int m, int n, long long nnz, const int* ap, const int* ai, const double* ax,
+           const int* cp, const int* ci, const double* acx, const double* c,
+           const double* cl, const double* cu, const double* rmin, const double* rmax,
+           double obj_const, int device);
+    ~Engine();
+
+    void solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x, double* y);
+
+    // inspection / parity entry points
+    int m, n;
+    long long nnz;
+    double obj_const;
+    std::vector<double> h_dr, h_dc;
+    double lam2 = 1, eta0 = 1, omega0 = 1;
+    double setup_ms = 0;
+    void get_transpose(int* cp, int* ci, double* acx);
+    void iterate(int precision, long long iters, double* x, double* y, double* xavg,
+                 double* yavg, double* axc, double* st6);
+    void evaluate(const double* x, const double* y, double* out6);
+    void spmv(int transpose, int precision, const double* x, double* y);
+
+   private:
+    int device_ = 0;
+    cudaStream_t st_ = nullptr;
+    Arena ar_;
+    // matrix (scaled in place at setup)
+    int *ap_, *ai_, *cp_, *ci_;
+    double *ax_, *acx_;
+    float *ax32_, *acx32_;
+    Sched sA_, sAT_;
+    double *dr_, *dc_;
+    Vecs base_{};
+    // workspace
+    Work<double> w64_{};
+    Work<float> w32_{};
+    bool have64_ = false, have32_ = false;
+    DevCtl* ctl_ = nullptr;
+    DevCtl* h_ctl_ = nullptr;      // pinned mirror
+    DevMetrics* met_ = nullptr;    // device [2]
+    DevMetrics* h_met_ = nullptr;  // pinned mirror [2]
+    double* kkt_part_ = nullptr;
+    double* red_part_ = nullptr;
+    double* scal_ = nullptr;       // device scalars
+    double* h_scal_ = nullptr;     // pinned
+    unsigned int* ticket_ = nullptr;
+    int* flag_ = nullptr;
+    double* tmp_n_ = nullptr;      // FP64 scratch vectors
+    double* tmp_n2_ = nullptr;
+    double* tmp_m_ = nullptr;
+    double* tmp_m2_ = nullptr;
+    int red_blocks_ = 0;
+    std::map<GraphKey, cudaGraphExec_t> graphs_;
+    std::chrono::steady_clock::time_point t0_;
+    cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
+    double attempt_ms_ = 0;   // accumulated time of attempt launches
+
+    template <typename T> Work<T>& work();
+    template <typename T> Csr<T> csrA() const;
+    template <typename T> Csr<T> csrAT() const;
+    template <typename T> void ensure_work();
+    template <typename T> void launch_attempts(int count, const Vecs& v, bool graphs);
+    template <typename T> void run_until_stop(const Vecs& v, bool graphs, LoopOut& out);
+    template <typename T> void kkt(const Vecs& v, const T* x0, const T* y0, const T* x1,
+                                   const T* y1, int ncand);
+    template <typename T> void spmv_dev(bool transpose, const T* x, T* y);
+    template <typename T> LoopOut loop(const Vecs& v, const LoopOpts& o);
+    template <typename T> void fetch_scaled(const T* src, int len, double* dst);
+    void upload_ctl();
+    void download_ctl();
+    double elapsed() const;
+    void setup_scaling();
+    void power_iteration();
+    void solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x, double* y);
+};
+
+}  // namespace igx

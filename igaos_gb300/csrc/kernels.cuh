@@ -1,0 +1,520 @@
+// Kernels of the GB300 PDHG engine. Reference algorithm: IGAOS
+// src/pdhg/pdhg.cu (file:line cited per kernel).
+#pragma once
+
+#include "device.cuh"
+
+namespace igx {
+
+// ------------------------------------------------------------ attempt state
+// Per-launch view of the control block, read once per CTA.
+struct CtlView {
+    int parity, stop;
+    double eta, omega, hn;
+};
+__device__ __forceinline__ CtlView read_ctl(const DevCtl* c) {
+    CtlView v;
+    v.stop = *(volatile const int*)&c->stop;
+    v.parity = c->parity;
+    v.eta = c->eta;
+    v.omega = c->omega;
+    v.hn = (double)c->hn;
+    return v;
+}
+
+template <typename T>
+struct PrimalArgs {
+    TileSched ts;
+    Csr<T> AT;              // A~^T (rows = columns of A)
+    const T* y[2];          // dual iterate slots
+    const T* c;             // scaled cost
+    const T* lo;            // scaled column bounds
+    const T* hi;
+    T* x[2];
+    T* xavg[2];
+    T* xbar;
+    double* part;           // per-CTA ||dx||^2
+    DevCtl* ctl;
+};
+
+// Primal half of one line-search attempt, fused into the A^T y SpMV:
+//   g = c + A^T y;  x' = P_[l,u](x - tau g);  xbar = 2x' - x;  dx = x' - x
+// (kern_primal, src/pdhg/pdhg.cu:33-45) plus the candidate Halpern average
+// xavg' = xavg + w (x' - xavg), w = 2/(hn+2) (kern_mix2, :129-141, :795-799),
+// written to the other parity slot so that a rejected attempt leaves the
+// accepted state untouched.
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_primal(PrimalArgs<T> a) {
+    __shared__ TileSmem<T> sm;
+    const CtlView cv = read_ctl(a.ctl);
+    if (cv.stop) return;
+    const int p = cv.parity, q = p ^ 1;
+    const T tau = (T)(cv.eta / cv.omega);
+    const T w = (T)(2.0 / (cv.hn + 2.0));
+    const T* __restrict__ xc = a.x[p];
+    const T* __restrict__ xa = a.xavg[p];
+    T* __restrict__ xn_out = a.x[q];
+    T* __restrict__ xa_out = a.xavg[q];
+    T dx2 = 0;
+    auto f = [&](int j, const Acc<T>& acc) {
+        const T g = a.c[j] + acc.result();
+        const T xv = xc[j];
+        const T xn = fmin(fmax(fma(-tau, g, xv), a.lo[j]), a.hi[j]);
+        xn_out[j] = xn;
+        a.xbar[j] = fma((T)2, xn, -xv);
+        const T dx = xn - xv;
+        dx2 = fma(dx, dx, dx2);
+        const T av = xa[j];
+        xa_out[j] = fma(w, xn - av, av);
+    };
+    tile_rows<T>(sm, a.ts, a.AT, a.y[p], blockIdx.x, f);
+    double v[1] = {(double)dx2};
+    block_sum<1>(v, sm.red);
+    if (threadIdx.x == 0) a.part[blockIdx.x] = v[0];
+}
+
+template <typename T>
+struct DualArgs {
+    TileSched ts;
+    Csr<T> A;
+    const T* xbar;
+    const T* rmin;          // scaled row bounds
+    const T* rmax;
+    T* y[2];
+    T* axc[2];              // A x of the accepted iterate
+    T* yavg[2];
+    double* part;           // per-CTA (||dy||^2, dy'A dx)
+    const double* part_primal;
+    int n_primal;
+    DevCtl* ctl;
+};
+
+// Adaptive step decision (src/pdhg/pdhg.cu:770-794), one thread. Host-side
+// arithmetic of the reference has no FMA contraction; the explicit _rn
+// intrinsics keep it that way here.
+__device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cross) {
+    c->dots[0] = dx2;
+    c->dots[1] = dy2;
+    c->dots[2] = cross;
+    if (!isfinite(dx2) || !isfinite(dy2) || !isfinite(cross)) c->nan_flag = 1;
+    const double eta = c->eta, omega = c->omega;
+    const double num = __dadd_rn(__dmul_rn(omega, dx2), __ddiv_rn(dy2, omega));
+    const double etabar =
+        (num > 0.0 && cross > 0.0) ? __ddiv_rn(num, __dmul_rn(2.0, cross)) : CUDART_INF;
+    const double kk = (double)c->k;
+    double eta_new = CUDART_INF;
+    if (isfinite(etabar))
+        eta_new = smin(__dmul_rn(__dsub_rn(1.0, pow(kk, -0.3)), etabar),
+                       __dmul_rn(__dadd_rn(1.0, pow(kk, -0.6)), eta));
+    bool accept = !(eta > etabar) || num <= 0.0 || cross <= 0.0;
+    if (!accept) accept = ++c->retries > 20;
+    c->attempts += 1;
+    if (accept) {
+        if (isfinite(eta_new) && eta_new > 1e-12) c->eta = smin(eta_new, 1e12);
+        c->parity ^= 1;
+        c->hn += 1;
+        c->accepted += 1;
+        c->retries = 0;
+        if (c->k >= c->k_stop || c->nan_flag) c->stop = 1;
+        c->k += 1;
+    } else {
+        c->eta = smax(eta_new, 1e-12);
+    }
+}
+
+// Dual half of one attempt, fused into the A xbar SpMV:
+//   t = y + sigma A xbar;  y' = t - sigma P_[rmin,rmax](t/sigma);
+//   A(x'-x) = (A xbar - A x)/2   (kern_dual, src/pdhg/pdhg.cu:49-61),
+// the candidate averages/commits of kern_mix2 (:129-141), the dot partials of
+// kern_dots (:67-97), and -- in the last CTA to finish -- the fixed-order
+// reduction of all partials (kern_dotfin, :99-125) and the step decision that
+// the reference made on the host after a blocking copy (:768-794).
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
+    __shared__ TileSmem<T> sm;
+    const CtlView cv = read_ctl(a.ctl);
+    if (cv.stop) return;
+    const int p = cv.parity, q = p ^ 1;
+    const T sigma = (T)(cv.eta * cv.omega);
+    const T w = (T)(2.0 / (cv.hn + 2.0));
+    const T* __restrict__ yc = a.y[p];
+    const T* __restrict__ axc = a.axc[p];
+    const T* __restrict__ ya = a.yavg[p];
+    T* __restrict__ yn_out = a.y[q];
+    T* __restrict__ axc_out = a.axc[q];
+    T* __restrict__ ya_out = a.yavg[q];
+    T dy2 = 0, cross = 0;
+    auto f = [&](int i, const Acc<T>& acc) {
+        const T ab = acc.result();
+        const T yv = yc[i];
+        const T t = fma(sigma, ab, yv);
+        const T yn = fma(-sigma, fmin(fmax(t / sigma, a.rmin[i]), a.rmax[i]), t);
+        yn_out[i] = yn;
+        const T dy = yn - yv;
+        const T ax = axc[i];
+        const T adx = (T)0.5 * (ab - ax);
+        axc_out[i] = ax + adx;
+        dy2 = fma(dy, dy, dy2);
+        cross = fma(dy, adx, cross);
+        const T av = ya[i];
+        ya_out[i] = fma(w, yn - av, av);
+    };
+    tile_rows<T>(sm, a.ts, a.A, a.xbar, blockIdx.x, f);
+    double v[2] = {(double)dy2, (double)cross};
+    block_sum<2>(v, sm.red);
+    if (threadIdx.x == 0) {
+        a.part[2 * blockIdx.x] = v[0];
+        a.part[2 * blockIdx.x + 1] = v[1];
+    }
+    if (!last_cta(&a.ctl->ticket)) return;
+    double s[3] = {0.0, 0.0, 0.0};
+    for (int i = threadIdx.x; i < a.n_primal; i += kThreads) s[0] += a.part_primal[i];
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += kThreads) {
+        s[1] += a.part[2 * i];
+        s[2] += a.part[2 * i + 1];
+    }
+    block_sum<3>(s, sm.red);
+    if (threadIdx.x == 0) decide_step(a.ctl, s[0], s[1], s[2]);
+}
+
+// ------------------------------------------------------------- plain SpMV
+// y = A x (Spmv::mv, src/pdhg/pdhg.cu:143-157), optional skip flag.
+template <typename T, typename TO>
+__global__ void __launch_bounds__(kThreads)
+    k_spmv(TileSched ts, Csr<T> A, const T* __restrict__ x, TO* __restrict__ y) {
+    __shared__ TileSmem<T> sm;
+    auto f = [&](int r, const Acc<T>& acc) { y[r] = (TO)acc.result_d(); };
+    tile_rows<T>(sm, ts, A, x, blockIdx.x, f);
+}
+
+// -------------------------------------------------------- Ruiz equilibration
+// src/pdhg/pdhg.cu:474-481: dr_i *= sqrt(max_j |a_ij| dc_j / dr_i). A warp per
+// row; max is order-free, the division and sqrt are IEEE, so the result is
+// bit-identical to the sequential host loop.
+__global__ void k_ruiz_rows(int m, const int* __restrict__ ap, const int* __restrict__ ai,
+                            const double* __restrict__ ax, const double* __restrict__ dc,
+                            double* __restrict__ dr) {
+    const int lane = threadIdx.x & 31;
+    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (i >= m) return;
+    const double dri = dr[i];
+    double mx = 0.0;
+    for (int p = ap[i] + lane; p < ap[i + 1]; p += 32)
+        mx = smax(mx, __ddiv_rn(__dmul_rn(fabs(ax[p]), dc[ai[p]]), dri));
+    mx = warp_max(mx);
+    if (lane == 0 && (mx > 0) && isfinite(mx)) dr[i] = __dmul_rn(dri, __dsqrt_rn(mx));
+}
+
+// src/pdhg/pdhg.cu:482-490: dc_j /= sqrt(max_i |a_ij| / dr_i * dc_j).
+__global__ void k_ruiz_cols(int n, const int* __restrict__ cp, const int* __restrict__ ci,
+                            const double* __restrict__ acx, const double* __restrict__ dr,
+                            double* __restrict__ dc) {
+    const int lane = threadIdx.x & 31;
+    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (j >= n) return;
+    const double dcj = dc[j];
+    double mx = 0.0;
+    for (int p = cp[j] + lane; p < cp[j + 1]; p += 32)
+        mx = smax(mx, __dmul_rn(__ddiv_rn(fabs(acx[p]), dr[ci[p]]), dcj));
+    mx = warp_max(mx);
+    if (lane == 0 && (mx > 0) && isfinite(mx)) dc[j] = __ddiv_rn(dcj, __dsqrt_rn(mx));
+}
+
+__global__ void k_fill(int n, double v, double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = v;
+}
+
+// :491-492 -- non-finite or non-positive factors fall back to 1.
+__global__ void k_fix_scale(int n, double* __restrict__ d) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        if (!(d[i] > 0) || !isfinite(d[i])) d[i] = 1.0;
+}
+
+// Scaled values a~_ij = a_ij dc_j / dr_i (src/pdhg/pdhg.cu:505,512), in
+// place over the original FP64 values, with an FP32 copy. `rowmajor`
+// selects which index array names the column.
+__global__ void k_scale_matrix(int rows, const int* __restrict__ ptr, const int* __restrict__ idx,
+                               double* __restrict__ val, float* __restrict__ val32,
+                               const double* __restrict__ dr, const double* __restrict__ dc,
+                               int rowmajor) {
+    const int lane = threadIdx.x & 31;
+    const int r = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    if (r >= rows) return;
+    for (int p = ptr[r] + lane; p < ptr[r + 1]; p += 32) {
+        double v;
+        if (rowmajor) v = __ddiv_rn(__dmul_rn(val[p], dc[idx[p]]), dr[r]);
+        else v = __ddiv_rn(__dmul_rn(val[p], dc[r]), dr[idx[p]]);
+        val[p] = v;
+        val32[p] = (float)v;
+    }
+}
+
+// s = v / d (bounds) or v * d (cost), elementwise, FP64 and FP32 copies.
+__global__ void k_scale_vec(int n, const double* __restrict__ v, const double* __restrict__ d,
+                            int mul, double* __restrict__ out, float* __restrict__ out32) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        double s = mul ? __dmul_rn(v[i], d[i]) : __ddiv_rn(v[i], d[i]);
+        out[i] = s;
+        if (out32) out32[i] = (float)s;
+    }
+}
+
+// ----------------------------------------------------- reductions / norms
+// out[0] = sum v^2 (sqrt if `root`), deterministic fixed-order tree.
+struct NormArgs {
+    const double* v;
+    int n;
+    double* part;
+    double* out;
+    unsigned int* ticket;
+};
+__global__ void k_sumsq(NormArgs a, int root) {
+    __shared__ double red[kWarps * 4];
+    double s = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < a.n; i += gridDim.x * blockDim.x)
+        s = fma(a.v[i], a.v[i], s);
+    double v[1] = {s};
+    block_sum<1>(v, red);
+    if (threadIdx.x == 0) a.part[blockIdx.x] = v[0];
+    if (!last_cta(a.ticket)) return;
+    double t[1] = {0.0};
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += kThreads) t[0] += a.part[i];
+    block_sum<1>(t, red);
+    if (threadIdx.x == 0) a.out[0] = root ? sqrt(t[0]) : t[0];
+}
+
+// Power-iteration normalisation (src/pdhg/pdhg.cu:617-622): v = w / ||w||
+// unless ||w|| < 1e-300, in which case the loop is over (flag latched).
+__global__ void k_power_normalise(int n, const double* __restrict__ w, double* __restrict__ v,
+                                  const double* nw, int* done) {
+    if (*(volatile int*)done) return;
+    const double nrm = *nw;
+    if (nrm < 1e-300) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) *done = 1;
+        return;
+    }
+    const double inv = 1.0 / nrm;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        v[i] = w[i] * inv;
+}
+
+// sum (a-b)^2 over two vector pairs (primal-weight update,
+// src/pdhg/pdhg.cu:1044-1052), FP64 accumulation.
+template <typename T>
+__global__ void k_diffnorms(int n, const T* __restrict__ x, const T* __restrict__ px, int m,
+                            const T* __restrict__ y, const T* __restrict__ py,
+                            double* part, double* out, unsigned int* ticket) {
+    __shared__ double red[kWarps * 4];
+    double s[2] = {0.0, 0.0};
+    const int stride = gridDim.x * blockDim.x;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+        double d = (double)x[i] - (double)px[i];
+        s[0] = fma(d, d, s[0]);
+    }
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += stride) {
+        double d = (double)y[i] - (double)py[i];
+        s[1] = fma(d, d, s[1]);
+    }
+    block_sum<2>(s, red);
+    if (threadIdx.x == 0) {
+        part[2 * blockIdx.x] = s[0];
+        part[2 * blockIdx.x + 1] = s[1];
+    }
+    if (!last_cta(ticket)) return;
+    double t[2] = {0.0, 0.0};
+    for (int i = threadIdx.x; i < (int)gridDim.x; i += kThreads) {
+        t[0] += part[2 * i];
+        t[1] += part[2 * i + 1];
+    }
+    block_sum<2>(t, red);
+    if (threadIdx.x == 0) {
+        out[0] = t[0];
+        out[1] = t[1];
+    }
+}
+
+template <typename TI, typename TO>
+__global__ void k_convert(int n, const TI* __restrict__ in, TO* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = (TO)in[i];
+}
+
+// --------------------------------------------------------------- KKT pass
+// FP64 metrics of candidate pairs (x~, y~) in ORIGINAL units, one fused
+// device pass replacing metrics_of + evaluate (src/pdhg/pdhg.cu:698-733,
+// 173-254). Candidate v = blockIdx.y. Three launches:
+//   rows  : A x -> pinf numerator/normaliser, prow, max |y|
+//   cols  : A^T y -> reduced costs d, dinf, c^T x, column part of the bound
+//   rowdual: row part of the Lagrangian bound (needs max |y| for its noise
+//            threshold) and the final metrics.
+
+template <typename T>
+struct KktArgs {
+    TileSched tsA, tsAT;
+    Csr<T> A, AT;
+    const T* x[2];
+    const T* y[2];
+    const double *dr, *dc;
+    const double *c, *cl, *cu, *rmin, *rmax;  // original units
+    double cmax;
+    double* part;   // >= 2 * max(tiles) * 4 doubles
+    DevMetrics* out;
+    unsigned int* ticket;
+};
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
+    __shared__ TileSmem<T> sm;
+    const int v = blockIdx.y;
+    const T* __restrict__ yv = a.y[v];
+    double pv = 0.0, pa = 0.0, prow = 0.0, ymax = 0.0;
+    auto f = [&](int i, const Acc<T>& acc) {
+        const double Ax = acc.result_d() * a.dr[i];
+        const double lo = a.rmin[i], hi = a.rmax[i];
+        const double vi = smax(lo - Ax, Ax - hi);
+        pv = smax(pv, vi);
+        pa = smax(pa, fabs(smin(smax(Ax, lo), hi)));
+        const double viol = smax(0.0, vi);
+        double sc = fabs(Ax);
+        if (isfinite(lo)) sc = smax(sc, fabs(lo));
+        if (isfinite(hi)) sc = smax(sc, fabs(hi));
+        prow = smax(prow, viol / (1.0 + sc));
+        ymax = smax(ymax, fabs((double)yv[i] * (1.0 / a.dr[i])));
+    };
+    tile_rows<T>(sm, a.tsA, a.A, a.x[v], blockIdx.x, f);
+    double r[4] = {pv, pa, prow, ymax};
+    block_max<4>(r, sm.red);
+    const int nt = gridDim.x;
+    if (threadIdx.x == 0)
+        for (int q = 0; q < 4; ++q) a.part[(v * nt + blockIdx.x) * 4 + q] = r[q];
+    if (!last_cta(a.ticket)) return;
+    for (int cv = 0; cv < (int)gridDim.y; ++cv) {
+        double t[4] = {0.0, 0.0, 0.0, 0.0};
+        for (int b = threadIdx.x; b < nt; b += kThreads)
+            for (int q = 0; q < 4; ++q) t[q] = smax(t[q], a.part[(cv * nt + b) * 4 + q]);
+        block_max<4>(t, sm.red);
+        if (threadIdx.x == 0) {
+            DevMetrics& o = a.out[cv];
+            o.pv = t[0];
+            o.pa = t[1];
+            o.pinf = smax(t[0], 0.0) / (1.0 + t[1]);
+            o.prow = t[2];
+            o.ymax = t[3];
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a) {
+    __shared__ TileSmem<T> sm;
+    const int v = blockIdx.y;
+    const T* __restrict__ xv = a.x[v];
+    const double dz = 1e-8 * (1.0 + a.cmax);
+    double dv = 0.0, op = 0.0, od = 0.0, unb = 0.0;
+    auto f = [&](int j, const Acc<T>& acc) {
+        const double d = a.c[j] + 1.0 * acc.result_d() / a.dc[j];
+        const double x = (double)xv[j] * a.dc[j];
+        const double cl = a.cl[j], cu = a.cu[j];
+        const double bnd = fabs(isfinite(cu) ? cu : cl);
+        const double tol = 1e-9 * (1.0 + bnd);
+        double e;
+        if (x <= cl + tol && d > 0) e = 0.0;
+        else if (x >= cu - tol && d < 0) e = 0.0;
+        else e = fabs(d);
+        dv = smax(dv, e);
+        op += a.c[j] * x;
+        if (d >= 0) {
+            if (isfinite(cl)) od += d * cl;
+            else if (d > dz) unb = 1.0;
+        } else {
+            if (isfinite(cu)) od += d * cu;
+            else if (-d > dz) unb = 1.0;
+        }
+    };
+    tile_rows<T>(sm, a.tsAT, a.AT, a.y[v], blockIdx.x, f);
+    double mx[2] = {dv, unb};
+    block_max<2>(mx, sm.red);
+    double sm2[2] = {op, od};
+    block_sum<2>(sm2, sm.red);
+    const int nt = gridDim.x;
+    if (threadIdx.x == 0) {
+        double* P = a.part + (v * nt + blockIdx.x) * 4;
+        P[0] = mx[0];
+        P[1] = mx[1];
+        P[2] = sm2[0];
+        P[3] = sm2[1];
+    }
+    if (!last_cta(a.ticket)) return;
+    for (int cv = 0; cv < (int)gridDim.y; ++cv) {
+        double tm[2] = {0.0, 0.0}, ts[2] = {0.0, 0.0};
+        for (int b = threadIdx.x; b < nt; b += kThreads) {
+            const double* P = a.part + (cv * nt + b) * 4;
+            tm[0] = smax(tm[0], P[0]);
+            tm[1] = smax(tm[1], P[1]);
+            ts[0] += P[2];
+            ts[1] += P[3];
+        }
+        block_max<2>(tm, sm.red);
+        block_sum<2>(ts, sm.red);
+        if (threadIdx.x == 0) {
+            DevMetrics& o = a.out[cv];
+            o.dv = tm[0];
+            o.dinf = tm[0] / (1.0 + a.cmax);
+            o.unb_col = tm[1] > 0.0;
+            o.op = ts[0];
+            o.od_col = ts[1];
+        }
+    }
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_kkt_rowdual(KktArgs<T> a, int m) {
+    __shared__ double red[kWarps * 4];
+    const int v = blockIdx.y;
+    const T* __restrict__ yv = a.y[v];
+    const double yz = 1e-8 * (1.0 + a.out[v].ymax);
+    double od = 0.0, unb = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const double y = (double)yv[i] * (1.0 / a.dr[i]);
+        if (y > yz) {
+            if (isfinite(a.rmax[i])) od -= y * a.rmax[i];
+            else unb = 1.0;
+        } else if (y < -yz) {
+            if (isfinite(a.rmin[i])) od -= y * a.rmin[i];
+            else unb = 1.0;
+        }
+    }
+    double s[1] = {od};
+    block_sum<1>(s, red);
+    double u[1] = {unb};
+    block_max<1>(u, red);
+    const int nb = gridDim.x;
+    if (threadIdx.x == 0) {
+        a.part[(v * nb + blockIdx.x) * 2] = s[0];
+        a.part[(v * nb + blockIdx.x) * 2 + 1] = u[0];
+    }
+    if (!last_cta(a.ticket)) return;
+    for (int cv = 0; cv < (int)gridDim.y; ++cv) {
+        double t[1] = {0.0}, w[1] = {0.0};
+        for (int b = threadIdx.x; b < nb; b += kThreads) {
+            t[0] += a.part[(cv * nb + b) * 2];
+            w[0] = smax(w[0], a.part[(cv * nb + b) * 2 + 1]);
+        }
+        block_sum<1>(t, red);
+        block_max<1>(w, red);
+        if (threadIdx.x == 0) {
+            DevMetrics& o = a.out[cv];
+            o.od_row = t[0];
+            o.unb_row = w[0] > 0.0;
+            const bool bounded = !o.unb_col && !o.unb_row;
+            o.od = bounded ? o.od_col + o.od_row : -CUDART_INF;
+            o.gap = bounded ? smax(0.0, o.op - o.od) / (1.0 + fabs(o.op)) : CUDART_INF;
+            o.finite = isfinite(o.pinf) && isfinite(o.dinf);
+            const double g = isfinite(o.gap) ? o.gap : 0.0;
+            o.err = smax(o.pinf, smax(o.dinf, g));
+        }
+    }
+}
+
+}  // namespace igx

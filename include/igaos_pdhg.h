@@ -1,0 +1,191 @@
+/*
+ * igaos_pdhg -- C ABI of the GB300 PDHG LP engine.
+ *
+ * This is the boundary the reference's PDHG path sits behind: the reference
+ * exposes `igaos::Solution igaos::pdhg::solve(const io::Model&, const
+ * Options&)` (src/pdhg/pdhg.hpp:9), called only from
+ * igaos::solve_with_engine(model, opts, "pdhg") (src/api/engine.hpp:32-38).
+ * Every entry point here takes plain pointers and sizes, never throws, and
+ * reports failure as a nonzero IGAOS_PDHG_ERR_* code with a message readable
+ * through igaos_pdhg_last_error(). The C++ igaos::pdhg::solve of this repo is
+ * a thin wrapper over igaos_pdhg_create / igaos_pdhg_solve.
+ *
+ * Conventions shared with the reference model (src/io/model.hpp:16-37):
+ *   minimise c^T x + obj_const  s.t.  rmin <= A x <= rmax,  cl <= x <= cu,
+ *   A is m x n, CSR (ap[m+1], ai[nnz], ax[nnz]) with int32 indices, FP64
+ *   values; absent bounds are +-INFINITY. The dual y follows the reference
+ *   sign convention: reduced cost d = c + A^T y.
+ */
+#ifndef IGAOS_PDHG_H
+#define IGAOS_PDHG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define IGAOS_PDHG_ABI_VERSION 1
+
+/* Return codes of every entry point. */
+enum {
+    IGAOS_PDHG_OK = 0,
+    IGAOS_PDHG_ERR_INVALID = 1,  /* bad argument: sizes, NULL, NaN in data */
+    IGAOS_PDHG_ERR_CUDA = 2,     /* CUDA runtime failure */
+    IGAOS_PDHG_ERR_NOMEM = 3,    /* device allocation failed */
+    IGAOS_PDHG_ERR_NODEVICE = 4, /* no usable CUDA device */
+    IGAOS_PDHG_ERR_NUMERIC = 5,  /* NaN/Inf appeared in the iterates */
+    IGAOS_PDHG_ERR_TIMEOUT = 6   /* a bounded device wait ran out */
+};
+
+/* Solution status, same order and meaning as igaos::Status
+ * (include/igaos/status.h:5-14 of the reference). */
+enum {
+    IGAOS_STATUS_OPTIMAL = 0,
+    IGAOS_STATUS_NEAR_OPTIMAL = 1,
+    IGAOS_STATUS_FEASIBLE = 2,
+    IGAOS_STATUS_INFEASIBLE = 3,
+    IGAOS_STATUS_UNBOUNDED = 4,
+    IGAOS_STATUS_ITERATION_LIMIT = 5,
+    IGAOS_STATUS_TIME_LIMIT = 6,
+    IGAOS_STATUS_ERROR = 7
+};
+
+/* Arithmetic of the iteration loop. */
+enum {
+    IGAOS_PDHG_FP64 = 0,        /* reference algorithm, all FP64 */
+    IGAOS_PDHG_FP32_REFINE = 1, /* FP32 iterates + FP64 residual refinement */
+    IGAOS_PDHG_FP32 = 2         /* FP32 iterates, FP64 checks, no refinement */
+};
+
+/* Options. The first seven fields mirror igaos::Options
+ * (include/igaos/options.h:5-13 of the reference) with the same defaults;
+ * the rest are engine controls. As in the reference engine
+ * (src/pdhg/pdhg.cu:669-671), max_iterations only binds when the time limit
+ * is not finite (<= 0 or >= 1e6); otherwise the cap is 20,000,000. */
+typedef struct igaos_pdhg_options {
+    double time_limit_s;      /* 120 */
+    double tolerance;         /* 1e-4: relative KKT (pinf, prow, dinf, gap) */
+    int64_t max_iterations;   /* 500000 */
+    int seed;                 /* ignored, as in the reference engine */
+    int presolve;             /* ignored, as in the reference engine */
+    int restarts;             /* ignored: the engine always restarts */
+    int verbosity;            /* 0 quiet, 1 progress, 2 debug (stderr) */
+    int precision;            /* IGAOS_PDHG_FP64 (default) / FP32_REFINE / FP32 */
+    int check_period;         /* 64: iterations between KKT checks */
+    double inner_tolerance;   /* FP32_REFINE: tolerance of each FP32 solve (1e-4) */
+    int max_refinements;      /* FP32_REFINE: outer rounds (12) */
+    int use_graphs;           /* 1: replay captured CUDA graphs of attempts */
+    int device;               /* CUDA device ordinal (-1: current) */
+} igaos_pdhg_options;
+
+typedef struct igaos_pdhg_result {
+    int status;               /* IGAOS_STATUS_* */
+    int error_code;           /* IGAOS_PDHG_OK or IGAOS_PDHG_ERR_* */
+    double objective;         /* c^T x + obj_const, original units */
+    double pinf, dinf, rel_gap, prow;
+    int64_t iterations;       /* accepted PDHG iterations (all rounds) */
+    int64_t attempts;         /* line-search attempts */
+    int64_t kkt_checks;       /* KKT evaluations */
+    int64_t restarts;
+    int64_t kkt_passes;       /* matrix passes: one A + one A^T product each */
+    int refinements;          /* FP32_REFINE outer rounds taken */
+    double solve_time_ms;     /* solve loop wall time (setup excluded) */
+    double setup_time_ms;     /* upload + scaling + power iteration */
+    double device_time_ms;    /* solve, CUDA events on the engine stream */
+    double attempt_time_ms;   /* of which in line-search attempt launches */
+    char message[160];
+} igaos_pdhg_result;
+
+typedef struct igaos_pdhg_problem igaos_pdhg_problem;
+
+/* ABI version (IGAOS_PDHG_ABI_VERSION). No reference counterpart. */
+int igaos_pdhg_abi_version(void);
+
+/* Number of visible CUDA devices (0 when none). Replaces the handle-creation
+ * probe of src/pdhg/pdhg.cu:459-465. */
+int igaos_pdhg_device_count(void);
+
+/* Fills *o with the defaults above. Mirrors igaos::Options{} defaults. */
+void igaos_pdhg_default_options(igaos_pdhg_options* o);
+
+/* Copies the calling thread's last error message into buf (NUL-terminated,
+ * truncated to len); returns the last error code. Replaces Solution.message
+ * on failure paths ("CUDA error in PDHG engine", src/pdhg/pdhg.cu:14-23). */
+int igaos_pdhg_last_error(char* buf, size_t len);
+
+/* Uploads an LP and prepares it on the device: Ruiz scaling (10 sweeps,
+ * src/pdhg/pdhg.cu:472-492), scaled FP64/FP32 copies (:499-513), SpMV tile
+ * schedules, power iteration (:605-631). Replaces the upload block
+ * src/pdhg/pdhg.cu:515-603. cp/ci/acx may all be NULL: A^T is then built from
+ * the CSR by a stable counting sort (bit-identical values, the orientation
+ * src/io/model.hpp:39-67 builds). Host buffers are only read during the call. */
+int igaos_pdhg_create(igaos_pdhg_problem** out, int m, int n, int64_t nnz,
+                      const int* ap, const int* ai, const double* ax,
+                      const int* cp, const int* ci, const double* acx,
+                      const double* c, const double* cl, const double* cu,
+                      const double* rmin, const double* rmax, double obj_const,
+                      const igaos_pdhg_options* opt);
+
+/* Solves the uploaded LP. x (n) and y (m) may be NULL; else they receive the
+ * answer in original units. Replaces the solve loop + unscale of
+ * src/pdhg/pdhg.cu:605-1141; result fields mirror igaos::Solution
+ * (include/igaos/solution.h:10-22). The problem can be solved again. */
+int igaos_pdhg_solve(igaos_pdhg_problem* p, const igaos_pdhg_options* opt,
+                     igaos_pdhg_result* res, double* x, double* y);
+
+/* Frees every device buffer of the problem (src/pdhg/pdhg.cu:1143-1154). */
+void igaos_pdhg_destroy(igaos_pdhg_problem* p);
+
+/* Convenience: create + solve + destroy in one call, the shape of the
+ * reference's pdhg::solve(Model, Options). */
+int igaos_pdhg_solve_csr(int m, int n, int64_t nnz, const int* ap,
+                         const int* ai, const double* ax, const int* cp,
+                         const int* ci, const double* acx, const double* c,
+                         const double* cl, const double* cu,
+                         const double* rmin, const double* rmax,
+                         double obj_const, const igaos_pdhg_options* opt,
+                         igaos_pdhg_result* res, double* x, double* y);
+
+/* ---- inspection entry points (parity tests, tooling) --------------------
+ * Row/column scaling factors dr (m), dc (n) computed at create: the Ruiz
+ * vectors of src/pdhg/pdhg.cu:472-492. */
+int igaos_pdhg_get_scaling(const igaos_pdhg_problem* p, double* dr, double* dc);
+
+/* Power-iteration estimate of ||A~||_2^2 (src/pdhg/pdhg.cu:605-631) and the
+ * initial step eta0 = 1.2/sqrt(lambda) and weight omega0 (:642-663). */
+int igaos_pdhg_get_step_init(const igaos_pdhg_problem* p, double* lambda,
+                             double* eta0, double* omega0);
+
+/* The device-built A^T (CSR of the transpose of the scaled A): pointers,
+ * indices and FP64 values (src/io/model.hpp:39-67 orientation). */
+int igaos_pdhg_get_transpose(const igaos_pdhg_problem* p, int* cp, int* ci,
+                             double* acx_scaled);
+
+/* Runs exactly `iters` accepted PDHG iterations (adaptive line search +
+ * Halpern averaging, src/pdhg/pdhg.cu:748-799) from the given scaled-unit
+ * state, without KKT checks or restarts, in the given precision, and returns
+ * the new state. state6 = {eta, omega, k, hn, attempts(out), parity(out)};
+ * x, y, xavg, yavg, axcur are read and overwritten (scaled units, FP64). */
+int igaos_pdhg_iterate(igaos_pdhg_problem* p, int precision, int64_t iters,
+                       double* x, double* y, double* xavg, double* yavg,
+                       double* axcur, double* state6);
+
+/* FP64 KKT metrics of (x, y) given in ORIGINAL units, evaluated on the
+ * device (the fused pass replacing src/pdhg/pdhg.cu:173-254 + :698-733).
+ * out6 = {pinf, dinf, gap, op, od, prow}. */
+int igaos_pdhg_evaluate(igaos_pdhg_problem* p, const double* x,
+                        const double* y, double* out6);
+
+/* y = A~ x or A~^T x (transpose != 0) with the engine's tiled SpMV on the
+ * scaled matrix, in FP64 (precision 0) or FP32 (precision 2; x and y are
+ * still passed as FP64 host arrays). Replaces Spmv::mv (cuSPARSE,
+ * src/pdhg/pdhg.cu:143-157). */
+int igaos_pdhg_spmv(igaos_pdhg_problem* p, int transpose, int precision,
+                    const double* x, double* y);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

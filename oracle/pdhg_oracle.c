@@ -1,0 +1,648 @@
+/*
+ * CPU oracle for the PDHG LP engine -- TEST INFRASTRUCTURE ONLY (see
+ * pdhg_oracle.h). FP64 restatement of IGAOS src/pdhg/pdhg.cu (engine) and
+ * src/io/model.hpp (matrix build).
+ *
+ * Floating-point conventions, chosen so that this file reproduces what the
+ * reference computes rather than what a C compiler happens to emit:
+ *  - compiled with -ffp-contract=off (no implicit FMA on any host);
+ *  - the reference's device kernels (kern_primal/kern_dual/kern_dots/
+ *    kern_mix2) are compiled by nvcc with FMA contraction on, so their
+ *    restatements below use explicit fma() at exactly the expressions nvcc
+ *    contracts (a - b*c, a + b*c, b*c - a);
+ *  - the reference's host code (evaluate, Ruiz, scaling, line search) is
+ *    plain x86-64 code without FMA, restated without fma().
+ * max/min follow std::max/std::min ((a<b)?b:a, (b<a)?b:a), which differ from
+ * fmax/fmin on NaN; fmax/fmin are used exactly where the reference uses them.
+ */
+#include "pdhg_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#include <time.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+static inline double smax(double a, double b) { return (a < b) ? b : a; }
+static inline double smin(double a, double b) { return (b < a) ? b : a; }
+static const double ORC_INF = 1.0 / 0.0;
+
+static double now_s(void) {
+    struct timespec ts;
+    clock_gettime(CLOCK_MONOTONIC, &ts);
+    return (double)ts.tv_sec + 1e-9 * (double)ts.tv_nsec;
+}
+
+void orc_default_options(orc_options* o) {
+    o->time_limit_s = 120.0;
+    o->tolerance = 1e-4;
+    o->max_iterations = 500000;
+    o->check_period = 64;
+    o->threads = 1;
+    o->verbosity = 0;
+}
+
+/* ---------------------------------------------------------------- evaluate
+ * reference src/pdhg/pdhg.cu:173-254 */
+void orc_evaluate(int m, int n, const double* rmin, const double* rmax,
+                  const double* cl, const double* cu, const double* c,
+                  const double* x, const double* y, const double* Ax,
+                  const double* d, orc_metrics* mt) {
+    double pv = 0.0, pa = 0.0, prow = 0.0;
+    for (int i = 0; i < m; ++i) {
+        pv = smax(pv, smax(rmin[i] - Ax[i], Ax[i] - rmax[i]));
+        pa = smax(pa, fabs(smin(smax(Ax[i], rmin[i]), rmax[i])));
+        double viol = smax(0.0, smax(rmin[i] - Ax[i], Ax[i] - rmax[i]));
+        double sc = fabs(Ax[i]);
+        if (isfinite(rmin[i])) sc = smax(sc, fabs(rmin[i]));
+        if (isfinite(rmax[i])) sc = smax(sc, fabs(rmax[i]));
+        prow = smax(prow, viol / (1.0 + sc));
+    }
+    mt->pinf = smax(pv, 0.0) / (1.0 + pa);
+    mt->prow = prow;
+    double dv = 0.0;
+    for (int j = 0; j < n; ++j) {
+        double bnd = fabs(isfinite(cu[j]) ? cu[j] : cl[j]);
+        double tol = 1e-9 * (1.0 + bnd);
+        double v;
+        if (x[j] <= cl[j] + tol && d[j] > 0) v = 0.0;
+        else if (x[j] >= cu[j] - tol && d[j] < 0) v = 0.0;
+        else v = fabs(d[j]);
+        dv = smax(dv, v);
+    }
+    double cmax = 0.0;
+    for (int j = 0; j < n; ++j) cmax = smax(cmax, fabs(c[j]));
+    mt->dinf = dv / (1.0 + cmax);
+    mt->op = 0.0;
+    for (int j = 0; j < n; ++j) mt->op += c[j] * x[j];
+    double od = 0.0;
+    int bounded = 1;
+    double ymax = 0.0;
+    for (int i = 0; i < m; ++i) ymax = smax(ymax, fabs(y[i]));
+    const double dz = 1e-8 * (1.0 + cmax);
+    const double yz = 1e-8 * (1.0 + ymax);
+    for (int j = 0; j < n; ++j) {
+        if (d[j] >= 0) {
+            if (isfinite(cl[j])) od += d[j] * cl[j];
+            else if (d[j] > dz) { bounded = 0; break; }
+        } else {
+            if (isfinite(cu[j])) od += d[j] * cu[j];
+            else if (-d[j] > dz) { bounded = 0; break; }
+        }
+    }
+    if (bounded) {
+        for (int i = 0; i < m; ++i) {
+            if (y[i] > yz) {
+                if (isfinite(rmax[i])) od -= y[i] * rmax[i];
+                else { bounded = 0; break; }
+            } else if (y[i] < -yz) {
+                if (isfinite(rmin[i])) od -= y[i] * rmin[i];
+                else { bounded = 0; break; }
+            }
+        }
+    }
+    mt->od = bounded ? od : -ORC_INF;
+    mt->gap = bounded ? smax(0.0, mt->op - od) / (1.0 + fabs(mt->op)) : ORC_INF;
+}
+
+/* ------------------------------------------------------------ matrix build
+ * reference src/io/model.hpp:39-67 */
+void orc_counting_sort(int64_t nt, const int* ti, const int* tj,
+                       const double* tv, int rows, int cols, int* ap, int* ai,
+                       double* ax, int* cp, int* ci, double* acx) {
+    memset(ap, 0, sizeof(int) * (size_t)(rows + 1));
+    memset(cp, 0, sizeof(int) * (size_t)(cols + 1));
+    for (int64_t t = 0; t < nt; ++t) {
+        ap[ti[t] + 1]++;
+        cp[tj[t] + 1]++;
+    }
+    for (int i = 0; i < rows; ++i) ap[i + 1] += ap[i];
+    for (int j = 0; j < cols; ++j) cp[j + 1] += cp[j];
+    int* nr = (int*)malloc(sizeof(int) * (size_t)(rows + 1));
+    int* nc = (int*)malloc(sizeof(int) * (size_t)(cols + 1));
+    memcpy(nr, ap, sizeof(int) * (size_t)(rows + 1));
+    memcpy(nc, cp, sizeof(int) * (size_t)(cols + 1));
+    for (int64_t t = 0; t < nt; ++t) {
+        int r = ti[t], c = tj[t];
+        ai[nr[r]] = c;
+        ax[nr[r]] = tv[t];
+        nr[r]++;
+        ci[nc[c]] = r;
+        acx[nc[c]] = tv[t];
+        nc[c]++;
+    }
+    free(nr);
+    free(nc);
+}
+
+void orc_transpose(int rows, int cols, const int* ap, const int* ai,
+                   const double* ax, int* cp, int* ci, double* acx) {
+    memset(cp, 0, sizeof(int) * (size_t)(cols + 1));
+    for (int p = 0; p < ap[rows]; ++p) cp[ai[p] + 1]++;
+    for (int j = 0; j < cols; ++j) cp[j + 1] += cp[j];
+    int* nc = (int*)malloc(sizeof(int) * (size_t)(cols + 1));
+    memcpy(nc, cp, sizeof(int) * (size_t)(cols + 1));
+    for (int i = 0; i < rows; ++i)
+        for (int p = ap[i]; p < ap[i + 1]; ++p) {
+            int j = ai[p];
+            ci[nc[j]] = i;
+            acx[nc[j]] = ax[p];
+            nc[j]++;
+        }
+    free(nc);
+}
+
+void orc_spmv(int rows, const int* ptr, const int* idx, const double* val,
+              const double* x, double* y, int threads) {
+    (void)threads;
+#ifdef _OPENMP
+#pragma omp parallel for schedule(static) num_threads(threads > 0 ? threads : 1) if (threads > 1)
+#endif
+    for (int i = 0; i < rows; ++i) {
+        double s = 0.0;
+        for (int p = ptr[i]; p < ptr[i + 1]; ++p) s += val[p] * x[idx[p]];
+        y[i] = s;
+    }
+}
+
+/* ------------------------------------------------------------------ scaling
+ * reference src/pdhg/pdhg.cu:472-492 */
+void orc_ruiz(const orc_lp* lp, int sweeps, double* dr, double* dc) {
+    const int m = lp->m, n = lp->n;
+    for (int i = 0; i < m; ++i) dr[i] = 1.0;
+    for (int j = 0; j < n; ++j) dc[j] = 1.0;
+    for (int sweep = 0; sweep < sweeps; ++sweep) {
+        for (int i = 0; i < m; ++i) {
+            double mx = 0.0;
+            for (int p = lp->ap[i]; p < lp->ap[i + 1]; ++p)
+                mx = smax(mx, fabs(lp->ax[p]) * dc[lp->ai[p]] / dr[i]);
+            if (!(mx > 0) || !isfinite(mx)) continue;
+            dr[i] *= sqrt(mx);
+        }
+        for (int j = 0; j < n; ++j) {
+            double mx = 0.0;
+            for (int p = lp->cp[j]; p < lp->cp[j + 1]; ++p)
+                mx = smax(mx, fabs(lp->acx[p]) / dr[lp->ci[p]] * dc[j]);
+            if (!(mx > 0) || !isfinite(mx)) continue;
+            dc[j] /= sqrt(mx);
+        }
+    }
+    for (int i = 0; i < m; ++i)
+        if (!(dr[i] > 0) || !isfinite(dr[i])) dr[i] = 1.0;
+    for (int j = 0; j < n; ++j)
+        if (!(dc[j] > 0) || !isfinite(dc[j])) dc[j] = 1.0;
+}
+
+/* reference src/pdhg/pdhg.cu:499-513 (gamma = 1, so c/gamma == c). */
+void orc_scale(const orc_lp* lp, const double* dr, const double* dc,
+               double* sax, double* sacx, double* sc, double* scl,
+               double* scu, double* srmin, double* srmax) {
+    for (int i = 0; i < lp->m; ++i) {
+        srmin[i] = lp->rmin[i] / dr[i];
+        srmax[i] = lp->rmax[i] / dr[i];
+        for (int p = lp->ap[i]; p < lp->ap[i + 1]; ++p)
+            sax[p] = lp->ax[p] * dc[lp->ai[p]] / dr[i];
+    }
+    for (int j = 0; j < lp->n; ++j) {
+        sc[j] = lp->c[j] * dc[j] / 1.0;
+        scl[j] = lp->cl[j] / dc[j];
+        scu[j] = lp->cu[j] / dc[j];
+        for (int p = lp->cp[j]; p < lp->cp[j + 1]; ++p)
+            sacx[p] = lp->acx[p] * dc[j] / dr[lp->ci[p]];
+    }
+}
+
+static double nrm2(int n, const double* v) {
+    double s = 0.0;
+    for (int i = 0; i < n; ++i) s += v[i] * v[i];
+    return sqrt(s);
+}
+
+/* reference src/pdhg/pdhg.cu:605-631 */
+double orc_power_iteration(int m, int n, const int* ap, const int* ai,
+                           const double* sax, const int* cp, const int* ci,
+                           const double* sacx, int iters, int threads) {
+    double* v = (double*)malloc(sizeof(double) * (size_t)n);
+    double* w = (double*)malloc(sizeof(double) * (size_t)n);
+    double* tm = (double*)malloc(sizeof(double) * (size_t)(m > 0 ? m : 1));
+    for (int j = 0; j < n; ++j) v[j] = 1.0 / sqrt((double)n);
+    for (int it = 0; it < iters; ++it) {
+        orc_spmv(m, ap, ai, sax, v, tm, threads);
+        orc_spmv(n, cp, ci, sacx, tm, w, threads);
+        double nw = nrm2(n, w);
+        if (nw < 1e-300) break;
+        double inv = 1.0 / nw;
+        for (int j = 0; j < n; ++j) w[j] *= inv;
+        memcpy(v, w, sizeof(double) * (size_t)n);
+    }
+    orc_spmv(m, ap, ai, sax, v, tm, threads);
+    double na = nrm2(m, tm);
+    double lam2 = na * na;
+    if (!(lam2 > 0) || !isfinite(lam2)) lam2 = 1.0;
+    free(v);
+    free(w);
+    free(tm);
+    return lam2;
+}
+
+/* -------------------------------------------------------- iteration kernels
+ * reference src/pdhg/pdhg.cu:33-45 (kern_primal) */
+void orc_primal(int n, double tau, const double* x, const double* c,
+                const double* ata, const double* lo, const double* hi,
+                double* xnew, double* xbar, double* dx) {
+    for (int i = 0; i < n; ++i) {
+        double g = c[i] + ata[i];
+        double xn = fmin(fmax(fma(-tau, g, x[i]), lo[i]), hi[i]);
+        xnew[i] = xn;
+        xbar[i] = fma(2.0, xn, -x[i]);
+        dx[i] = xn - x[i];
+    }
+}
+
+/* reference src/pdhg/pdhg.cu:49-61 (kern_dual) */
+void orc_dual(int m, double s, const double* y, const double* axb,
+              const double* rmin, const double* rmax, const double* axcur,
+              double* ynew, double* dy, double* adx) {
+    for (int i = 0; i < m; ++i) {
+        double t = fma(s, axb[i], y[i]);
+        double yn = fma(-s, fmin(fmax(t / s, rmin[i]), rmax[i]), t);
+        ynew[i] = yn;
+        dy[i] = yn - y[i];
+        adx[i] = 0.5 * (axb[i] - axcur[i]);
+    }
+}
+
+/* reference src/pdhg/pdhg.cu:67-125 (kern_dots + kern_dotfin); summed
+ * sequentially here -- the reference's two-stage tree order is a property of
+ * its launch shape, not of the algorithm. */
+void orc_dots(int n, int m, const double* dx, const double* dy,
+              const double* adx, double out[3]) {
+    double a0 = 0.0, a1 = 0.0, a2 = 0.0;
+    for (int i = 0; i < n; ++i) a0 = fma(dx[i], dx[i], a0);
+    for (int i = 0; i < m; ++i) {
+        a1 = fma(dy[i], dy[i], a1);
+        a2 = fma(dy[i], adx[i], a2);
+    }
+    out[0] = a0;
+    out[1] = a1;
+    out[2] = a2;
+}
+
+typedef struct {
+    double *xnew, *xbar, *dx, *ynew, *dy, *adx, *ata, *tm;
+} orc_scratch;
+
+static void scratch_alloc(orc_scratch* s, int m, int n) {
+    size_t nb = sizeof(double) * (size_t)(n > 0 ? n : 1);
+    size_t mb = sizeof(double) * (size_t)(m > 0 ? m : 1);
+    s->xnew = (double*)malloc(nb);
+    s->xbar = (double*)malloc(nb);
+    s->dx = (double*)malloc(nb);
+    s->ata = (double*)malloc(nb);
+    s->ynew = (double*)malloc(mb);
+    s->dy = (double*)malloc(mb);
+    s->adx = (double*)malloc(mb);
+    s->tm = (double*)malloc(mb);
+}
+static void scratch_free(orc_scratch* s) {
+    free(s->xnew); free(s->xbar); free(s->dx); free(s->ata);
+    free(s->ynew); free(s->dy); free(s->adx); free(s->tm);
+}
+
+/* One accepted iteration with its line search, reference
+ * src/pdhg/pdhg.cu:749-799. Returns the attempts made. */
+static int one_iteration(int m, int n, const int* ap, const int* ai,
+                         const double* sax, const int* cp, const int* ci,
+                         const double* sacx, const double* sc,
+                         const double* scl, const double* scu,
+                         const double* srmin, const double* srmax,
+                         orc_state* st, orc_scratch* w, int threads) {
+    orc_spmv(n, cp, ci, sacx, st->y, w->ata, threads);
+    int retries = 0, attempts = 0;
+    double dots[3];
+    for (;;) {
+        ++attempts;
+        const double tau = st->eta / st->omega, sigma = st->eta * st->omega;
+        orc_primal(n, tau, st->x, sc, w->ata, scl, scu, w->xnew, w->xbar, w->dx);
+        orc_spmv(m, ap, ai, sax, w->xbar, w->tm, threads);
+        orc_dual(m, sigma, st->y, w->tm, srmin, srmax, st->axcur, w->ynew,
+                 w->dy, w->adx);
+        orc_dots(n, m, w->dx, w->dy, w->adx, dots);
+        const double num = st->omega * dots[0] + dots[1] / st->omega;
+        const double cross = dots[2];
+        const double etabar =
+            (num > 0.0 && cross > 0.0) ? num / (2.0 * cross) : ORC_INF;
+        const double kk = (double)st->k;
+        const double eta_new =
+            isfinite(etabar) ? smin((1.0 - pow(kk, -0.3)) * etabar,
+                                    (1.0 + pow(kk, -0.6)) * st->eta)
+                             : ORC_INF;
+        const int accept = !(st->eta > etabar) || num <= 0.0 ||
+                           cross <= 0.0 || ++retries > 20;
+        if (accept) {
+            if (isfinite(eta_new) && eta_new > 1e-12)
+                st->eta = smin(eta_new, 1e12);
+            double* t = st->x; st->x = w->xnew; w->xnew = t;
+            t = st->y; st->y = w->ynew; w->ynew = t;
+            break;
+        }
+        st->eta = smax(eta_new, 1e-12);
+    }
+    /* kern_mix2, reference :129-141, :795-799 */
+    const double weta = 2.0 / ((double)st->hn + 2.0);
+    ++st->hn;
+    for (int i = 0; i < n; ++i)
+        st->xavg[i] = fma(weta, st->x[i] - st->xavg[i], st->xavg[i]);
+    for (int i = 0; i < m; ++i) {
+        st->yavg[i] = fma(weta, st->y[i] - st->yavg[i], st->yavg[i]);
+        st->axcur[i] += w->adx[i];
+    }
+    ++st->k;
+    return attempts;
+}
+
+int64_t orc_iterate(int m, int n, const int* ap, const int* ai,
+                    const double* sax, const int* cp, const int* ci,
+                    const double* sacx, const double* sc, const double* scl,
+                    const double* scu, const double* srmin,
+                    const double* srmax, orc_state* st, int64_t iters,
+                    int threads) {
+    orc_scratch w;
+    scratch_alloc(&w, m, n);
+    /* one_iteration swaps st->x with a scratch buffer; keep the caller's
+     * buffers as the final home of x and y. */
+    double* x0 = st->x;
+    double* y0 = st->y;
+    int64_t att = 0;
+    for (int64_t t = 0; t < iters; ++t)
+        att += one_iteration(m, n, ap, ai, sax, cp, ci, sacx, sc, scl, scu,
+                             srmin, srmax, st, &w, threads);
+    if (st->x != x0) {
+        memcpy(x0, st->x, sizeof(double) * (size_t)n);
+        w.xnew = st->x;
+        st->x = x0;
+    }
+    if (st->y != y0) {
+        memcpy(y0, st->y, sizeof(double) * (size_t)m);
+        w.ynew = st->y;
+        st->y = y0;
+    }
+    scratch_free(&w);
+    return att;
+}
+
+/* ---------------------------------------------------------------- full solve
+ * reference src/pdhg/pdhg.cu:457-1156 */
+typedef struct {
+    int pass_set;
+    double err;
+} orc_dummy;
+
+static int metrics_finite(const orc_metrics* t) {
+    return isfinite(t->pinf) && isfinite(t->dinf);
+}
+static double metrics_err(const orc_metrics* t) {
+    double g = isfinite(t->gap) ? t->gap : 0.0;
+    return smax(t->pinf, smax(t->dinf, g));
+}
+
+int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
+                   double* xout, double* yout) {
+    const int m = lp->m, n = lp->n;
+    const int64_t nnz = lp->nnz;
+    const int th = opt->threads > 0 ? opt->threads : 1;
+    memset(res, 0, sizeof(*res));
+    res->status = 7;
+    size_t nb = sizeof(double) * (size_t)(n > 0 ? n : 1);
+    size_t mb = sizeof(double) * (size_t)(m > 0 ? m : 1);
+    double* dr = (double*)malloc(mb);
+    double* dc = (double*)malloc(nb);
+    orc_ruiz(lp, 10, dr, dc);
+    double* sax = (double*)malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+    double* sacx = (double*)malloc(sizeof(double) * (size_t)(nnz > 0 ? nnz : 1));
+    double *sc = (double*)malloc(nb), *scl = (double*)malloc(nb),
+           *scu = (double*)malloc(nb);
+    double *srmin = (double*)malloc(mb), *srmax = (double*)malloc(mb);
+    orc_scale(lp, dr, dc, sax, sacx, sc, scl, scu, srmin, srmax);
+
+    double t0 = now_s();
+    double lam2 = orc_power_iteration(m, n, lp->ap, lp->ai, sax, lp->cp,
+                                      lp->ci, sacx, 30, th);
+    const double eta0 = 1.2 / sqrt(lam2);
+    orc_state st;
+    st.eta = eta0;
+    st.omega = 1.0;
+    {
+        double cn = 0.0, qn = 0.0;
+        for (int j = 0; j < n; ++j) cn += sc[j] * sc[j];
+        for (int i = 0; i < m; ++i) {
+            double q = isfinite(srmax[i]) ? srmax[i]
+                                          : (isfinite(srmin[i]) ? srmin[i] : 0.0);
+            qn += q * q;
+        }
+        if (cn > 1e-24 && qn > 1e-24) {
+            double w = sqrt(cn / qn);
+            st.omega = w < 0.3 ? 0.3 : (w > 3.0 ? 3.0 : w);
+        }
+    }
+    st.x = (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+    st.y = (double*)calloc((size_t)(m > 0 ? m : 1), sizeof(double));
+    st.xavg = (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+    st.yavg = (double*)calloc((size_t)(m > 0 ? m : 1), sizeof(double));
+    st.axcur = (double*)calloc((size_t)(m > 0 ? m : 1), sizeof(double));
+    st.k = 1;
+    st.hn = 0;
+    double* xb = (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
+    double* yb = (double*)calloc((size_t)(m > 0 ? m : 1), sizeof(double));
+    double* pesx = (double*)malloc(nb);
+    double* pesy = (double*)malloc(mb);
+    double *hx = (double*)malloc(nb), *hy = (double*)malloc(mb),
+           *hax = (double*)malloc(mb), *hd = (double*)malloc(nb);
+    double *tm = (double*)malloc(mb), *ta = (double*)malloc(nb);
+    orc_scratch w;
+    scratch_alloc(&w, m, n);
+
+    const int CHECK = opt->check_period > 0 ? opt->check_period : 64;
+    const int64_t MAXIT = (opt->time_limit_s > 0 && opt->time_limit_s < 1e6)
+                              ? 20000000LL
+                              : opt->max_iterations;
+    const double TOL = opt->tolerance;
+    double epoch_kkt = -1.0, prev_cand = ORC_INF;
+    int64_t epoch_start = 0;
+    int have_pe = 0;
+    int64_t iters_run = 0, attempts = 0, restarts = 0, checks = 0;
+    int timed_out = 0;
+    orc_metrics last, inc;
+    memset(&last, 0, sizeof(last));
+    memset(&inc, 0, sizeof(inc));
+    int last_is_avg = 0, have_inc = 0, have_last = 0;
+    double inc_op = 0.0;
+    int64_t last_rollback = 0;
+
+#define METRICS_OF(XS, YS, MT)                                                \
+    do {                                                                      \
+        for (int j = 0; j < n; ++j) hx[j] = (XS)[j] * dc[j];                  \
+        for (int i = 0; i < m; ++i) hy[i] = (YS)[i] * (1.0 / dr[i]);          \
+        orc_spmv(m, lp->ap, lp->ai, sax, (XS), tm, th);                       \
+        for (int i = 0; i < m; ++i) hax[i] = tm[i] * dr[i];                   \
+        orc_spmv(n, lp->cp, lp->ci, sacx, (YS), ta, th);                      \
+        for (int j = 0; j < n; ++j) hd[j] = lp->c[j] + 1.0 * ta[j] / dc[j];   \
+        orc_evaluate(m, n, lp->rmin, lp->rmax, lp->cl, lp->cu, lp->c, hx, hy, \
+                     hax, hd, &(MT));                                         \
+    } while (0)
+
+    for (int64_t k = 1; k <= MAXIT; ++k) {
+        iters_run = k;
+        st.k = k;
+        attempts += one_iteration(m, n, lp->ap, lp->ai, sax, lp->cp, lp->ci,
+                                  sacx, sc, scl, scu, srmin, srmax, &st, &w, th);
+        if (k % CHECK != 0) continue;
+        ++checks;
+        orc_metrics mc, ma;
+        METRICS_OF(st.x, st.y, mc);
+        METRICS_OF(st.xavg, st.yavg, ma);
+        const double ec = metrics_finite(&mc) ? metrics_err(&mc) : ORC_INF;
+        const double ea = metrics_finite(&ma) ? metrics_err(&ma) : ORC_INF;
+        last = (ec <= ea) ? mc : ma;
+        last_is_avg = (ea < ec);
+        have_last = 1;
+        {
+#define PASSES(t) ((t).pinf <= TOL && (t).dinf <= TOL && (t).prow <= TOL && \
+                   isfinite((t).gap) && (t).gap <= TOL)
+            if (PASSES(mc)) { last = mc; last_is_avg = 0; break; }
+            if (PASSES(ma)) { last = ma; last_is_avg = 1; break; }
+#undef PASSES
+        }
+        /* incumbent, reference :937-958 */
+        int inc_src = -1;
+        for (int c = 0; c < 2; ++c) {
+            const orc_metrics* t = c ? &ma : &mc;
+            if (t->pinf <= 1e-4 && isfinite(t->op) && (!have_inc || t->op < inc_op)) {
+                have_inc = 1;
+                inc_op = t->op;
+                inc = *t;
+                inc_src = c;
+            }
+        }
+        if (inc_src >= 0) {
+            memcpy(xb, inc_src ? st.xavg : st.x, nb);
+            memcpy(yb, inc_src ? st.yavg : st.y, mb);
+        }
+        /* rollback, reference :965-988 */
+        if (mc.pinf >= 0.5 && have_inc && k - last_rollback > 2000) {
+            memcpy(st.x, xb, nb);
+            memcpy(st.y, yb, mb);
+            memcpy(st.xavg, xb, nb);
+            memcpy(st.yavg, yb, mb);
+            st.eta = smin(st.eta, 0.5 * eta0);
+            st.hn = 0;
+            epoch_start = k;
+            epoch_kkt = -1.0;
+            prev_cand = ORC_INF;
+            orc_spmv(m, lp->ap, lp->ai, sax, st.x, st.axcur, th);
+            last_rollback = k;
+        }
+        /* restart + primal weight, reference :1001-1075 */
+        const double cand = smin(ec, ea);
+        if (epoch_kkt < 0.0) {
+            epoch_kkt = cand;
+            prev_cand = cand;
+        }
+        const int64_t t_epoch = k - epoch_start;
+        const int restart_now =
+            (isfinite(cand) && isfinite(epoch_kkt) && epoch_kkt > 0.0 &&
+             (cand <= 0.2 * epoch_kkt ||
+              (cand <= 0.8 * epoch_kkt && isfinite(prev_cand) &&
+               cand > prev_cand))) ||
+            (double)t_epoch >= 0.36 * (double)k;
+        prev_cand = cand;
+        if (restart_now) {
+            ++restarts;
+            if (ea < ec) {
+                memcpy(st.x, st.xavg, nb);
+                memcpy(st.y, st.yavg, mb);
+            }
+            memcpy(st.xavg, st.x, nb);
+            memcpy(st.yavg, st.y, mb);
+            st.hn = 0;
+            epoch_start = k;
+            epoch_kkt = cand;
+            prev_cand = ORC_INF;
+            orc_spmv(m, lp->ap, lp->ai, sax, st.x, st.axcur, th);
+            if (have_pe) {
+                double dxn = 0.0, dyn = 0.0;
+                for (int j = 0; j < n; ++j) {
+                    double d = st.x[j] - pesx[j];
+                    dxn += d * d;
+                }
+                for (int i = 0; i < m; ++i) {
+                    double d = st.y[i] - pesy[i];
+                    dyn += d * d;
+                }
+                if (dxn > 1e-24 && dyn > 1e-24) {
+                    double om = sqrt(st.omega * sqrt(dyn / dxn));
+                    if (isfinite(om) && om > 0.0)
+                        st.omega = om < 1e-6 ? 1e-6 : (om > 1e6 ? 1e6 : om);
+                }
+            } else {
+                have_pe = 1;
+            }
+            memcpy(pesx, st.x, nb);
+            memcpy(pesy, st.y, mb);
+        }
+        if (now_s() - t0 > opt->time_limit_s) {
+            timed_out = 1;
+            break;
+        }
+    }
+    const double secs = now_s() - t0;
+    if (!have_last) {
+        /* The reference leaves `last` zero-initialised when no check ran
+         * (fewer than 64 iterations), which reads as certified; evaluate the
+         * final iterate instead. */
+        orc_metrics mc;
+        METRICS_OF(st.x, st.y, mc);
+        last = mc;
+        last_is_avg = 0;
+    }
+#undef METRICS_OF
+#define CERTIFIED(t) ((t).pinf <= TOL && (t).prow <= TOL && isfinite((t).gap) && \
+                      (t).gap <= TOL)
+    if (timed_out) res->status = 6;
+    else res->status = CERTIFIED(last) ? 1 : 5;
+    const double* fx = last_is_avg ? st.xavg : st.x;
+    const double* fy = last_is_avg ? st.yavg : st.y;
+    if (!CERTIFIED(last) && have_inc && inc.pinf <= TOL && isfinite(inc.op) &&
+        (inc.op < last.op || last.pinf > TOL)) {
+        last = inc;
+        fx = xb;
+        fy = yb;
+    }
+#undef CERTIFIED
+    res->objective = last.op + lp->obj_const;
+    res->pinf = last.pinf;
+    res->dinf = last.dinf;
+    res->gap = last.gap;
+    res->prow = last.prow;
+    res->iterations = iters_run;
+    res->attempts = attempts;
+    res->restarts = restarts;
+    res->checks = checks;
+    res->seconds = secs;
+    res->eta = st.eta;
+    res->omega = st.omega;
+    if (xout)
+        for (int j = 0; j < n; ++j) xout[j] = fx[j] * dc[j];
+    if (yout)
+        for (int i = 0; i < m; ++i) yout[i] = 1.0 * fy[i] / dr[i];
+
+    scratch_free(&w);
+    free(st.x); free(st.y); free(st.xavg); free(st.yavg); free(st.axcur);
+    free(xb); free(yb); free(pesx); free(pesy);
+    free(hx); free(hy); free(hax); free(hd); free(tm); free(ta);
+    free(dr); free(dc); free(sax); free(sacx);
+    free(sc); free(scl); free(scu); free(srmin); free(srmax);
+    return 0;
+}

@@ -1,0 +1,85 @@
+// Exposes helpers of the reference PDHG engine through a C ABI so the oracle
+// can be pinned against them. The reference translation unit is compiled
+// as-is (it is included, not copied): its internal evaluate() sits in an
+// anonymous namespace and is only reachable from inside the same unit.
+// Built by oracle/Makefile into oracle/_ref/; test infrastructure only.
+#include "pdhg.cu"  // reference src/pdhg/pdhg.cu (include path set by the Makefile)
+
+#include <cstring>
+#include <tuple>
+#include <vector>
+
+extern "C" {
+
+void ref_evaluate(int m, int n, const double* rmin, const double* rmax,
+                  const double* cl, const double* cu, const double* c,
+                  const double* x, const double* y, const double* Ax,
+                  const double* d, double* out6) {
+    std::vector<double> vrmin(rmin, rmin + m), vrmax(rmax, rmax + m),
+        vcl(cl, cl + n), vcu(cu, cu + n), vc(c, c + n), vx(x, x + n),
+        vy(y, y + m), vAx(Ax, Ax + m), vd(d, d + n);
+    auto mt = igaos::pdhg::evaluate(m, n, vrmin, vrmax, vcl, vcu, vc, vx, vy,
+                                    vAx, vd);
+    out6[0] = mt.pinf;
+    out6[1] = mt.dinf;
+    out6[2] = mt.gap;
+    out6[3] = mt.op;
+    out6[4] = mt.od;
+    out6[5] = mt.prow;
+}
+
+void ref_counting_sort(long nt, const int* ti, const int* tj, const double* tv,
+                       int rows, int cols, int* ap, int* ai, double* ax,
+                       int* cp, int* ci, double* acx) {
+    std::vector<std::tuple<int, int, double>> trips;
+    trips.reserve(nt);
+    for (long t = 0; t < nt; ++t) trips.emplace_back(ti[t], tj[t], tv[t]);
+    std::vector<int> vap, vai, vcp, vci;
+    std::vector<double> vax, vacx;
+    igaos::io::counting_sort(trips, rows, cols, vap, vai, vax, vcp, vci, vacx);
+    std::memcpy(ap, vap.data(), sizeof(int) * vap.size());
+    std::memcpy(cp, vcp.data(), sizeof(int) * vcp.size());
+    if (nt > 0) {
+        std::memcpy(ai, vai.data(), sizeof(int) * nt);
+        std::memcpy(ax, vax.data(), sizeof(double) * nt);
+        std::memcpy(ci, vci.data(), sizeof(int) * nt);
+        std::memcpy(acx, vacx.data(), sizeof(double) * nt);
+    }
+}
+
+// MPS reader: parse into a static model, then fetch arrays.
+static igaos::io::Model g_model;
+
+int ref_parse_mps(const char* path, int* m, int* n, long* nnz,
+                  double* obj_const) {
+    g_model = igaos::io::Model();
+    try {
+        igaos::io::parse_mps(path, g_model);
+    } catch (...) {
+        return 1;
+    }
+    *m = g_model.m;
+    *n = g_model.n;
+    *nnz = g_model.nnz();
+    *obj_const = g_model.obj_const;
+    return 0;
+}
+
+void ref_fetch_model(int* ap, int* ai, double* ax, int* cp, int* ci,
+                     double* acx, double* c, double* cl, double* cu,
+                     double* rmin, double* rmax) {
+    const auto& M = g_model;
+    std::memcpy(ap, M.ap.data(), sizeof(int) * M.ap.size());
+    std::memcpy(cp, M.cp.data(), sizeof(int) * M.cp.size());
+    std::memcpy(ai, M.ai.data(), sizeof(int) * M.ai.size());
+    std::memcpy(ax, M.ax.data(), sizeof(double) * M.ax.size());
+    std::memcpy(ci, M.ci.data(), sizeof(int) * M.ci.size());
+    std::memcpy(acx, M.acx.data(), sizeof(double) * M.acx.size());
+    std::memcpy(c, M.c.data(), sizeof(double) * M.c.size());
+    std::memcpy(cl, M.cl.data(), sizeof(double) * M.cl.size());
+    std::memcpy(cu, M.cu.data(), sizeof(double) * M.cu.size());
+    std::memcpy(rmin, M.rmin.data(), sizeof(double) * M.rmin.size());
+    std::memcpy(rmax, M.rmax.data(), sizeof(double) * M.rmax.size());
+}
+
+}  // extern "C"

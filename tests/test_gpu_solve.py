@@ -1,0 +1,129 @@
+"""End-to-end parity of GPU solves through the C ABI against the reference
+simplex optimum (golden fixtures made by tests/golden/make_golden.py from the
+reference's own simplex) and against the CPU oracle of the reference PDHG.
+
+Objective parity bar: |obj - obj_ref| / max(1, |obj_ref|) <= 1e-6 at a
+relative-KKT tolerance of 1e-8 (FP64, FP32+refine); FP32 without refinement
+is only held to its own tolerance.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from igaos_gb300 import generators as G
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = json.load(open(os.path.join(HERE, "golden", "lp_objectives.json")))
+
+
+def make(name):
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    from make_golden import checksum, make_lp
+    e = GOLD[name]
+    lp = make_lp(e["generator"], e["kwargs"])
+    assert checksum(lp) == e["checksum"], "generator drift: regenerate tests/golden"
+    return lp, e["simplex_objective"]
+
+
+def rel(a, b):
+    return abs(a - b) / max(1.0, abs(b))
+
+
+@pytest.mark.parametrize("name", sorted(GOLD))
+def test_fp64_matches_simplex(native, name):
+    from igaos_gb300 import capi
+    lp, ref = make(name)
+    r = capi.solve_lp(lp, tolerance=1e-8, time_limit=60.0)
+    assert r["status_name"] == "near-optimal", r["message"]
+    assert rel(r["objective"], ref) <= 1e-6, (r["objective"], ref)
+    assert r["pinf"] <= 1e-8 and r["dinf"] <= 1e-8 and r["rel_gap"] <= 1e-8 and r["prow"] <= 1e-8
+
+
+@pytest.mark.parametrize("name", ["rand60x150-s0", "mixed80x200-s1", "zipf400x1000"])
+def test_fp64_tracks_oracle_pdhg(native, orc, name):
+    """Same algorithm on both sides: the iteration counts agree closely and the
+    objectives agree to the tolerance."""
+    from igaos_gb300 import capi
+    lp, ref = make(name)
+    want = orc.pdhg_solve(orc.lp_from(lp), tolerance=1e-6, time_limit=60.0)
+    got = capi.solve_lp(lp, tolerance=1e-6, time_limit=60.0)
+    assert got["status_name"] == want["status_name"] == "near-optimal"
+    assert rel(got["objective"], want["objective"]) <= 1e-5
+    assert abs(got["iterations"] - want["iterations"]) <= max(64, 0.25 * want["iterations"])
+
+
+def test_solution_vectors_certify(native, orc):
+    """x, y returned in original units reproduce the reported metrics under the
+    oracle's evaluate()."""
+    from igaos_gb300 import capi
+    lp, ref = make("rand200x500-s0")
+    r = capi.solve_lp(lp, tolerance=1e-8, time_limit=60.0)
+    olp = orc.lp_from(lp)
+    Ax = orc.spmv(olp.ap, olp.ai, olp.ax, r["x"])
+    d = lp.c + orc.spmv(olp.cp, olp.ci, olp.acx, r["y"])
+    m = orc.evaluate(olp, r["x"], r["y"], Ax, d)
+    assert m["pinf"] <= 1e-8 and m["prow"] <= 1e-8 and m["gap"] <= 1e-8 and m["dinf"] <= 1e-8
+    assert rel(m["op"] + lp.obj_const, ref) <= 1e-6
+
+
+def test_deterministic_repeat(native):
+    from igaos_gb300 import capi
+    lp, _ = make("zipf400x1000")
+    with capi.Problem(lp) as P:
+        a = P.solve(tolerance=1e-6, time_limit=60.0)
+        b = P.solve(tolerance=1e-6, time_limit=60.0)
+    assert a["objective"] == b["objective"] and a["iterations"] == b["iterations"]
+    assert np.array_equal(a["x"], b["x"])
+
+
+def test_graphs_and_direct_launch_agree(native):
+    from igaos_gb300 import capi
+    lp, _ = make("mixed80x200-s0")
+    a = capi.solve_lp(lp, tolerance=1e-6, time_limit=60.0, use_graphs=1)
+    b = capi.solve_lp(lp, tolerance=1e-6, time_limit=60.0, use_graphs=0)
+    assert a["objective"] == b["objective"] and a["iterations"] == b["iterations"]
+
+
+def test_fp32_reaches_its_tolerance(native):
+    from igaos_gb300 import capi
+    lp, ref = make("rand200x500-s1")
+    r = capi.solve_lp(lp, tolerance=1e-4, time_limit=60.0, precision="fp32")
+    assert r["status_name"] == "near-optimal", r["message"]
+    assert rel(r["objective"], ref) <= 1e-3
+
+
+def test_iteration_limit_and_time_limit(native):
+    from igaos_gb300 import capi
+    lp, _ = make("rand200x500-s0")
+    # max_iterations binds only without a finite time limit (src/pdhg/pdhg.cu:669-671)
+    r = capi.solve_lp(lp, tolerance=1e-12, time_limit=0.0, max_iterations=200)
+    assert r["status_name"] == "iteration-limit" and r["iterations"] == 200
+    r = capi.solve_lp(lp, tolerance=1e-14, time_limit=0.05)
+    assert r["status_name"] == "time-limit"
+    assert r["message"] == "wall-clock budget exhausted"
+
+
+def test_short_run_without_check_is_not_certified(native):
+    """Fewer iterations than one check period: the final iterate is evaluated
+    (the reference would report its zero-initialised metrics as certified)."""
+    from igaos_gb300 import capi
+    lp, _ = make("rand200x500-s0")
+    r = capi.solve_lp(lp, tolerance=1e-8, time_limit=0.0, max_iterations=10)
+    assert r["iterations"] == 10 and r["status_name"] == "iteration-limit"
+
+
+def test_c1_full_size_matches_simplex(native):
+    path = os.path.join(HERE, "golden", "c1_objectives.json")
+    if not os.path.exists(path):
+        pytest.skip("c1 golden not generated")
+    from igaos_gb300 import capi
+    gold = json.load(open(path))
+    e = gold["c1-s0"]
+    lp = G.config1(seed=0)
+    r = capi.solve_lp(lp, tolerance=1e-8, time_limit=120.0)
+    assert r["status_name"] == "near-optimal", r["message"]
+    assert rel(r["objective"], e["simplex_objective"]) <= 1e-6
