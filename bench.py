@@ -1,0 +1,296 @@
+"""Benchmark of the GB300 PDHG LP engine on the large sparse LP shape.
+
+Workload (one step): the large sparse LP (m=200,000 rows, half equality half
+<=, n=500,000 box-bounded columns, ~5.2M nonzeros with Zipf(1.5) column
+degrees and |A_ij| log-uniform in [1e-3, 1e3]; seeded synthetic data), one
+solve call of ITERS accepted PDHG iterations in FP32 (FP64 KKT checks every
+64 iterations), from a cold start on device-resident data.
+
+value: SpMV GB/s -- algorithmic bytes of every fused A^T y / A xbar attempt
+of the solve divided by the solve's CUDA-event device time (checks, restarts
+and host round trips included). Algorithmic bytes per attempt (s = 4 for
+FP32, 8 for FP64; int32 indices):
+    2*nnz*(s+4) + 4*(m+n+2) + s*9*(m+n)
+(each matrix entry and index once per orientation, row/column pointers once,
+nine m- and nine n-vectors read or written once each: x, xavg, c, l, u, xbar
+and y, A x, yavg, rmin, rmax gathered/read; x', xavg', xbar, y', A x', yavg'
+written).
+e2e: the same metric through the C ABI with HOST buffers: igaos_pdhg_solve_csr
+(upload, device setup, solve, download, free) timed on the host.
+L2: flushed (512 MiB write) between steps. Reference arm and cpu_baseline:
+the CPU oracle of the reference FP64 PDHG (tests' checker) on the machine's host
+cores over a bounded sample of the same solve.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "time-to-1e-8 rel KKT & SpMV GB/s: FP32+refine vs FP64 PDHG; batched LPs/sec"
+
+
+def bytes_per_attempt(m, n, nnz, s):
+    return 2 * nnz * (s + 4) + 4 * (m + n + 2) + s * 9 * (m + n)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile(key):
+    """Per-launch DRAM bytes of the fused attempt from the committed ncu
+    summary (profiles/roofline_traffic.txt: `key bytes` lines), if any."""
+    path = os.path.join(ROOT, "profiles", "roofline_traffic.txt")
+    try:
+        for line in open(path):
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == key:
+                return float(parts[1])
+    except OSError:
+        pass
+    return None
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(device), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm = [float(r[1]) for r in rows if len(r) > 8 and r[1].strip().replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in rows if len(r) > 8 and r[2].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows if len(r) > 8 for i in range(4)
+                          if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(sm)}
+
+
+def dist():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def barrier_max(value, ws):
+    if ws == 1:
+        return value
+    import torch
+    import torch.distributed as td
+    t = torch.tensor([value], dtype=torch.float64,
+                     device="cuda" if td.get_backend() == "nccl" else "cpu")
+    td.all_reduce(t, op=td.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as td
+        td.barrier()
+
+
+def cpu_sample(lp, iters, threads):
+    """The oracle of the reference FP64 PDHG on the host cores: GB/s of its
+    SpMVs (FP64 values) over a bounded number of iterations."""
+    from oracle import oracle as O
+    olp = O.lp_from(lp)
+    r = O.pdhg_solve(olp, tolerance=1e-12, time_limit=0.0, max_iterations=iters, threads=threads)
+    b = bytes_per_attempt(lp.m, lp.n, lp.nnz, 8) * r["attempts"]
+    return b / r["loop_seconds"] / 1e9, r
+
+
+def run_reference(args, lp, ws, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup and 1):
+        cpu_sample(lp, 8, threads)
+    vals = []
+    sample = None
+    for _ in range(args.steps):
+        v, r = cpu_sample(lp, args.cpu_iters, threads)
+        vals.append(v)
+        sample = r
+    value = statistics.mean(vals)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "GB/s",
+        "n_gpus": ws, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * sample["loop_seconds"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": config_dict(lp, args),
+        "cpu_baseline": {"value": value, "unit": "GB/s", "cores": threads, "kind": "port",
+                         "sample": f"{args.cpu_iters} iterations of the reference FP64 PDHG "
+                                   f"(CPU oracle, OpenMP) on the same LP, per step"},
+        "e2e": {"value": value, "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "gpu_launches": 0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def config_dict(lp, args):
+    return {"workload": "large sparse LP (m=200k, n=500k, ~5.2M nnz, Zipf(1.5) column "
+                        "degrees, |A_ij| log-uniform [1e-3,1e3], box [0,10]); one solve of "
+                        f"{args.iters} PDHG iterations per step",
+            "m": lp.m, "n": lp.n, "nnz": lp.nnz, "precision": args.precision,
+            "iters_per_step": args.iters, "l2": "flushed between steps (512 MiB write)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--iters", type=int, default=2048)
+    ap.add_argument("--precision", default="fp32", choices=["fp32", "fp64", "fp32-refine"])
+    ap.add_argument("--cpu-iters", type=int, default=64)
+    ap.add_argument("--scale", type=float, default=1.0, help="shrink the LP (testing only)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--tol-probe", type=float, default=0.0,
+                    help="also report time-to-tolerance probes within this many seconds")
+    args = ap.parse_args()
+    args.warmup = max(3, args.warmup)
+    ws, rank, local = dist()
+    from igaos_gb300 import generators as G
+    s = args.scale
+    lp = G.config2(seed=0, m=int(200_000 * s), n=int(500_000 * s), target_nnz=int(5_000_000 * s))
+    if args.impl == "reference":
+        if ws > 1:
+            import torch.distributed as td
+            td.init_process_group("gloo")
+        run_reference(args, lp, ws, rank)
+        return
+
+    import torch
+    if ws > 1:
+        import torch.distributed as td
+        td.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    from igaos_gb300 import capi
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
+    opts = dict(precision=args.precision, tolerance=1e-12, time_limit=0.0,
+                max_iterations=args.iters, device=local)
+    bpa = bytes_per_attempt(lp.m, lp.n, lp.nnz, 8 if args.precision == "fp64" else 4)
+    with capi.Problem(lp, device=local) as P:
+        for _ in range(args.warmup):
+            P.solve(**opts)
+        clocks = Clocks(local)
+        barrier(ws)
+        torch.cuda.synchronize()
+        res = []
+        for _ in range(args.steps):
+            flush.fill_(1)
+            torch.cuda.synchronize()
+            res.append(P.solve(**opts))
+        torch.cuda.synchronize()
+        barrier(ws)
+        ck = clocks.stop()
+    dev_ms = sum(r["device_time_ms"] for r in res)
+    att = sum(r["attempts"] for r in res)
+    att_ms = sum(r["attempt_time_ms"] for r in res)
+    launches = sum(r["launches"] for r in res)
+    dev_ms_max = barrier_max(dev_ms, ws)
+    value = ws * bpa * att / (dev_ms_max / 1e3) / 1e9
+    # e2e through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        h2d = sum(np.asarray(a).nbytes for a in (lp.ap, lp.ai, lp.ax, lp.cp, lp.ci, lp.acx, lp.c,
+                                                   lp.cl, lp.cu, lp.rmin, lp.rmax))
+        d2h = 8 * (lp.m + lp.n)
+        e_steps = min(args.steps, 3)
+        capi.solve_lp(lp, **opts)
+        barrier(ws)
+        t0 = time.perf_counter()
+        e_att = 0
+        for _ in range(e_steps):
+            r = capi.solve_lp(lp, **opts)
+            e_att += r["attempts"]
+        torch.cuda.synchronize()
+        el = barrier_max(time.perf_counter() - t0, ws)
+        e2e = {"value": ws * bpa * e_att / el / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * el / e_steps}
+    # time-to-tolerance probes (not part of `value`)
+    probes = {}
+    if args.tol_probe > 0:
+        with capi.Problem(lp, device=local) as P:
+            for prec in ("fp32", "fp64"):
+                for tol in (1e-4, 1e-8):
+                    r = P.solve(precision=prec, tolerance=tol, time_limit=args.tol_probe)
+                    probes[f"{prec}@{tol:g}"] = {
+                        "status": r["status_name"], "device_s": r["device_time_ms"] / 1e3,
+                        "iterations": r["iterations"], "pinf": r["pinf"], "dinf": r["dinf"],
+                        "rel_gap": r["rel_gap"]}
+    if rank != 0:
+        return
+    pk, pk_kind = peaks()
+    achieved = bpa * att / (att_ms / 1e3) / 1e9
+    traffic = traffic_from_profile(f"fused_attempt_{args.precision}_{'c2' if s == 1.0 else 'scaled'}")
+    if args.no_cpu:
+        cpu_v, cpu_r = None, {"loop_seconds": 0.0}
+    else:
+        cpu_v, cpu_r = cpu_sample(lp, args.cpu_iters, os.cpu_count() or 1)
+    line = {
+        "metric": METRIC, "value": value, "unit": "GB/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dev_ms_max / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic",
+        "config": config_dict(lp, args),
+        "roofline": {"kernel": "fused PDHG attempt (k_primal: A^T y + primal step; k_dual: "
+                               "A xbar + dual step + step decision)",
+                     "bound": "hbm", "achieved": achieved, "peak": pk, "peak_kind": pk_kind,
+                     "unit": "GB/s", "frac": achieved / pk,
+                     "bytes_per_launch": bpa, "launch_us": 1e3 * att_ms / att,
+                     "traffic": traffic},
+        "cpu_baseline": {"value": cpu_v, "unit": "GB/s", "cores": os.cpu_count(),
+                         "kind": "port",
+                         "sample": f"{args.cpu_iters} iterations of the reference FP64 PDHG "
+                                   f"(CPU oracle, OpenMP) on the same LP ({cpu_r['loop_seconds']:.1f} s)"},
+        "e2e": e2e,
+        "gpu_launches": launches,
+        "clocks": ck,
+        "kkt_passes_per_s": ws * att / (dev_ms_max / 1e3),
+        "iterations_per_step": res[-1]["iterations"], "attempts_per_step": res[-1]["attempts"],
+    }
+    if probes:
+        line["time_to_tol"] = probes
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

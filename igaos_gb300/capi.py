@@ -42,7 +42,8 @@ class Result(C.Structure):
         ("kkt_checks", C.c_int64), ("restarts", C.c_int64), ("kkt_passes", C.c_int64),
         ("refinements", C.c_int), ("solve_time_ms", C.c_double),
         ("setup_time_ms", C.c_double), ("device_time_ms", C.c_double),
-        ("attempt_time_ms", C.c_double), ("message", C.c_char * 160),
+        ("attempt_time_ms", C.c_double), ("launches", C.c_int64),
+        ("message", C.c_char * 160),
     ]
 
     def as_dict(self):
@@ -109,10 +110,15 @@ def _i(a):
     return None if a is None else a.ctypes.data_as(_ip)
 
 
+# igaos.solve keyword names (python/igaos_bindings.cpp:26-28) -> option fields
+_ALIASES = {"time_limit": "time_limit_s"}
+
+
 def default_options(**kw) -> Options:
     o = Options()
     lib().igaos_pdhg_default_options(C.byref(o))
     for k, v in kw.items():
+        k = _ALIASES.get(k, k)
         if k == "precision" and isinstance(v, str):
             v = PRECISIONS[v]
         if not hasattr(o, k):

@@ -59,7 +59,22 @@ struct DevCtl {
     int nan_flag;
     unsigned int ticket;  // last-CTA-done counter of the dual-side launch
     unsigned int ticket2; // counter for KKT / reduction launches
+    // Step quantities derived once per decision (ctl_derive), so that no CTA
+    // of the hot kernels spends FP64 divisions on them: tau = eta/omega,
+    // sigma = eta*omega (src/pdhg/pdhg.cu:756) and the averaging weight
+    // w = 2/(hn+2) (:795), in FP64 and rounded to FP32.
+    double tau, sigma, w;
+    float tau_f, sigma_f, w_f, pad_f;
 };
+
+__host__ __device__ inline void ctl_derive(DevCtl* c) {
+    c->tau = c->eta / c->omega;
+    c->sigma = c->eta * c->omega;
+    c->w = 2.0 / ((double)c->hn + 2.0);
+    c->tau_f = (float)c->tau;
+    c->sigma_f = (float)c->sigma;
+    c->w_f = (float)c->w;
+}
 
 // FP64 KKT metrics of one candidate (see k_kkt_* in kernels.cuh).
 struct DevMetrics {
@@ -160,6 +175,30 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
     __syncthreads();
 }
 
+// Same tree in the working precision (FP32 partials of FP32 kernels; the
+// cross-CTA finish is FP64). `sh` needs kWarps * NV values of type T.
+template <typename T, int NV>
+__device__ __forceinline__ void block_sum_t(T (&v)[NV], T* sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+        for (int o = 16; o > 0; o >>= 1) v[q] += __shfl_xor_sync(0xffffffffu, v[q], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh[w * NV + q] = v[q];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            T s = 0;
+            for (int k = 0; k < kWarps; ++k) s += sh[k * NV + q];
+            v[q] = s;
+        }
+    }
+    __syncthreads();
+}
+
 template <int NV>
 __device__ __forceinline__ void block_max(double (&v)[NV], double* sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -206,6 +245,8 @@ __device__ __forceinline__ bool last_cta(unsigned int* ticket) {
 template <typename T>
 struct TileSmem {
     typename Vec2<T>::type stage[kTileNnz];
+    alignas(16) unsigned char rsum_raw[kTileRows * sizeof(Acc<T>)];  // row sums
+    __device__ __forceinline__ Acc<T>* rsum() { return reinterpret_cast<Acc<T>*>(rsum_raw); }
     int rowptr[kTileRows + 1];
     double red[kWarps * 4];
 };
@@ -274,8 +315,11 @@ __device__ __forceinline__ void tile_rows(TileSmem<T>& sm, const TileSched& ts, 
             acc.add(v.x, v.y);
         }
         for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(gmask, o, G);
-        if (lane == 0) f(r0 + rr, acc);
+        if (lane == 0) sm.rsum()[rr] = acc;
     }
+    __syncthreads();
+    // epilogue: consecutive threads on consecutive rows (coalesced vectors)
+    for (int rr = threadIdx.x; rr < nrows; rr += kThreads) f(r0 + rr, sm.rsum()[rr]);
 }
 
 }  // namespace igx

@@ -256,6 +256,7 @@ template <> Csr<float> Engine::csrAT<float>() const { return Csr<float>{cp_, ci_
 
 template <typename T>
 void Engine::spmv_dev(bool transpose, const T* x, T* y) {
+    ++launches_;
     if (transpose)
         k_spmv<T, T><<<sAT_.ntiles, kThreads, 0, st_>>>(sAT_.view(), csrAT<T>(), x, y);
     else
@@ -364,6 +365,7 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     da.part_primal = w.part_p;
     da.n_primal = sAT_.ntiles;
     da.ctl = ctl_;
+    launches_ += 2LL * count;
     auto enqueue = [&](int cnt) {
         for (int a = 0; a < cnt; ++a) {
             k_primal<T><<<sAT_.ntiles, kThreads, 0, st_>>>(pa);
@@ -393,6 +395,7 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
 }
 
 void Engine::upload_ctl() {
+    ctl_derive(h_ctl_);
     CU(cudaMemcpyAsync(ctl_, h_ctl_, sizeof(DevCtl), cudaMemcpyHostToDevice, st_));
 }
 void Engine::download_ctl() {
@@ -451,6 +454,7 @@ void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* 
     ka.part = kkt_part_;
     ka.out = met_;
     ka.ticket = ticket_ + 2;
+    launches_ += 3;
     k_kkt_rows<T><<<dim3(sA_.ntiles, ncand), kThreads, 0, st_>>>(ka);
     k_kkt_cols<T><<<dim3(sAT_.ntiles, ncand), kThreads, 0, st_>>>(ka);
     k_kkt_rowdual<T><<<dim3(red_blocks_, ncand), kThreads, 0, st_>>>(ka, m);
@@ -574,6 +578,7 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
                 spmv_dev<T>(false, w.x[p], w.axc[p]);
                 ++out.spmvs;
                 if (have_pe) {
+                    ++launches_;
                     k_diffnorms<T><<<red_blocks_, kThreads, 0, st_>>>(
                         n, w.x[p], w.pesx, m, w.y[p], w.pesy, red_part_, scal_, ticket_ + 1);
                     CU(cudaGetLastError());
@@ -659,6 +664,7 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     }
     t0_ = std::chrono::steady_clock::now();
     attempt_ms_ = 0;
+    launches_ = 0;
     CU(cudaEventRecord(ev_[0], st_));
     LoopOpts lo;
     lo.tol = o.tolerance;
@@ -698,6 +704,7 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
         CU(cudaEventElapsedTime(&ms, ev_[0], ev_[1]));
         r.device_time_ms = ms;
         r.attempt_time_ms = attempt_ms_;
+        r.launches = launches_;
     }
     r.status = out.status;
     r.objective = out.last.op + obj_const;

@@ -149,6 +149,7 @@ class Engine {
     std::chrono::steady_clock::time_point t0_;
     cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
     double attempt_ms_ = 0;   // accumulated time of attempt launches
+    long long launches_ = 0;  // kernel launches of the current solve
 
     template <typename T> Work<T>& work();
     template <typename T> Csr<T> csrA() const;

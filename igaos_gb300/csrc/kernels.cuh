@@ -8,18 +8,20 @@ namespace igx {
 
 // ------------------------------------------------------------ attempt state
 // Per-launch view of the control block, read once per CTA.
+template <typename T>
 struct CtlView {
     int parity, stop;
-    double eta, omega, hn;
+    T tau, sigma, w;
 };
-__device__ __forceinline__ CtlView read_ctl(const DevCtl* c) {
-    CtlView v;
-    v.stop = *(volatile const int*)&c->stop;
-    v.parity = c->parity;
-    v.eta = c->eta;
-    v.omega = c->omega;
-    v.hn = (double)c->hn;
-    return v;
+template <typename T>
+__device__ __forceinline__ CtlView<T> read_ctl(const DevCtl* c);
+template <>
+__device__ __forceinline__ CtlView<double> read_ctl<double>(const DevCtl* c) {
+    return CtlView<double>{c->parity, *(volatile const int*)&c->stop, c->tau, c->sigma, c->w};
+}
+template <>
+__device__ __forceinline__ CtlView<float> read_ctl<float>(const DevCtl* c) {
+    return CtlView<float>{c->parity, *(volatile const int*)&c->stop, c->tau_f, c->sigma_f, c->w_f};
 }
 
 template <typename T>
@@ -46,11 +48,10 @@ struct PrimalArgs {
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_primal(PrimalArgs<T> a) {
     __shared__ TileSmem<T> sm;
-    const CtlView cv = read_ctl(a.ctl);
+    const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
     const int p = cv.parity, q = p ^ 1;
-    const T tau = (T)(cv.eta / cv.omega);
-    const T w = (T)(2.0 / (cv.hn + 2.0));
+    const T tau = cv.tau, w = cv.w;
     const T* __restrict__ xc = a.x[p];
     const T* __restrict__ xa = a.xavg[p];
     T* __restrict__ xn_out = a.x[q];
@@ -68,9 +69,9 @@ __global__ void __launch_bounds__(kThreads) k_primal(PrimalArgs<T> a) {
         xa_out[j] = fma(w, xn - av, av);
     };
     tile_rows<T>(sm, a.ts, a.AT, a.y[p], blockIdx.x, f);
-    double v[1] = {(double)dx2};
-    block_sum<1>(v, sm.red);
-    if (threadIdx.x == 0) a.part[blockIdx.x] = v[0];
+    T v[1] = {dx2};
+    block_sum_t<T, 1>(v, reinterpret_cast<T*>(sm.red));
+    if (threadIdx.x == 0) a.part[blockIdx.x] = (double)v[0];
 }
 
 template <typename T>
@@ -120,6 +121,7 @@ __device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cro
     } else {
         c->eta = smax(eta_new, 1e-12);
     }
+    ctl_derive(c);
 }
 
 // Dual half of one attempt, fused into the A xbar SpMV:
@@ -132,11 +134,10 @@ __device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cro
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
     __shared__ TileSmem<T> sm;
-    const CtlView cv = read_ctl(a.ctl);
+    const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
     const int p = cv.parity, q = p ^ 1;
-    const T sigma = (T)(cv.eta * cv.omega);
-    const T w = (T)(2.0 / (cv.hn + 2.0));
+    const T sigma = cv.sigma, w = cv.w;
     const T* __restrict__ yc = a.y[p];
     const T* __restrict__ axc = a.axc[p];
     const T* __restrict__ ya = a.yavg[p];
@@ -160,11 +161,11 @@ __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
         ya_out[i] = fma(w, yn - av, av);
     };
     tile_rows<T>(sm, a.ts, a.A, a.xbar, blockIdx.x, f);
-    double v[2] = {(double)dy2, (double)cross};
-    block_sum<2>(v, sm.red);
+    T v[2] = {dy2, cross};
+    block_sum_t<T, 2>(v, reinterpret_cast<T*>(sm.red));
     if (threadIdx.x == 0) {
-        a.part[2 * blockIdx.x] = v[0];
-        a.part[2 * blockIdx.x + 1] = v[1];
+        a.part[2 * blockIdx.x] = (double)v[0];
+        a.part[2 * blockIdx.x + 1] = (double)v[1];
     }
     if (!last_cta(&a.ctl->ticket)) return;
     double s[3] = {0.0, 0.0, 0.0};

@@ -95,6 +95,7 @@ typedef struct igaos_pdhg_result {
     double setup_time_ms;     /* upload + scaling + power iteration */
     double device_time_ms;    /* solve, CUDA events on the engine stream */
     double attempt_time_ms;   /* of which in line-search attempt launches */
+    int64_t launches;         /* engine kernel launches during the solve */
     char message[160];
 } igaos_pdhg_result;
 

@@ -60,7 +60,8 @@ class orc_result(C.Structure):
         ("dinf", C.c_double), ("gap", C.c_double), ("prow", C.c_double),
         ("iterations", C.c_int64), ("attempts", C.c_int64),
         ("restarts", C.c_int64), ("checks", C.c_int64),
-        ("seconds", C.c_double), ("eta", C.c_double), ("omega", C.c_double),
+        ("seconds", C.c_double), ("loop_seconds", C.c_double),
+        ("eta", C.c_double), ("omega", C.c_double),
     ]
 
 

@@ -454,6 +454,7 @@ int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
     st.axcur = (double*)calloc((size_t)(m > 0 ? m : 1), sizeof(double));
     st.k = 1;
     st.hn = 0;
+    const double t_loop = now_s();
     double* xb = (double*)calloc((size_t)(n > 0 ? n : 1), sizeof(double));
     double* yb = (double*)calloc((size_t)(m > 0 ? m : 1), sizeof(double));
     double* pesx = (double*)malloc(nb);
@@ -631,6 +632,7 @@ int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
     res->restarts = restarts;
     res->checks = checks;
     res->seconds = secs;
+    res->loop_seconds = now_s() - t_loop;
     res->eta = st.eta;
     res->omega = st.omega;
     if (xout)

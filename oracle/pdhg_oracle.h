@@ -51,7 +51,8 @@ typedef struct {
     int status; /* 1 near-optimal, 5 iteration-limit, 6 time-limit, 7 error */
     double objective, pinf, dinf, gap, prow;
     int64_t iterations, attempts, restarts, checks;
-    double seconds;
+    double seconds;      /* power iteration + iteration loop */
+    double loop_seconds; /* iteration loop only */
     double eta, omega; /* final step controller state (scaled units) */
 } orc_result;
 

@@ -33,7 +33,13 @@ def rel(a, b):
     return abs(a - b) / max(1.0, abs(b))
 
 
-@pytest.mark.parametrize("name", sorted(GOLD))
+# The reference's PDHG does not reach 1e-8 on the Zipf / log-uniform shape in
+# any practical budget (its own oracle plateaus at dinf ~1e-1 after 3.5M
+# iterations); that instance is covered by fixed-budget tracking below.
+CONVERGING = sorted(k for k in GOLD if not k.startswith("zipf"))
+
+
+@pytest.mark.parametrize("name", CONVERGING)
 def test_fp64_matches_simplex(native, name):
     from igaos_gb300 import capi
     lp, ref = make(name)
@@ -43,7 +49,7 @@ def test_fp64_matches_simplex(native, name):
     assert r["pinf"] <= 1e-8 and r["dinf"] <= 1e-8 and r["rel_gap"] <= 1e-8 and r["prow"] <= 1e-8
 
 
-@pytest.mark.parametrize("name", ["rand60x150-s0", "mixed80x200-s1", "zipf400x1000"])
+@pytest.mark.parametrize("name", ["rand60x150-s0", "mixed80x200-s1"])
 def test_fp64_tracks_oracle_pdhg(native, orc, name):
     """Same algorithm on both sides: the iteration counts agree closely and the
     objectives agree to the tolerance."""
@@ -54,6 +60,19 @@ def test_fp64_tracks_oracle_pdhg(native, orc, name):
     assert got["status_name"] == want["status_name"] == "near-optimal"
     assert rel(got["objective"], want["objective"]) <= 1e-5
     assert abs(got["iterations"] - want["iterations"]) <= max(64, 0.25 * want["iterations"])
+
+
+def test_fp64_fixed_budget_tracks_oracle_on_zipf(native, orc):
+    """On the shape where neither side converges, a fixed budget of the same
+    algorithm (checks, restarts and all) lands on the same point."""
+    from igaos_gb300 import capi
+    lp, _ = make("zipf400x1000")
+    want = orc.pdhg_solve(orc.lp_from(lp), tolerance=1e-12, time_limit=0.0, max_iterations=3000)
+    got = capi.solve_lp(lp, tolerance=1e-12, time_limit=0.0, max_iterations=3000)
+    assert got["iterations"] == want["iterations"] == 3000
+    assert got["restarts"] == want["restarts"]
+    assert rel(got["objective"], want["objective"]) <= 1e-6
+    assert got["pinf"] == pytest.approx(want["pinf"], rel=1e-3, abs=1e-12)
 
 
 def test_solution_vectors_certify(native, orc):
@@ -74,8 +93,8 @@ def test_deterministic_repeat(native):
     from igaos_gb300 import capi
     lp, _ = make("zipf400x1000")
     with capi.Problem(lp) as P:
-        a = P.solve(tolerance=1e-6, time_limit=60.0)
-        b = P.solve(tolerance=1e-6, time_limit=60.0)
+        a = P.solve(tolerance=1e-12, time_limit=0.0, max_iterations=3000)
+        b = P.solve(tolerance=1e-12, time_limit=0.0, max_iterations=3000)
     assert a["objective"] == b["objective"] and a["iterations"] == b["iterations"]
     assert np.array_equal(a["x"], b["x"])
 
