@@ -8,13 +8,14 @@
 // attempt costs no copy and an accepted one no swap on the host.
 //
 // The hot SpMV is tile-scheduled: the host cuts the rows into tiles of at
-// most kTileNnz nonzeros / kTileRows rows (a longer row is a tile of its own)
-// and picks, per tile, how many lanes cooperate on one row (1..32) from the
-// tile's row-length profile. A CTA streams its tile's values and column
-// indices with coalesced loads, gathers x through the read-only path, stages
-// (a_ij, x_j) pairs in shared memory and reduces each row with warp shuffles.
-// The PDHG step for that row runs in the same CTA right after its sum, so
-// A^T y / A xbar never round-trip through HBM.
+// most kTileNnz nonzeros / kTileRows rows (a longer row is a tile of its own).
+// A CTA streams its tile's values and column indices with coalesced loads,
+// gathers x through the read-only path, stages (a_ij, x_j) pairs in shared
+// memory and reduces the rows with a segmented sum balanced by nonzeros (every
+// thread owns the same number of staged entries, whatever the row lengths --
+// the Zipf-degree columns of the large LPs range from 1 to hundreds). The PDHG
+// step for each row then runs in the same CTA with consecutive threads on
+// consecutive rows, so A^T y / A xbar never round-trip through HBM.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -31,7 +32,7 @@ constexpr unsigned char kLongTile = 255;
 
 struct TileSched {
     const int* tile_row;           // ntiles + 1 row boundaries
-    const unsigned char* tile_lg;  // log2(lanes per row), or kLongTile
+    const unsigned char* tile_lg;  // 0, or kLongTile for a single long row
     int ntiles;
 };
 
@@ -53,6 +54,7 @@ struct DevCtl {
     long long attempts;  // total attempts
     long long accepted;  // total accepted iterations
     long long k_stop;    // raise `stop` once iteration k_stop is accepted
+    long long fac_base;  // iteration index of entry 0 of the step-factor table
     int retries;
     int parity;
     int stop;
@@ -220,6 +222,30 @@ __device__ __forceinline__ void block_max(double (&v)[NV], double* sh) {
     __syncthreads();
 }
 
+// Block-wide fixed-order merge of NV compensated accumulators; result in
+// thread 0. `sh` needs kWarps * NV entries.
+template <typename T, int NV>
+__device__ __forceinline__ void block_merge(Acc<T> (&v)[NV], Acc<T>* sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+        for (int o = 16; o > 0; o >>= 1) v[q].shfl_xor(0xffffffffu, o, 32);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh[w * NV + q] = v[q];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            Acc<T> s = sh[q];
+            for (int k = 1; k < kWarps; ++k) s.merge(sh[k * NV + q]);
+            v[q] = s;
+        }
+    }
+    __syncthreads();
+}
+
 // Last-CTA-done handshake: every CTA publishes its partials, fences, takes a
 // ticket; the CTA holding the last ticket sees every partial and resets the
 // counter for the next launch. No CTA waits on another.
@@ -245,8 +271,10 @@ __device__ __forceinline__ bool last_cta(unsigned int* ticket) {
 template <typename T>
 struct TileSmem {
     typename Vec2<T>::type stage[kTileNnz];
-    alignas(16) unsigned char rsum_raw[kTileRows * sizeof(Acc<T>)];  // row sums
+    alignas(16) unsigned char rsum_raw[kTileRows * sizeof(Acc<T>)];   // row sums
+    alignas(16) unsigned char carry_raw[kThreads * sizeof(Acc<T>)];   // per-chunk carry-out
     __device__ __forceinline__ Acc<T>* rsum() { return reinterpret_cast<Acc<T>*>(rsum_raw); }
+    __device__ __forceinline__ Acc<T>* carry() { return reinterpret_cast<Acc<T>*>(carry_raw); }
     int rowptr[kTileRows + 1];
     double red[kWarps * 4];
 };
@@ -303,19 +331,56 @@ __device__ __forceinline__ void tile_rows(TileSmem<T>& sm, const TileSched& ts, 
     }
     for (; q < cnt; q += kThreads) st[q] = mk2<T>(__ldg(A.val + p0 + q), __ldg(x + __ldg(A.idx + p0 + q)));
     __syncthreads();
-    const int G = 1 << lg;
-    const int grp = threadIdx.x >> lg, lane = threadIdx.x & (G - 1), ngrp = kThreads >> lg;
-    const unsigned gmask = (G == 32) ? 0xffffffffu
-                                     : (((1u << G) - 1u) << ((threadIdx.x & 31) & ~(G - 1)));
-    for (int rr = grp; rr < nrows; rr += ngrp) {
-        const int b = sm.rowptr[rr], e = sm.rowptr[rr + 1];
-        Acc<T> acc;
-        for (int k = b + lane; k < e; k += G) {
-            auto v = st[k];
-            acc.add(v.x, v.y);
+    // Segmented reduction, balanced by nonzeros: thread t owns the staged
+    // elements [t*E, t*E+E) whatever the row lengths. A row that closes inside
+    // its chunk is written directly; a row spanning chunks is summed by the
+    // thread that closes it, over the spanning threads' carry-out pieces in
+    // increasing order (deterministic).
+    const int* rp = sm.rowptr;
+    Acc<T>* rsum = sm.rsum();
+    Acc<T>* carry = sm.carry();
+    for (int rr = threadIdx.x; rr < nrows; rr += kThreads)
+        if (rp[rr] == rp[rr + 1]) rsum[rr] = Acc<T>();  // empty row
+    const int E = (cnt + kThreads - 1) / kThreads;
+    const int q0 = min((int)threadIdx.x * E, cnt), q1 = min(q0 + E, cnt);
+    Acc<T> head;
+    int head_row = -1;
+    Acc<T> acc;
+    if (q0 < q1) {
+        int lo = 0, hi = nrows - 1;  // first row with rp[i+1] > q0
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (rp[mid + 1] > q0) hi = mid;
+            else lo = mid + 1;
         }
-        for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(gmask, o, G);
-        if (lane == 0) sm.rsum()[rr] = acc;
+        int i = lo;
+        bool started_here = rp[i] == q0;
+        int end = rp[i + 1];
+        for (int k = q0; k < q1; ++k) {
+            const auto v = st[k];
+            acc.add(v.x, v.y);
+            if (k + 1 == end) {
+                if (started_here) {
+                    rsum[i] = acc;
+                } else {
+                    head = acc;
+                    head_row = i;
+                }
+                acc = Acc<T>();
+                ++i;
+                while (i < nrows && rp[i + 1] == rp[i]) ++i;
+                started_here = true;
+                end = i < nrows ? rp[i + 1] : cnt + 1;
+            }
+        }
+    }
+    carry[threadIdx.x] = acc;  // piece of a row that continues past the chunk
+    __syncthreads();
+    if (head_row >= 0) {
+        Acc<T> tot;
+        for (int s = rp[head_row] / E; s < (int)threadIdx.x; ++s) tot.merge(carry[s]);
+        tot.merge(head);
+        rsum[head_row] = tot;
     }
     __syncthreads();
     // epilogue: consecutive threads on consecutive rows (coalesced vectors)

@@ -38,31 +38,8 @@ void* Arena::raw(size_t bytes) {
 }
 
 // ---------------------------------------------------------- tile schedule
-// Lanes per row for one tile: the candidate width G minimising the busiest
-// group's work (rows are dealt round-robin to kThreads/G groups; a row costs
-// ceil(len/G) staged reads plus its shuffle tree and epilogue).
-static unsigned char pick_lanes(const int* ptr, int r0, int r1) {
-    long best = -1;
-    int best_lg = 0;
-    for (int lg = 0; lg <= 5; ++lg) {
-        const int G = 1 << lg, ngrp = kThreads >> lg;
-        long worst = 0;
-        for (int g = 0; g < ngrp && g < r1 - r0; ++g) {
-            long cost = 0;
-            for (int r = r0 + g; r < r1; r += ngrp) {
-                const int len = ptr[r + 1] - ptr[r];
-                cost += (len + G - 1) / G + lg + 2;
-            }
-            worst = std::max(worst, cost);
-        }
-        if (best < 0 || worst < best) {
-            best = worst;
-            best_lg = lg;
-        }
-    }
-    return (unsigned char)best_lg;
-}
-
+// Greedy cut of the rows into tiles of at most kTileNnz nonzeros and
+// kTileRows rows; a row longer than a tile becomes a long tile of its own.
 void build_tiles(const int* ptr, int rows, std::vector<int>& tile_row,
                  std::vector<unsigned char>& tile_lg) {
     tile_row.assign(1, 0);
@@ -85,7 +62,7 @@ void build_tiles(const int* ptr, int rows, std::vector<int>& tile_row,
             ++e;
         }
         tile_row.push_back(e);
-        tile_lg.push_back(pick_lanes(ptr, r, e));
+        tile_lg.push_back(0);
         r = e;
     }
 }
@@ -170,6 +147,8 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     CU(cudaMallocHost(&h_ctl_, sizeof(DevCtl)));
     CU(cudaMallocHost(&h_met_, 2 * sizeof(DevMetrics)));
     CU(cudaMallocHost(&h_scal_, 16 * sizeof(double)));
+    CU(cudaMallocHost(&h_fac_, 2 * kFac * sizeof(double)));
+    fac_ = ar_.alloc<double>(2 * kFac);
     std::memset(h_ctl_, 0, sizeof(DevCtl));
     red_blocks_ = grid_for(std::max(m, n), kThreads, 152 * 4);
     const int kkt_blocks = std::max(std::max(sA_.ntiles, sAT_.ntiles), red_blocks_);
@@ -215,6 +194,7 @@ Engine::~Engine() {
     if (h_ctl_) cudaFreeHost(h_ctl_);
     if (h_met_) cudaFreeHost(h_met_);
     if (h_scal_) cudaFreeHost(h_scal_);
+    if (h_fac_) cudaFreeHost(h_fac_);
     if (st_) cudaStreamDestroy(st_);
 }
 
@@ -348,7 +328,7 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
         pa.xavg[s] = w.xavg[s];
     }
     pa.xbar = w.xbar;
-    pa.part = w.part_p;
+    pa.part = reinterpret_cast<Acc<T>*>(w.part_p);
     pa.ctl = ctl_;
     DualArgs<T> da;
     da.ts = sA_.view();
@@ -361,9 +341,11 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
         da.axc[s] = w.axc[s];
         da.yavg[s] = w.yavg[s];
     }
-    da.part = w.part_d;
-    da.part_primal = w.part_p;
+    da.part = reinterpret_cast<Acc<T>*>(w.part_d);
+    da.part_primal = reinterpret_cast<const Acc<T>*>(w.part_p);
     da.n_primal = sAT_.ntiles;
+    da.fac = fac_;
+    da.n_fac = kFac;
     da.ctl = ctl_;
     launches_ += 2LL * count;
     auto enqueue = [&](int cnt) {
@@ -395,6 +377,20 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
 }
 
 void Engine::upload_ctl() {
+    // Step-growth factors 1 - k^-0.3 and 1 + k^-0.6 for the iterations the
+    // next launches can reach, computed with std::pow exactly as the
+    // reference does on the host (src/pdhg/pdhg.cu:778-782).
+    const long long k = h_ctl_->k;
+    if (fac_base_ < 1 || k < fac_base_ || h_ctl_->k_stop >= fac_base_ + kFac) {
+        fac_base_ = std::max(1LL, k);
+        for (int i = 0; i < kFac; ++i) {
+            const double kk = (double)(fac_base_ + i);
+            h_fac_[2 * i] = 1.0 - std::pow(kk, -0.3);
+            h_fac_[2 * i + 1] = 1.0 + std::pow(kk, -0.6);
+        }
+        CU(cudaMemcpyAsync(fac_, h_fac_, sizeof(double) * 2 * kFac, cudaMemcpyHostToDevice, st_));
+    }
+    h_ctl_->fac_base = fac_base_;
     ctl_derive(h_ctl_);
     CU(cudaMemcpyAsync(ctl_, h_ctl_, sizeof(DevCtl), cudaMemcpyHostToDevice, st_));
 }

@@ -149,6 +149,10 @@ class Engine {
     std::chrono::steady_clock::time_point t0_;
     cudaEvent_t ev_[4] = {nullptr, nullptr, nullptr, nullptr};
     double attempt_ms_ = 0;   // accumulated time of attempt launches
+    static constexpr int kFac = 512;  // step-factor table entries
+    double* fac_ = nullptr;   // device (1 - k^-0.3, 1 + k^-0.6) table
+    double* h_fac_ = nullptr; // pinned staging
+    long long fac_base_ = 0;  // iteration index of table entry 0 (0: empty)
     long long launches_ = 0;  // kernel launches of the current solve
 
     template <typename T> Work<T>& work();

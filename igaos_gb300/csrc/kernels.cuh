@@ -35,7 +35,7 @@ struct PrimalArgs {
     T* x[2];
     T* xavg[2];
     T* xbar;
-    double* part;           // per-CTA ||dx||^2
+    Acc<T>* part;           // per-CTA ||dx||^2 (compensated in FP32 kernels)
     DevCtl* ctl;
 };
 
@@ -71,7 +71,11 @@ __global__ void __launch_bounds__(kThreads) k_primal(PrimalArgs<T> a) {
     tile_rows<T>(sm, a.ts, a.AT, a.y[p], blockIdx.x, f);
     T v[1] = {dx2};
     block_sum_t<T, 1>(v, reinterpret_cast<T*>(sm.red));
-    if (threadIdx.x == 0) a.part[blockIdx.x] = (double)v[0];
+    if (threadIdx.x == 0) {
+        Acc<T> e;
+        e.s = v[0];
+        a.part[blockIdx.x] = e;
+    }
 }
 
 template <typename T>
@@ -84,8 +88,10 @@ struct DualArgs {
     T* y[2];
     T* axc[2];              // A x of the accepted iterate
     T* yavg[2];
-    double* part;           // per-CTA (||dy||^2, dy'A dx)
-    const double* part_primal;
+    Acc<T>* part;           // per-CTA (||dy||^2, dy'A dx)
+    const Acc<T>* part_primal;
+    const double* fac;      // (1 - k^-0.3, 1 + k^-0.6) for k = ctl->fac_base + i
+    int n_fac;
     int n_primal;
     DevCtl* ctl;
 };
@@ -93,7 +99,8 @@ struct DualArgs {
 // Adaptive step decision (src/pdhg/pdhg.cu:770-794), one thread. Host-side
 // arithmetic of the reference has no FMA contraction; the explicit _rn
 // intrinsics keep it that way here.
-__device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cross) {
+__device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cross,
+                                   const double* fac, int n_fac) {
     c->dots[0] = dx2;
     c->dots[1] = dy2;
     c->dots[2] = cross;
@@ -102,11 +109,20 @@ __device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cro
     const double num = __dadd_rn(__dmul_rn(omega, dx2), __ddiv_rn(dy2, omega));
     const double etabar =
         (num > 0.0 && cross > 0.0) ? __ddiv_rn(num, __dmul_rn(2.0, cross)) : CUDART_INF;
-    const double kk = (double)c->k;
+    // growth/shrink factors 1 - k^-0.3 and 1 + k^-0.6, tabulated by the host
+    // (std::pow, as the reference) for the iterations of this chunk
+    const long long fi = c->k - c->fac_base;
+    double f_lo, f_hi;
+    if (fac && fi >= 0 && fi < n_fac) {
+        f_lo = fac[2 * fi];
+        f_hi = fac[2 * fi + 1];
+    } else {
+        const double kk = (double)c->k;
+        f_lo = __dsub_rn(1.0, pow(kk, -0.3));
+        f_hi = __dadd_rn(1.0, pow(kk, -0.6));
+    }
     double eta_new = CUDART_INF;
-    if (isfinite(etabar))
-        eta_new = smin(__dmul_rn(__dsub_rn(1.0, pow(kk, -0.3)), etabar),
-                       __dmul_rn(__dadd_rn(1.0, pow(kk, -0.6)), eta));
+    if (isfinite(etabar)) eta_new = smin(__dmul_rn(f_lo, etabar), __dmul_rn(f_hi, eta));
     bool accept = !(eta > etabar) || num <= 0.0 || cross <= 0.0;
     if (!accept) accept = ++c->retries > 20;
     c->attempts += 1;
@@ -164,18 +180,23 @@ __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
     T v[2] = {dy2, cross};
     block_sum_t<T, 2>(v, reinterpret_cast<T*>(sm.red));
     if (threadIdx.x == 0) {
-        a.part[2 * blockIdx.x] = (double)v[0];
-        a.part[2 * blockIdx.x + 1] = (double)v[1];
+        Acc<T> e0, e1;
+        e0.s = v[0];
+        e1.s = v[1];
+        a.part[2 * blockIdx.x] = e0;
+        a.part[2 * blockIdx.x + 1] = e1;
     }
     if (!last_cta(&a.ctl->ticket)) return;
-    double s[3] = {0.0, 0.0, 0.0};
-    for (int i = threadIdx.x; i < a.n_primal; i += kThreads) s[0] += a.part_primal[i];
+    // fixed-order compensated merge of all CTA partials
+    Acc<T> s[3];
+    for (int i = threadIdx.x; i < a.n_primal; i += kThreads) s[0].merge(a.part_primal[i]);
     for (int i = threadIdx.x; i < (int)gridDim.x; i += kThreads) {
-        s[1] += a.part[2 * i];
-        s[2] += a.part[2 * i + 1];
+        s[1].merge(a.part[2 * i]);
+        s[2].merge(a.part[2 * i + 1]);
     }
-    block_sum<3>(s, sm.red);
-    if (threadIdx.x == 0) decide_step(a.ctl, s[0], s[1], s[2]);
+    block_merge<T, 3>(s, sm.carry());
+    if (threadIdx.x == 0)
+        decide_step(a.ctl, s[0].result_d(), s[1].result_d(), s[2].result_d(), a.fac, a.n_fac);
 }
 
 // ------------------------------------------------------------- plain SpMV
