@@ -7,15 +7,12 @@
 // slot 1-p, the device-side line search flips p on acceptance, so a rejected
 // attempt costs no copy and an accepted one no swap on the host.
 //
-// The hot SpMV is tile-scheduled: the host cuts the rows into tiles of at
-// most kTileNnz nonzeros / kTileRows rows (a longer row is a tile of its own).
-// A CTA streams its tile's values and column indices with coalesced loads,
-// gathers x through the read-only path, stages (a_ij, x_j) pairs in shared
-// memory and reduces the rows with a segmented sum balanced by nonzeros (every
-// thread owns the same number of staged entries, whatever the row lengths --
-// the Zipf-degree columns of the large LPs range from 1 to hundreds). The PDHG
-// step for each row then runs in the same CTA with consecutive threads on
-// consecutive rows, so A^T y / A xbar never round-trip through HBM.
+// The hot SpMV is warp-scheduled over a length-sorted permutation of the LP
+// (see WarpSched below): rows of similar length share a warp, G lanes per
+// row, coalesced streaming of values and indices, x gathered through the
+// read-only path, warp-shuffle reductions. The PDHG step for each row runs
+// right after its sum, with consecutive lanes on consecutive rows, so
+// A^T y / A xbar never round-trip through HBM.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -26,15 +23,6 @@ namespace igx {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-constexpr int kTileNnz = 2048;
-constexpr int kTileRows = 512;
-constexpr unsigned char kLongTile = 255;
-
-struct TileSched {
-    const int* tile_row;           // ntiles + 1 row boundaries
-    const unsigned char* tile_lg;  // 0, or kLongTile for a single long row
-    int ntiles;
-};
 
 template <typename T>
 struct Csr {
@@ -112,6 +100,11 @@ template <> struct Acc<double> {
         o.s = __shfl_xor_sync(mask, s, off, width);
         merge(o);
     }
+    __device__ __forceinline__ Acc shfl_from(unsigned mask, int src) const {
+        Acc o;
+        o.s = __shfl_sync(mask, s, src);
+        return o;
+    }
     __device__ __forceinline__ double result() const { return s; }
     __device__ __forceinline__ double result_d() const { return s; }
 };
@@ -140,6 +133,12 @@ template <> struct Acc<float> {
         o.s = __shfl_xor_sync(mask, s, off, width);
         o.c = __shfl_xor_sync(mask, c, off, width);
         merge(o);
+    }
+    __device__ __forceinline__ Acc shfl_from(unsigned mask, int src) const {
+        Acc o;
+        o.s = __shfl_sync(mask, s, src);
+        o.c = __shfl_sync(mask, c, src);
+        return o;
     }
     __device__ __forceinline__ float result() const { return s + c; }
     __device__ __forceinline__ double result_d() const { return (double)s + (double)c; }
@@ -265,126 +264,53 @@ __device__ __forceinline__ bool last_cta(unsigned int* ticket) {
     return is_last;
 }
 
-// --------------------------------------------------- tiled row reduction
-// Shared staging area of one tile: (a_ij, x_j) pairs, the tile's row
-// pointers and reduction scratch. 32 KB (FP64) / 16 KB (FP32) + 2.3 KB.
-template <typename T>
-struct TileSmem {
-    typename Vec2<T>::type stage[kTileNnz];
-    alignas(16) unsigned char rsum_raw[kTileRows * sizeof(Acc<T>)];   // row sums
-    alignas(16) unsigned char carry_raw[kThreads * sizeof(Acc<T>)];   // per-chunk carry-out
-    __device__ __forceinline__ Acc<T>* rsum() { return reinterpret_cast<Acc<T>*>(rsum_raw); }
-    __device__ __forceinline__ Acc<T>* carry() { return reinterpret_cast<Acc<T>*>(carry_raw); }
-    int rowptr[kTileRows + 1];
-    double red[kWarps * 4];
+// ------------------------------------------------------ warp row schedule
+// Rows are processed by warps. The host permutes the LP so that rows (and
+// columns) appear in decreasing nonzero count, then deals consecutive rows to
+// warps: a warp owns 32/G consecutive rows of similar length with G lanes per
+// row (G = 1..32, about four entries per lane). No shared memory and no
+// block-wide barrier on the hot path.
+struct WarpSched {
+    const int* row;           // nwarps + 1 row boundaries
+    const unsigned char* lg;  // log2(G) of each warp
+    int nwarps;
 };
 
-template <typename T>
-__device__ __forceinline__ typename Vec2<T>::type mk2(T a, T b);
-template <>
-__device__ __forceinline__ double2 mk2<double>(double a, double b) { return make_double2(a, b); }
-template <>
-__device__ __forceinline__ float2 mk2<float>(float a, float b) { return make_float2(a, b); }
-
-// Computes every row sum of tile `t` of A (times x) and calls
-// f(row, acc) once per row (acc: the row's Acc<T>) from exactly one lane. Rows of a tile are
-// consecutive, so consecutive f calls touch consecutive vector entries.
+// Sums every row of warp item `w` of A (times x) and calls f(row, acc) for
+// each row, from lane i for the warp's i-th row: consecutive lanes touch
+// consecutive vector entries in the epilogue. Lanes of a row read its entries
+// strided by G (coalesced across the warp), four loads in flight per lane.
 template <typename T, class F>
-__device__ __forceinline__ void tile_rows(TileSmem<T>& sm, const TileSched& ts, const Csr<T>& A,
-                                          const T* __restrict__ x, int t, F& f) {
-    const int r0 = ts.tile_row[t], r1 = ts.tile_row[t + 1];
-    const int p0 = A.ptr[r0], p1 = A.ptr[r1];
-    const int cnt = p1 - p0;
-    const unsigned char lg = ts.tile_lg[t];
-    if (lg == kLongTile) {  // one row, longer than a tile: whole CTA on it
-        Acc<T> acc;
-        for (int q = p0 + threadIdx.x; q < p1; q += kThreads)
-            acc.add(__ldg(A.val + q), __ldg(x + __ldg(A.idx + q)));
-        for (int o = 16; o > 0; o >>= 1) acc.shfl_xor(0xffffffffu, o, 32);
-        __shared__ __align__(16) unsigned char wacc_raw[kWarps * sizeof(Acc<T>)];
-        Acc<T>* wacc = reinterpret_cast<Acc<T>*>(wacc_raw);
-        __syncthreads();
-        if ((threadIdx.x & 31) == 0) wacc[threadIdx.x >> 5] = acc;
-        __syncthreads();
-        if (threadIdx.x == 0) {
-            Acc<T> tot = wacc[0];
-            for (int w = 1; w < kWarps; ++w) tot.merge(wacc[w]);
-            f(r0, tot);
-        }
-        return;
-    }
-    auto* st = sm.stage;
-    const int nrows = r1 - r0;
-    for (int r = threadIdx.x; r <= nrows; r += kThreads) sm.rowptr[r] = A.ptr[r0 + r] - p0;
-    // stage (a_ij, x_j): 4 independent loads in flight per thread
-    int q = threadIdx.x;
-    for (; q + 3 * kThreads < cnt; q += 4 * kThreads) {
-        T a0 = __ldg(A.val + p0 + q), a1 = __ldg(A.val + p0 + q + kThreads);
-        T a2 = __ldg(A.val + p0 + q + 2 * kThreads), a3 = __ldg(A.val + p0 + q + 3 * kThreads);
-        int j0 = __ldg(A.idx + p0 + q), j1 = __ldg(A.idx + p0 + q + kThreads);
-        int j2 = __ldg(A.idx + p0 + q + 2 * kThreads), j3 = __ldg(A.idx + p0 + q + 3 * kThreads);
-        T x0 = __ldg(x + j0), x1 = __ldg(x + j1), x2 = __ldg(x + j2), x3 = __ldg(x + j3);
-        st[q] = mk2<T>(a0, x0);
-        st[q + kThreads] = mk2<T>(a1, x1);
-        st[q + 2 * kThreads] = mk2<T>(a2, x2);
-        st[q + 3 * kThreads] = mk2<T>(a3, x3);
-    }
-    for (; q < cnt; q += kThreads) st[q] = mk2<T>(__ldg(A.val + p0 + q), __ldg(x + __ldg(A.idx + p0 + q)));
-    __syncthreads();
-    // Segmented reduction, balanced by nonzeros: thread t owns the staged
-    // elements [t*E, t*E+E) whatever the row lengths. A row that closes inside
-    // its chunk is written directly; a row spanning chunks is summed by the
-    // thread that closes it, over the spanning threads' carry-out pieces in
-    // increasing order (deterministic).
-    const int* rp = sm.rowptr;
-    Acc<T>* rsum = sm.rsum();
-    Acc<T>* carry = sm.carry();
-    for (int rr = threadIdx.x; rr < nrows; rr += kThreads)
-        if (rp[rr] == rp[rr + 1]) rsum[rr] = Acc<T>();  // empty row
-    const int E = (cnt + kThreads - 1) / kThreads;
-    const int q0 = min((int)threadIdx.x * E, cnt), q1 = min(q0 + E, cnt);
-    Acc<T> head;
-    int head_row = -1;
+__device__ __forceinline__ void warp_rows(const WarpSched& ws, const Csr<T>& A,
+                                          const T* __restrict__ x, int w, F& f) {
+    const int lane = threadIdx.x & 31;
+    const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
+    const int lg = __ldg(ws.lg + w);
+    const int G = 1 << lg;
+    const int g = lane >> lg, gl = lane & (G - 1);
+    const int r = r0 + g;
     Acc<T> acc;
-    if (q0 < q1) {
-        int lo = 0, hi = nrows - 1;  // first row with rp[i+1] > q0
-        while (lo < hi) {
-            const int mid = (lo + hi) >> 1;
-            if (rp[mid + 1] > q0) hi = mid;
-            else lo = mid + 1;
+    if (r < r1) {
+        const int b = __ldg(A.ptr + r), e = __ldg(A.ptr + r + 1);
+        int p = b + gl;
+        for (; p + 3 * G < e; p += 4 * G) {
+            const T a0 = __ldg(A.val + p), a1 = __ldg(A.val + p + G);
+            const T a2 = __ldg(A.val + p + 2 * G), a3 = __ldg(A.val + p + 3 * G);
+            const int j0 = __ldg(A.idx + p), j1 = __ldg(A.idx + p + G);
+            const int j2 = __ldg(A.idx + p + 2 * G), j3 = __ldg(A.idx + p + 3 * G);
+            const T x0 = __ldg(x + j0), x1 = __ldg(x + j1), x2 = __ldg(x + j2), x3 = __ldg(x + j3);
+            acc.add(a0, x0);
+            acc.add(a1, x1);
+            acc.add(a2, x2);
+            acc.add(a3, x3);
         }
-        int i = lo;
-        bool started_here = rp[i] == q0;
-        int end = rp[i + 1];
-        for (int k = q0; k < q1; ++k) {
-            const auto v = st[k];
-            acc.add(v.x, v.y);
-            if (k + 1 == end) {
-                if (started_here) {
-                    rsum[i] = acc;
-                } else {
-                    head = acc;
-                    head_row = i;
-                }
-                acc = Acc<T>();
-                ++i;
-                while (i < nrows && rp[i + 1] == rp[i]) ++i;
-                started_here = true;
-                end = i < nrows ? rp[i + 1] : cnt + 1;
-            }
-        }
+        for (; p < e; p += G) acc.add(__ldg(A.val + p), __ldg(x + __ldg(A.idx + p)));
     }
-    carry[threadIdx.x] = acc;  // piece of a row that continues past the chunk
-    __syncthreads();
-    if (head_row >= 0) {
-        Acc<T> tot;
-        for (int s = rp[head_row] / E; s < (int)threadIdx.x; ++s) tot.merge(carry[s]);
-        tot.merge(head);
-        rsum[head_row] = tot;
-    }
-    __syncthreads();
-    // epilogue: consecutive threads on consecutive rows (coalesced vectors)
-    for (int rr = threadIdx.x; rr < nrows; rr += kThreads) f(r0 + rr, sm.rsum()[rr]);
+    // reduce within each group of G lanes (all 32 lanes take part)
+    for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(0xffffffffu, o, G);
+    // lane i fetches the sum of the warp's i-th row from lane i*G
+    Acc<T> mine = acc.shfl_from(0xffffffffu, (lane << lg) & 31);
+    if (lane < (32 >> lg) && r0 + lane < r1) f(r0 + lane, mine);
 }
 
 }  // namespace igx

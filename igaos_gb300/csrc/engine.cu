@@ -37,47 +37,73 @@ void* Arena::raw(size_t bytes) {
     return p;
 }
 
-// ---------------------------------------------------------- tile schedule
-// Greedy cut of the rows into tiles of at most kTileNnz nonzeros and
-// kTileRows rows; a row longer than a tile becomes a long tile of its own.
-void build_tiles(const int* ptr, int rows, std::vector<int>& tile_row,
-                 std::vector<unsigned char>& tile_lg) {
-    tile_row.assign(1, 0);
-    tile_lg.clear();
+// ------------------------------------------------- permutation + schedule
+std::vector<int> length_order(const int* ptr, int rows) {
+    // counting sort by decreasing length, stable within a length
+    int maxlen = 0;
+    for (int r = 0; r < rows; ++r) maxlen = std::max(maxlen, ptr[r + 1] - ptr[r]);
+    std::vector<int> start(maxlen + 2, 0);
+    for (int r = 0; r < rows; ++r) ++start[maxlen - (ptr[r + 1] - ptr[r]) + 1];
+    for (int k = 0; k <= maxlen; ++k) start[k + 1] += start[k];
+    std::vector<int> ord(rows);
+    for (int r = 0; r < rows; ++r) ord[start[maxlen - (ptr[r + 1] - ptr[r])]++] = r;
+    return ord;
+}
+
+void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<unsigned char>& wlg) {
+    wrow.assign(1, 0);
+    wlg.clear();
     int r = 0;
     while (r < rows) {
         const int len = ptr[r + 1] - ptr[r];
-        if (len > kTileNnz) {
-            tile_row.push_back(r + 1);
-            tile_lg.push_back(kLongTile);
-            ++r;
-            continue;
-        }
-        int e = r;
-        long cnt = 0;
-        while (e < rows && e - r < kTileRows) {
-            const int l = ptr[e + 1] - ptr[e];
-            if (l > kTileNnz || cnt + l > kTileNnz) break;
-            cnt += l;
-            ++e;
-        }
-        tile_row.push_back(e);
-        tile_lg.push_back(0);
-        r = e;
+        int lg = 0;
+        while (lg < 5 && (1 << lg) * 4 < len) ++lg;  // about four entries per lane
+        r = std::min(rows, r + (32 >> lg));
+        wrow.push_back(r);
+        wlg.push_back((unsigned char)lg);
     }
 }
 
 static Sched upload_sched(Arena& ar, const int* ptr, int rows) {
-    std::vector<int> tr;
-    std::vector<unsigned char> tl;
-    build_tiles(ptr, rows, tr, tl);
+    std::vector<int> wr;
+    std::vector<unsigned char> wl;
+    build_warps(ptr, rows, wr, wl);
     Sched s;
-    s.ntiles = (int)tl.size();
-    s.row = ar.alloc<int>(tr.size());
-    s.lg = ar.alloc<unsigned char>(tl.size());
-    CU(cudaMemcpy(s.row, tr.data(), sizeof(int) * tr.size(), cudaMemcpyHostToDevice));
-    CU(cudaMemcpy(s.lg, tl.data(), tl.size(), cudaMemcpyHostToDevice));
+    s.nwarps = (int)wl.size();
+    s.ctas = std::max(1, (s.nwarps + kWarps - 1) / kWarps);
+    s.row = ar.alloc<int>(wr.size());
+    s.lg = ar.alloc<unsigned char>(wl.size());
+    CU(cudaMemcpy(s.row, wr.data(), sizeof(int) * wr.size(), cudaMemcpyHostToDevice));
+    CU(cudaMemcpy(s.lg, wl.data(), wl.size(), cudaMemcpyHostToDevice));
     return s;
+}
+
+// CSR of the row-permuted matrix with renumbered indices; each row keeps its
+// entries in their original order (the same summation order).
+static void permute_csr(int rows, const int* ptr, const int* idx, const double* val,
+                        const std::vector<int>& rnew2old, const std::vector<int>& iold2new,
+                        std::vector<int>& P, std::vector<int>& I, std::vector<double>& V) {
+    P.assign(rows + 1, 0);
+    for (int r = 0; r < rows; ++r) {
+        const int o = rnew2old[r];
+        P[r + 1] = P[r] + (ptr[o + 1] - ptr[o]);
+    }
+    I.resize(P[rows]);
+    V.resize(P[rows]);
+    for (int r = 0; r < rows; ++r) {
+        const int o = rnew2old[r];
+        int q = P[r];
+        for (int p = ptr[o]; p < ptr[o + 1]; ++p, ++q) {
+            I[q] = iold2new[idx[p]];
+            V[q] = val[p];
+        }
+    }
+}
+
+static std::vector<int> inverse(const std::vector<int>& p) {
+    std::vector<int> q(p.size());
+    for (size_t i = 0; i < p.size(); ++i) q[p[i]] = (int)i;
+    return q;
 }
 
 static int grid_for(long long n, int per_block = kThreads, int cap = 152 * 16) {
@@ -98,34 +124,48 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     CU(cudaGetDevice(&device_));
     CU(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
     for (auto& e : ev_) CU(cudaEventCreate(&e));
-    // matrix, both orientations
-    ap_ = ar_.alloc<int>(m + 1);
-    ai_ = ar_.alloc<int>(nnz);
-    ax_ = ar_.alloc<double>(nnz);
-    cp_ = ar_.alloc<int>(n + 1);
-    ci_ = ar_.alloc<int>(nnz);
-    acx_ = ar_.alloc<double>(nnz);
-    ax32_ = ar_.alloc<float>(nnz);
-    acx32_ = ar_.alloc<float>(nnz);
-    CU(cudaMemcpyAsync(ap_, ap, sizeof(int) * (m + 1), cudaMemcpyHostToDevice, st_));
-    CU(cudaMemcpyAsync(ai_, ai, sizeof(int) * nnz, cudaMemcpyHostToDevice, st_));
-    CU(cudaMemcpyAsync(ax_, ax, sizeof(double) * nnz, cudaMemcpyHostToDevice, st_));
-    CU(cudaMemcpyAsync(cp_, cp, sizeof(int) * (n + 1), cudaMemcpyHostToDevice, st_));
-    CU(cudaMemcpyAsync(ci_, ci, sizeof(int) * nnz, cudaMemcpyHostToDevice, st_));
-    CU(cudaMemcpyAsync(acx_, acx, sizeof(double) * nnz, cudaMemcpyHostToDevice, st_));
-    sA_ = upload_sched(ar_, ap, m);
-    sAT_ = upload_sched(ar_, cp, n);
+    // Length-sorted numbering of rows and columns (the warp schedule needs
+    // rows of similar length next to each other). Everything on the device
+    // lives in this numbering; the API permutes at its edges.
+    pr_ = length_order(ap, m);
+    pc_ = length_order(cp, n);
+    ipr_ = inverse(pr_);
+    ipc_ = inverse(pc_);
+    {
+        std::vector<int> P, I;
+        std::vector<double> V;
+        ap_ = ar_.alloc<int>(m + 1);
+        ai_ = ar_.alloc<int>(nnz);
+        ax_ = ar_.alloc<double>(nnz);
+        cp_ = ar_.alloc<int>(n + 1);
+        ci_ = ar_.alloc<int>(nnz);
+        acx_ = ar_.alloc<double>(nnz);
+        ax32_ = ar_.alloc<float>(nnz);
+        acx32_ = ar_.alloc<float>(nnz);
+        permute_csr(m, ap, ai, ax, pr_, ipc_, P, I, V);
+        CU(cudaMemcpy(ap_, P.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(ai_, I.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(ax_, V.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
+        sA_ = upload_sched(ar_, P.data(), m);
+        permute_csr(n, cp, ci, acx, pc_, ipr_, P, I, V);
+        CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(ci_, I.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(acx_, V.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
+        sAT_ = upload_sched(ar_, P.data(), n);
+    }
     // vectors
-    auto vec = [&](const double* h, int len) {
-        double* d = ar_.alloc<double>(len);
-        CU(cudaMemcpyAsync(d, h, sizeof(double) * len, cudaMemcpyHostToDevice, st_));
+    auto vec = [&](const double* h, const std::vector<int>& perm) {
+        std::vector<double> t(perm.size());
+        for (size_t i = 0; i < perm.size(); ++i) t[i] = h[perm[i]];
+        double* d = ar_.alloc<double>(t.size());
+        CU(cudaMemcpy(d, t.data(), sizeof(double) * t.size(), cudaMemcpyHostToDevice));
         return d;
     };
-    base_.c = vec(c, n);
-    base_.cl = vec(cl, n);
-    base_.cu = vec(cu, n);
-    base_.rmin = vec(rmin, m);
-    base_.rmax = vec(rmax, m);
+    base_.c = vec(c, pc_);
+    base_.cl = vec(cl, pc_);
+    base_.cu = vec(cu, pc_);
+    base_.rmin = vec(rmin, pr_);
+    base_.rmax = vec(rmax, pr_);
     base_.cmax = 0.0;
     for (int j = 0; j < n; ++j) base_.cmax = std::max(base_.cmax, std::fabs(c[j]));
     base_.sc = ar_.alloc<double>(n);
@@ -151,7 +191,7 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     fac_ = ar_.alloc<double>(2 * kFac);
     std::memset(h_ctl_, 0, sizeof(DevCtl));
     red_blocks_ = grid_for(std::max(m, n), kThreads, 152 * 4);
-    const int kkt_blocks = std::max(std::max(sA_.ntiles, sAT_.ntiles), red_blocks_);
+    const int kkt_blocks = std::max(std::max(sA_.ctas, sAT_.ctas), red_blocks_);
     kkt_part_ = ar_.alloc<double>((size_t)2 * kkt_blocks * 4);
     red_part_ = ar_.alloc<double>((size_t)2 * red_blocks_ + 8);
     scal_ = ar_.alloc<double>(16);
@@ -222,10 +262,15 @@ void Engine::setup_scaling() {
     k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cl, dc_, 0, base_.scl, base_.fcl);
     k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cu, dc_, 0, base_.scu, base_.fcu);
     CU(cudaGetLastError());
+    hp_dr_.resize(m);
+    hp_dc_.resize(n);
+    CU(cudaMemcpyAsync(hp_dr_.data(), dr_, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(hp_dc_.data(), dc_, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+    CU(cudaStreamSynchronize(st_));
     h_dr.resize(m);
     h_dc.resize(n);
-    CU(cudaMemcpyAsync(h_dr.data(), dr_, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
-    CU(cudaMemcpyAsync(h_dc.data(), dc_, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+    to_user_order(hp_dr_.data(), h_dr.data(), true);
+    to_user_order(hp_dc_.data(), h_dc.data(), false);
     CU(cudaStreamSynchronize(st_));
 }
 
@@ -238,9 +283,9 @@ template <typename T>
 void Engine::spmv_dev(bool transpose, const T* x, T* y) {
     ++launches_;
     if (transpose)
-        k_spmv<T, T><<<sAT_.ntiles, kThreads, 0, st_>>>(sAT_.view(), csrAT<T>(), x, y);
+        k_spmv<T, T><<<sAT_.ctas, kThreads, 0, st_>>>(sAT_.view(), csrAT<T>(), x, y);
     else
-        k_spmv<T, T><<<sA_.ntiles, kThreads, 0, st_>>>(sA_.view(), csrA<T>(), x, y);
+        k_spmv<T, T><<<sA_.ctas, kThreads, 0, st_>>>(sA_.view(), csrA<T>(), x, y);
     CU(cudaGetLastError());
 }
 
@@ -289,8 +334,8 @@ void Engine::ensure_work() {
     w.pesx = ar_.alloc<T>(n);
     w.yb = ar_.alloc<T>(m);
     w.pesy = ar_.alloc<T>(m);
-    w.part_p = ar_.alloc<double>(sAT_.ntiles);
-    w.part_d = ar_.alloc<double>(2 * (size_t)sA_.ntiles);
+    w.part_p = ar_.alloc<double>(sAT_.ctas);
+    w.part_d = ar_.alloc<double>(2 * (size_t)sA_.ctas);
     have = true;
 }
 
@@ -316,7 +361,7 @@ template <typename T>
 void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     Work<T>& w = work<T>();
     PrimalArgs<T> pa;
-    pa.ts = sAT_.view();
+    pa.ws = sAT_.view();
     pa.AT = csrAT<T>();
     pa.y[0] = w.y[0];
     pa.y[1] = w.y[1];
@@ -331,7 +376,7 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     pa.part = reinterpret_cast<Acc<T>*>(w.part_p);
     pa.ctl = ctl_;
     DualArgs<T> da;
-    da.ts = sA_.view();
+    da.ws = sA_.view();
     da.A = csrA<T>();
     da.xbar = w.xbar;
     da.rmin = VecSel<T>::rl(v);
@@ -343,15 +388,15 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     }
     da.part = reinterpret_cast<Acc<T>*>(w.part_d);
     da.part_primal = reinterpret_cast<const Acc<T>*>(w.part_p);
-    da.n_primal = sAT_.ntiles;
+    da.n_primal = sAT_.ctas;
     da.fac = fac_;
     da.n_fac = kFac;
     da.ctl = ctl_;
     launches_ += 2LL * count;
     auto enqueue = [&](int cnt) {
         for (int a = 0; a < cnt; ++a) {
-            k_primal<T><<<sAT_.ntiles, kThreads, 0, st_>>>(pa);
-            k_dual<T><<<sA_.ntiles, kThreads, 0, st_>>>(da);
+            k_primal<T><<<sAT_.ctas, kThreads, 0, st_>>>(pa);
+            k_dual<T><<<sA_.ctas, kThreads, 0, st_>>>(da);
         }
     };
     if (!graphs) {
@@ -431,8 +476,8 @@ void Engine::run_until_stop(const Vecs& v, bool graphs, LoopOut& out) {
 template <typename T>
 void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* y1, int ncand) {
     KktArgs<T> ka;
-    ka.tsA = sA_.view();
-    ka.tsAT = sAT_.view();
+    ka.wsA = sA_.view();
+    ka.wsAT = sAT_.view();
     ka.A = csrA<T>();
     ka.AT = csrAT<T>();
     ka.x[0] = x0;
@@ -451,8 +496,8 @@ void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* 
     ka.out = met_;
     ka.ticket = ticket_ + 2;
     launches_ += 3;
-    k_kkt_rows<T><<<dim3(sA_.ntiles, ncand), kThreads, 0, st_>>>(ka);
-    k_kkt_cols<T><<<dim3(sAT_.ntiles, ncand), kThreads, 0, st_>>>(ka);
+    k_kkt_rows<T><<<dim3(sA_.ctas, ncand), kThreads, 0, st_>>>(ka);
+    k_kkt_cols<T><<<dim3(sAT_.ctas, ncand), kThreads, 0, st_>>>(ka);
     k_kkt_rowdual<T><<<dim3(red_blocks_, ncand), kThreads, 0, st_>>>(ka, m);
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(h_met_, met_, ncand * sizeof(DevMetrics), cudaMemcpyDeviceToHost, st_));
@@ -727,18 +772,44 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
                               "-inf or > tol)"
                             : "iteration cap reached before tolerance");
     }
+    // unscale (x = dc x~, y = y~/dr) and return to the caller's numbering
     if (x)
-        for (int j = 0; j < n; ++j) x[j] = hx[j] * h_dc[j];
+        for (int j = 0; j < n; ++j) x[pc_[j]] = hx[j] * hp_dc_[j];
     if (y)
-        for (int i = 0; i < m; ++i) y[i] = 1.0 * hy[i] / h_dr[i];
+        for (int i = 0; i < m; ++i) y[pr_[i]] = 1.0 * hy[i] / hp_dr_[i];
+}
+
+// ------------------------------------------------------- numbering helpers
+void Engine::to_dev_order(const double* in, double* out, bool rows) const {
+    const std::vector<int>& p = rows ? pr_ : pc_;
+    for (size_t i = 0; i < p.size(); ++i) out[i] = in[p[i]];
+}
+void Engine::to_user_order(const double* in, double* out, bool rows) const {
+    const std::vector<int>& p = rows ? pr_ : pc_;
+    for (size_t i = 0; i < p.size(); ++i) out[p[i]] = in[i];
 }
 
 // --------------------------------------------------------- inspection API
+// The device CSC is in device numbering; map it back: column j of the
+// caller is device column ipc_[j], row indices through pr_, entries of a
+// column keep their order.
 void Engine::get_transpose(int* cp, int* ci, double* acx) {
-    CU(cudaMemcpyAsync(cp, cp_, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st_));
-    CU(cudaMemcpyAsync(ci, ci_, sizeof(int) * nnz, cudaMemcpyDeviceToHost, st_));
-    CU(cudaMemcpyAsync(acx, acx_, sizeof(double) * nnz, cudaMemcpyDeviceToHost, st_));
+    std::vector<int> dcp(n + 1), dci(nnz);
+    std::vector<double> dacx(nnz);
+    CU(cudaMemcpyAsync(dcp.data(), cp_, sizeof(int) * (n + 1), cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(dci.data(), ci_, sizeof(int) * nnz, cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(dacx.data(), acx_, sizeof(double) * nnz, cudaMemcpyDeviceToHost, st_));
     CU(cudaStreamSynchronize(st_));
+    cp[0] = 0;
+    for (int j = 0; j < n; ++j) {
+        const int d = ipc_[j];
+        const int len = dcp[d + 1] - dcp[d];
+        for (int k = 0; k < len; ++k) {
+            ci[cp[j] + k] = pr_[dci[dcp[d] + k]];
+            acx[cp[j] + k] = dacx[dcp[d] + k];
+        }
+        cp[j + 1] = cp[j] + len;
+    }
 }
 
 template <typename T>
@@ -755,15 +826,28 @@ static void upload_as(cudaStream_t st, T* dst, const double* src, int len, doubl
 
 void Engine::iterate(int precision, long long iters, double* x, double* y, double* xavg,
                      double* yavg, double* axc, double* st6) {
+    std::vector<double> bn(n), bm(m);
+    auto up = [&](auto* dst, const double* src, bool rows) {
+        using T = std::remove_pointer_t<decltype(dst)>;
+        double* b = rows ? bm.data() : bn.data();
+        to_dev_order(src, b, rows);
+        upload_as<T>(st_, dst, b, rows ? m : n, rows ? tmp_m_ : tmp_n_);
+    };
+    auto down = [&](const auto* src, double* dst, bool rows) {
+        using T = std::remove_const_t<std::remove_pointer_t<decltype(src)>>;
+        double* b = rows ? bm.data() : bn.data();
+        fetch_scaled<T>(src, rows ? m : n, b);
+        to_user_order(b, dst, rows);
+    };
     auto run = [&](auto tag) {
         using T = decltype(tag);
         ensure_work<T>();
         Work<T>& w = work<T>();
-        upload_as<T>(st_, w.x[0], x, n, tmp_n_);
-        upload_as<T>(st_, w.xavg[0], xavg, n, tmp_n_);
-        upload_as<T>(st_, w.y[0], y, m, tmp_m_);
-        upload_as<T>(st_, w.yavg[0], yavg, m, tmp_m_);
-        upload_as<T>(st_, w.axc[0], axc, m, tmp_m_);
+        up(w.x[0], x, false);
+        up(w.xavg[0], xavg, false);
+        up(w.y[0], y, true);
+        up(w.yavg[0], yavg, true);
+        up(w.axc[0], axc, true);
         std::memset(h_ctl_, 0, sizeof(DevCtl));
         h_ctl_->eta = st6[0];
         h_ctl_->omega = st6[1];
@@ -775,11 +859,11 @@ void Engine::iterate(int precision, long long iters, double* x, double* y, doubl
         if (iters > 0) run_until_stop<T>(base_, false, out);
         else download_ctl();
         const int p = h_ctl_->parity;
-        fetch_scaled<T>(w.x[p], n, x);
-        fetch_scaled<T>(w.xavg[p], n, xavg);
-        fetch_scaled<T>(w.y[p], m, y);
-        fetch_scaled<T>(w.yavg[p], m, yavg);
-        fetch_scaled<T>(w.axc[p], m, axc);
+        down(w.x[p], x, false);
+        down(w.xavg[p], xavg, false);
+        down(w.y[p], y, true);
+        down(w.yavg[p], yavg, true);
+        down(w.axc[p], axc, true);
         st6[0] = h_ctl_->eta;
         st6[1] = h_ctl_->omega;
         st6[2] = (double)h_ctl_->k;
@@ -794,8 +878,8 @@ void Engine::iterate(int precision, long long iters, double* x, double* y, doubl
 void Engine::evaluate(const double* x, const double* y, double* out6) {
     // scaled copies: x~ = x / dc, y~ = y * dr
     std::vector<double> xs(n), ys(m);
-    for (int j = 0; j < n; ++j) xs[j] = x[j] / h_dc[j];
-    for (int i = 0; i < m; ++i) ys[i] = y[i] * h_dr[i];
+    for (int j = 0; j < n; ++j) xs[j] = x[pc_[j]] / hp_dc_[j];
+    for (int i = 0; i < m; ++i) ys[i] = y[pr_[i]] * hp_dr_[i];
     CU(cudaMemcpyAsync(tmp_n2_, xs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st_));
     CU(cudaMemcpyAsync(tmp_m2_, ys.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st_));
     kkt<double>(base_, tmp_n2_, tmp_m2_, tmp_n2_, tmp_m2_, 1);
@@ -808,8 +892,19 @@ void Engine::evaluate(const double* x, const double* y, double* out6) {
     out6[5] = t.prow;
 }
 
-void Engine::spmv(int transpose, int precision, const double* x, double* y) {
+void Engine::spmv(int transpose, int precision, const double* x_user, double* y_user) {
     const int lin = transpose ? m : n, lout = transpose ? n : m;
+    std::vector<double> xin(lin), yout(lout);
+    to_dev_order(x_user, xin.data(), transpose != 0);
+    const double* x = xin.data();
+    double* y = yout.data();
+    struct Back {
+        const Engine* e;
+        double* y;
+        double* u;
+        bool rows;
+        ~Back() { e->to_user_order(y, u, rows); }
+    } back{this, y, y_user, transpose == 0};
     if (precision == IGAOS_PDHG_FP64) {
         double* dx = transpose ? tmp_m_ : tmp_n_;
         double* dy = transpose ? tmp_n2_ : tmp_m2_;

@@ -38,13 +38,17 @@ class Arena {
 struct Sched {
     int* row = nullptr;
     unsigned char* lg = nullptr;
-    int ntiles = 0;
-    TileSched view() const { return TileSched{row, lg, ntiles}; }
+    int nwarps = 0;
+    int ctas = 0;  // kWarps warps per CTA
+    WarpSched view() const { return WarpSched{row, lg, nwarps}; }
 };
 
-// Host-side tile schedule of a CSR row pointer (see device.cuh).
-void build_tiles(const int* ptr, int rows, std::vector<int>& tile_row,
-                 std::vector<unsigned char>& tile_lg);
+// Host-side warp schedule of a (length-sorted) CSR row pointer: consecutive
+// rows dealt to warps, G lanes per row from the first row's length.
+void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<unsigned char>& wlg);
+
+// Permutation sorting rows by decreasing length (stable): new -> old index.
+std::vector<int> length_order(const int* ptr, int rows);
 
 // Vectors defining one LP over the engine's shared matrix: original units
 // (FP64, for the KKT pass) and scaled units (FP64 and FP32, for iterating).
@@ -126,6 +130,11 @@ class Engine {
     Sched sA_, sAT_;
     double *dr_, *dc_;
     Vecs base_{};
+    // device numbering: new index -> original (pr_, pc_) and inverses
+    std::vector<int> pr_, pc_, ipr_, ipc_;
+    std::vector<double> hp_dr_, hp_dc_;  // scaling in device numbering
+    void to_dev_order(const double* in, double* out, bool rows) const;
+    void to_user_order(const double* in, double* out, bool rows) const;
     // workspace
     Work<double> w64_{};
     Work<float> w32_{};

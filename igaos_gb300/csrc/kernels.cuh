@@ -26,7 +26,7 @@ __device__ __forceinline__ CtlView<float> read_ctl<float>(const DevCtl* c) {
 
 template <typename T>
 struct PrimalArgs {
-    TileSched ts;
+    WarpSched ws;
     Csr<T> AT;              // A~^T (rows = columns of A)
     const T* y[2];          // dual iterate slots
     const T* c;             // scaled cost
@@ -47,7 +47,8 @@ struct PrimalArgs {
 // accepted state untouched.
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_primal(PrimalArgs<T> a) {
-    __shared__ TileSmem<T> sm;
+    __shared__ __align__(16) double smred[kWarps * 4];
+    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
     const int p = cv.parity, q = p ^ 1;
@@ -68,9 +69,9 @@ __global__ void __launch_bounds__(kThreads) k_primal(PrimalArgs<T> a) {
         const T av = xa[j];
         xa_out[j] = fma(w, xn - av, av);
     };
-    tile_rows<T>(sm, a.ts, a.AT, a.y[p], blockIdx.x, f);
+    if (wid < a.ws.nwarps) warp_rows<T>(a.ws, a.AT, a.y[p], wid, f);
     T v[1] = {dx2};
-    block_sum_t<T, 1>(v, reinterpret_cast<T*>(sm.red));
+    block_sum_t<T, 1>(v, reinterpret_cast<T*>(smred));
     if (threadIdx.x == 0) {
         Acc<T> e;
         e.s = v[0];
@@ -80,7 +81,7 @@ __global__ void __launch_bounds__(kThreads) k_primal(PrimalArgs<T> a) {
 
 template <typename T>
 struct DualArgs {
-    TileSched ts;
+    WarpSched ws;
     Csr<T> A;
     const T* xbar;
     const T* rmin;          // scaled row bounds
@@ -149,7 +150,8 @@ __device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cro
 // the reference made on the host after a blocking copy (:768-794).
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
-    __shared__ TileSmem<T> sm;
+    __shared__ __align__(16) double smred[kWarps * 4];
+    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
     const int p = cv.parity, q = p ^ 1;
@@ -176,9 +178,9 @@ __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
         const T av = ya[i];
         ya_out[i] = fma(w, yn - av, av);
     };
-    tile_rows<T>(sm, a.ts, a.A, a.xbar, blockIdx.x, f);
+    if (wid < a.ws.nwarps) warp_rows<T>(a.ws, a.A, a.xbar, wid, f);
     T v[2] = {dy2, cross};
-    block_sum_t<T, 2>(v, reinterpret_cast<T*>(sm.red));
+    block_sum_t<T, 2>(v, reinterpret_cast<T*>(smred));
     if (threadIdx.x == 0) {
         Acc<T> e0, e1;
         e0.s = v[0];
@@ -194,7 +196,7 @@ __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
         s[1].merge(a.part[2 * i]);
         s[2].merge(a.part[2 * i + 1]);
     }
-    block_merge<T, 3>(s, sm.carry());
+    block_merge<T, 3>(s, reinterpret_cast<Acc<T>*>(smred));
     if (threadIdx.x == 0)
         decide_step(a.ctl, s[0].result_d(), s[1].result_d(), s[2].result_d(), a.fac, a.n_fac);
 }
@@ -203,10 +205,11 @@ __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
 // y = A x (Spmv::mv, src/pdhg/pdhg.cu:143-157), optional skip flag.
 template <typename T, typename TO>
 __global__ void __launch_bounds__(kThreads)
-    k_spmv(TileSched ts, Csr<T> A, const T* __restrict__ x, TO* __restrict__ y) {
-    __shared__ TileSmem<T> sm;
+    k_spmv(WarpSched ws, Csr<T> A, const T* __restrict__ x, TO* __restrict__ y) {
+    __shared__ __align__(16) double smred[kWarps * 4];
+    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     auto f = [&](int r, const Acc<T>& acc) { y[r] = (TO)acc.result_d(); };
-    tile_rows<T>(sm, ts, A, x, blockIdx.x, f);
+    if (wid < ws.nwarps) warp_rows<T>(ws, A, x, wid, f);
 }
 
 // -------------------------------------------------------- Ruiz equilibration
@@ -373,7 +376,7 @@ __global__ void k_convert(int n, const TI* __restrict__ in, TO* __restrict__ out
 
 template <typename T>
 struct KktArgs {
-    TileSched tsA, tsAT;
+    WarpSched wsA, wsAT;
     Csr<T> A, AT;
     const T* x[2];
     const T* y[2];
@@ -387,7 +390,8 @@ struct KktArgs {
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
-    __shared__ TileSmem<T> sm;
+    __shared__ __align__(16) double smred[kWarps * 4];
+    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const int v = blockIdx.y;
     const T* __restrict__ yv = a.y[v];
     double pv = 0.0, pa = 0.0, prow = 0.0, ymax = 0.0;
@@ -404,9 +408,9 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
         prow = smax(prow, viol / (1.0 + sc));
         ymax = smax(ymax, fabs((double)yv[i] * (1.0 / a.dr[i])));
     };
-    tile_rows<T>(sm, a.tsA, a.A, a.x[v], blockIdx.x, f);
+    if (wid < a.wsA.nwarps) warp_rows<T>(a.wsA, a.A, a.x[v], wid, f);
     double r[4] = {pv, pa, prow, ymax};
-    block_max<4>(r, sm.red);
+    block_max<4>(r, smred);
     const int nt = gridDim.x;
     if (threadIdx.x == 0)
         for (int q = 0; q < 4; ++q) a.part[(v * nt + blockIdx.x) * 4 + q] = r[q];
@@ -415,7 +419,7 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
         double t[4] = {0.0, 0.0, 0.0, 0.0};
         for (int b = threadIdx.x; b < nt; b += kThreads)
             for (int q = 0; q < 4; ++q) t[q] = smax(t[q], a.part[(cv * nt + b) * 4 + q]);
-        block_max<4>(t, sm.red);
+        block_max<4>(t, smred);
         if (threadIdx.x == 0) {
             DevMetrics& o = a.out[cv];
             o.pv = t[0];
@@ -429,7 +433,8 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
 
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a) {
-    __shared__ TileSmem<T> sm;
+    __shared__ __align__(16) double smred[kWarps * 4];
+    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const int v = blockIdx.y;
     const T* __restrict__ xv = a.x[v];
     const double dz = 1e-8 * (1.0 + a.cmax);
@@ -454,11 +459,11 @@ __global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a) {
             else if (-d > dz) unb = 1.0;
         }
     };
-    tile_rows<T>(sm, a.tsAT, a.AT, a.y[v], blockIdx.x, f);
+    if (wid < a.wsAT.nwarps) warp_rows<T>(a.wsAT, a.AT, a.y[v], wid, f);
     double mx[2] = {dv, unb};
-    block_max<2>(mx, sm.red);
+    block_max<2>(mx, smred);
     double sm2[2] = {op, od};
-    block_sum<2>(sm2, sm.red);
+    block_sum<2>(sm2, smred);
     const int nt = gridDim.x;
     if (threadIdx.x == 0) {
         double* P = a.part + (v * nt + blockIdx.x) * 4;
@@ -477,8 +482,8 @@ __global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a) {
             ts[0] += P[2];
             ts[1] += P[3];
         }
-        block_max<2>(tm, sm.red);
-        block_sum<2>(ts, sm.red);
+        block_max<2>(tm, smred);
+        block_sum<2>(ts, smred);
         if (threadIdx.x == 0) {
             DevMetrics& o = a.out[cv];
             o.dv = tm[0];
