@@ -128,7 +128,7 @@ def cpu_sample(lp, iters, threads):
     SpMVs (FP64 values) over a bounded number of iterations."""
     from oracle import oracle as O
     olp = O.lp_from(lp)
-    r = O.pdhg_solve(olp, tolerance=1e-12, time_limit=0.0, max_iterations=iters, threads=threads)
+    r = O.pdhg_solve(olp, tolerance=1e-12, time_limit=1e9, max_iterations=iters, threads=threads)
     b = bytes_per_attempt(lp.m, lp.n, lp.nnz, 8) * r["attempts"]
     return b / r["loop_seconds"] / 1e9, r
 
@@ -204,7 +204,7 @@ def main():
     torch.cuda.set_device(local)
     from igaos_gb300 import capi
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    opts = dict(precision=args.precision, tolerance=1e-12, time_limit=0.0,
+    opts = dict(precision=args.precision, tolerance=1e-12, time_limit=1e9,
                 max_iterations=args.iters, device=local)
     bpa = bytes_per_attempt(lp.m, lp.n, lp.nnz, 8 if args.precision == "fp64" else 4)
     with capi.Problem(lp, device=local) as P:

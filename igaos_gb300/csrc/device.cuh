@@ -248,11 +248,13 @@ __device__ __forceinline__ void block_merge(Acc<T> (&v)[NV], Acc<T>* sh) {
 // Last-CTA-done handshake: every CTA publishes its partials, fences, takes a
 // ticket; the CTA holding the last ticket sees every partial and resets the
 // counter for the next launch. No CTA waits on another.
+// The partials are written by thread 0, so only thread 0 fences before its
+// ticket; the winner fences again (all threads) before reading them.
 __device__ __forceinline__ bool last_cta(unsigned int* ticket) {
     __shared__ bool is_last;
-    __threadfence();
     __syncthreads();
     if (threadIdx.x == 0) {
+        __threadfence();
         unsigned int t = atomicAdd(ticket, 1u);
         is_last = (t == gridDim.x * gridDim.y - 1);
     }
@@ -276,41 +278,70 @@ struct WarpSched {
     int nwarps;
 };
 
-// Sums every row of warp item `w` of A (times x) and calls f(row, acc) for
-// each row, from lane i for the warp's i-th row: consecutive lanes touch
-// consecutive vector entries in the epilogue. Lanes of a row read its entries
-// strided by G (coalesced across the warp), four loads in flight per lane.
-template <typename T, class F>
-__device__ __forceinline__ void warp_rows(const WarpSched& ws, const Csr<T>& A,
-                                          const T* __restrict__ x, int w, F& f) {
+
+// Epilogue adapter for kernels whose row step needs no prefetch.
+struct NoPre {};
+template <class F>
+struct PlainEpi {
+    F& f;
+    using Pre = NoPre;
+    __device__ __forceinline__ NoPre load(int) const { return NoPre{}; }
+    template <class A>
+    __device__ __forceinline__ void apply(int r, const A& acc, const NoPre&) { f(r, acc); }
+};
+
+// One warp item: every row of item `w` of A times x. The epilogue's vector
+// entries for the lane's row are loaded first (epi.load), then the row's
+// entries in predicated batches of four per lane (eight independent loads,
+// then four gathers in flight), the G-lane shuffle reduction, and the row step
+// (epi.apply) from lane i for the item's i-th row, so consecutive lanes touch
+// consecutive vector entries.
+template <typename T, class E>
+__device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
+                                          const T* __restrict__ x, int w, E& epi) {
     const int lane = threadIdx.x & 31;
     const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
     const int lg = __ldg(ws.lg + w);
     const int G = 1 << lg;
     const int g = lane >> lg, gl = lane & (G - 1);
     const int r = r0 + g;
+    const int er = r0 + lane;
+    const bool has_epi = lane < (32 >> lg) && er < r1;
+    typename E::Pre pre{};
+    if (has_epi) pre = epi.load(er);
     Acc<T> acc;
     if (r < r1) {
         const int b = __ldg(A.ptr + r), e = __ldg(A.ptr + r + 1);
-        int p = b + gl;
-        for (; p + 3 * G < e; p += 4 * G) {
-            const T a0 = __ldg(A.val + p), a1 = __ldg(A.val + p + G);
-            const T a2 = __ldg(A.val + p + 2 * G), a3 = __ldg(A.val + p + 3 * G);
-            const int j0 = __ldg(A.idx + p), j1 = __ldg(A.idx + p + G);
-            const int j2 = __ldg(A.idx + p + 2 * G), j3 = __ldg(A.idx + p + 3 * G);
-            const T x0 = __ldg(x + j0), x1 = __ldg(x + j1), x2 = __ldg(x + j2), x3 = __ldg(x + j3);
-            acc.add(a0, x0);
-            acc.add(a1, x1);
-            acc.add(a2, x2);
-            acc.add(a3, x3);
+        for (int p = b + gl; p < e; p += 4 * G) {
+            T a[4];
+            int j[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) {
+                const int q = p + u * G;
+                const bool ok = q < e;
+                a[u] = ok ? __ldg(A.val + q) : T(0);
+                j[u] = ok ? __ldg(A.idx + q) : 0;
+            }
+            T xv[4];
+#pragma unroll
+            for (int u = 0; u < 4; ++u) xv[u] = __ldg(x + j[u]);
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc.add(a[u], xv[u]);  // masked: 0 * x[0] adds 0
         }
-        for (; p < e; p += G) acc.add(__ldg(A.val + p), __ldg(x + __ldg(A.idx + p)));
     }
-    // reduce within each group of G lanes (all 32 lanes take part)
     for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(0xffffffffu, o, G);
-    // lane i fetches the sum of the warp's i-th row from lane i*G
-    Acc<T> mine = acc.shfl_from(0xffffffffu, (lane << lg) & 31);
-    if (lane < (32 >> lg) && r0 + lane < r1) f(r0 + lane, mine);
+    const Acc<T> mine = acc.shfl_from(0xffffffffu, (lane << lg) & 31);
+    if (has_epi) epi.apply(er, mine, pre);
+}
+
+// All warp items of the schedule, grid-stride over the launched warps
+// (CTAs are sized to stay resident, so per-CTA costs are paid once).
+template <typename T, class E>
+__device__ __forceinline__ void warp_rows_all(const WarpSched& ws, const Csr<T>& A,
+                                              const T* __restrict__ x, E& epi) {
+    const int stride = gridDim.x * kWarps;
+    for (int w = blockIdx.x * kWarps + (threadIdx.x >> 5); w < ws.nwarps; w += stride)
+        warp_item<T>(ws, A, x, w, epi);
 }
 
 }  // namespace igx

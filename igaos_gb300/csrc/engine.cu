@@ -64,13 +64,16 @@ void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<u
     }
 }
 
-static Sched upload_sched(Arena& ar, const int* ptr, int rows) {
+// Launch width: enough CTAs for every warp item, capped at what stays
+// resident (6 CTAs of 256 threads per SM at <= 40 registers); the kernels
+// grid-stride over the items.
+static Sched upload_sched(Arena& ar, const int* ptr, int rows, int resident_ctas) {
     std::vector<int> wr;
     std::vector<unsigned char> wl;
     build_warps(ptr, rows, wr, wl);
     Sched s;
     s.nwarps = (int)wl.size();
-    s.ctas = std::max(1, (s.nwarps + kWarps - 1) / kWarps);
+    s.ctas = std::max(1, std::min(resident_ctas, (s.nwarps + kWarps - 1) / kWarps));
     s.row = ar.alloc<int>(wr.size());
     s.lg = ar.alloc<unsigned char>(wl.size());
     CU(cudaMemcpy(s.row, wr.data(), sizeof(int) * wr.size(), cudaMemcpyHostToDevice));
@@ -146,12 +149,15 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         CU(cudaMemcpy(ap_, P.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(ai_, I.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(ax_, V.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
-        sA_ = upload_sched(ar_, P.data(), m);
+        int sms = 0;
+        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
+        const int resident = std::max(1, sms) * 6;
+        sA_ = upload_sched(ar_, P.data(), m, resident);
         permute_csr(n, cp, ci, acx, pc_, ipr_, P, I, V);
         CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(ci_, I.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(acx_, V.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
-        sAT_ = upload_sched(ar_, P.data(), n);
+        sAT_ = upload_sched(ar_, P.data(), n, resident);
     }
     // vectors
     auto vec = [&](const double* h, const std::vector<int>& perm) {
@@ -640,7 +646,7 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
                                  k_done, t_epoch, cand, h_ctl_->eta, h_ctl_->omega);
             }
             out.spmvs += 4;
-            if (o.deadline > 0 && elapsed() > o.deadline) {
+            if (elapsed() > o.deadline) {
                 out.status = IGAOS_STATUS_TIME_LIMIT;
                 break;
             }
@@ -710,7 +716,7 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     LoopOpts lo;
     lo.tol = o.tolerance;
     const bool finite_tl = o.time_limit_s > 0 && o.time_limit_s < 1e6;
-    lo.deadline = finite_tl ? o.time_limit_s : 0.0;
+    lo.deadline = o.time_limit_s;  // checked at every KKT check, as the reference (:1077-1083)
     lo.maxit = finite_tl ? 20000000LL : (long long)o.max_iterations;
     lo.check = o.check_period > 0 ? o.check_period : 64;
     lo.verbosity = o.verbosity;

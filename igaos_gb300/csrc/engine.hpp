@@ -78,7 +78,7 @@ struct GraphKey {
 
 struct LoopOpts {
     double tol = 1e-4;
-    double deadline = 0;    // seconds since solve start; <=0: none
+    double deadline = 1e300; // seconds since solve start, checked at each KKT check
     long long maxit = 500000;
     int check = 64;
     int verbosity = 0;

@@ -46,30 +46,37 @@ struct PrimalArgs {
 // written to the other parity slot so that a rejected attempt leaves the
 // accepted state untouched.
 template <typename T>
+struct PrimalEpi {
+    const T *c, *lo, *hi, *xc, *xa;
+    T *xn_out, *xa_out, *xbar;
+    T tau, w, dx2;
+    struct Pre {
+        T c, lo, hi, x, xa;
+    };
+    __device__ __forceinline__ Pre load(int j) const {
+        return Pre{__ldg(c + j), __ldg(lo + j), __ldg(hi + j), xc[j], xa[j]};
+    }
+    __device__ __forceinline__ void apply(int j, const Acc<T>& acc, const Pre& v) {
+        const T g = v.c + acc.result();
+        const T xn = fmin(fmax(fma(-tau, g, v.x), v.lo), v.hi);
+        xn_out[j] = xn;
+        xbar[j] = fma((T)2, xn, -v.x);
+        const T dx = xn - v.x;
+        dx2 = fma(dx, dx, dx2);
+        xa_out[j] = fma(w, xn - v.xa, v.xa);
+    }
+};
+
+template <typename T>
 __global__ void __launch_bounds__(kThreads) k_primal(PrimalArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
-    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
     const int p = cv.parity, q = p ^ 1;
-    const T tau = cv.tau, w = cv.w;
-    const T* __restrict__ xc = a.x[p];
-    const T* __restrict__ xa = a.xavg[p];
-    T* __restrict__ xn_out = a.x[q];
-    T* __restrict__ xa_out = a.xavg[q];
-    T dx2 = 0;
-    auto f = [&](int j, const Acc<T>& acc) {
-        const T g = a.c[j] + acc.result();
-        const T xv = xc[j];
-        const T xn = fmin(fmax(fma(-tau, g, xv), a.lo[j]), a.hi[j]);
-        xn_out[j] = xn;
-        a.xbar[j] = fma((T)2, xn, -xv);
-        const T dx = xn - xv;
-        dx2 = fma(dx, dx, dx2);
-        const T av = xa[j];
-        xa_out[j] = fma(w, xn - av, av);
-    };
-    if (wid < a.ws.nwarps) warp_rows<T>(a.ws, a.AT, a.y[p], wid, f);
+    PrimalEpi<T> epi{a.c, a.lo, a.hi, a.x[p], a.xavg[p], a.x[q], a.xavg[q], a.xbar,
+                     cv.tau, cv.w, (T)0};
+    warp_rows_all<T>(a.ws, a.AT, a.y[p], epi);
+    const T dx2 = epi.dx2;
     T v[1] = {dx2};
     block_sum_t<T, 1>(v, reinterpret_cast<T*>(smred));
     if (threadIdx.x == 0) {
@@ -95,6 +102,31 @@ struct DualArgs {
     int n_fac;
     int n_primal;
     DevCtl* ctl;
+};
+
+template <typename T>
+struct DualEpi {
+    const T *rmin, *rmax, *yc, *axc, *ya;
+    T *yn_out, *axc_out, *ya_out;
+    T sigma, w, dy2, cross;
+    struct Pre {
+        T lo, hi, y, ax, ya;
+    };
+    __device__ __forceinline__ Pre load(int i) const {
+        return Pre{__ldg(rmin + i), __ldg(rmax + i), yc[i], axc[i], ya[i]};
+    }
+    __device__ __forceinline__ void apply(int i, const Acc<T>& acc, const Pre& v) {
+        const T ab = acc.result();
+        const T t = fma(sigma, ab, v.y);
+        const T yn = fma(-sigma, fmin(fmax(t / sigma, v.lo), v.hi), t);
+        yn_out[i] = yn;
+        const T dy = yn - v.y;
+        const T adx = (T)0.5 * (ab - v.ax);
+        axc_out[i] = v.ax + adx;
+        dy2 = fma(dy, dy, dy2);
+        cross = fma(dy, adx, cross);
+        ya_out[i] = fma(w, yn - v.ya, v.ya);
+    }
 };
 
 // Adaptive step decision (src/pdhg/pdhg.cu:770-794), one thread. Host-side
@@ -151,35 +183,13 @@ __device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cro
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
-    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
     const int p = cv.parity, q = p ^ 1;
-    const T sigma = cv.sigma, w = cv.w;
-    const T* __restrict__ yc = a.y[p];
-    const T* __restrict__ axc = a.axc[p];
-    const T* __restrict__ ya = a.yavg[p];
-    T* __restrict__ yn_out = a.y[q];
-    T* __restrict__ axc_out = a.axc[q];
-    T* __restrict__ ya_out = a.yavg[q];
-    T dy2 = 0, cross = 0;
-    auto f = [&](int i, const Acc<T>& acc) {
-        const T ab = acc.result();
-        const T yv = yc[i];
-        const T t = fma(sigma, ab, yv);
-        const T yn = fma(-sigma, fmin(fmax(t / sigma, a.rmin[i]), a.rmax[i]), t);
-        yn_out[i] = yn;
-        const T dy = yn - yv;
-        const T ax = axc[i];
-        const T adx = (T)0.5 * (ab - ax);
-        axc_out[i] = ax + adx;
-        dy2 = fma(dy, dy, dy2);
-        cross = fma(dy, adx, cross);
-        const T av = ya[i];
-        ya_out[i] = fma(w, yn - av, av);
-    };
-    if (wid < a.ws.nwarps) warp_rows<T>(a.ws, a.A, a.xbar, wid, f);
-    T v[2] = {dy2, cross};
+    DualEpi<T> epi{a.rmin, a.rmax, a.y[p], a.axc[p], a.yavg[p], a.y[q], a.axc[q], a.yavg[q],
+                   cv.sigma, cv.w, (T)0, (T)0};
+    warp_rows_all<T>(a.ws, a.A, a.xbar, epi);
+    T v[2] = {epi.dy2, epi.cross};
     block_sum_t<T, 2>(v, reinterpret_cast<T*>(smred));
     if (threadIdx.x == 0) {
         Acc<T> e0, e1;
@@ -206,10 +216,9 @@ __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
 template <typename T, typename TO>
 __global__ void __launch_bounds__(kThreads)
     k_spmv(WarpSched ws, Csr<T> A, const T* __restrict__ x, TO* __restrict__ y) {
-    __shared__ __align__(16) double smred[kWarps * 4];
-    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     auto f = [&](int r, const Acc<T>& acc) { y[r] = (TO)acc.result_d(); };
-    if (wid < ws.nwarps) warp_rows<T>(ws, A, x, wid, f);
+    PlainEpi<decltype(f)> epi{f};
+    warp_rows_all<T>(ws, A, x, epi);
 }
 
 // -------------------------------------------------------- Ruiz equilibration
@@ -391,7 +400,6 @@ struct KktArgs {
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
-    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const int v = blockIdx.y;
     const T* __restrict__ yv = a.y[v];
     double pv = 0.0, pa = 0.0, prow = 0.0, ymax = 0.0;
@@ -408,7 +416,8 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
         prow = smax(prow, viol / (1.0 + sc));
         ymax = smax(ymax, fabs((double)yv[i] * (1.0 / a.dr[i])));
     };
-    if (wid < a.wsA.nwarps) warp_rows<T>(a.wsA, a.A, a.x[v], wid, f);
+    PlainEpi<decltype(f)> epi{f};
+    warp_rows_all<T>(a.wsA, a.A, a.x[v], epi);
     double r[4] = {pv, pa, prow, ymax};
     block_max<4>(r, smred);
     const int nt = gridDim.x;
@@ -434,7 +443,6 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
 template <typename T>
 __global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
-    const int wid = blockIdx.x * kWarps + (threadIdx.x >> 5);
     const int v = blockIdx.y;
     const T* __restrict__ xv = a.x[v];
     const double dz = 1e-8 * (1.0 + a.cmax);
@@ -459,7 +467,8 @@ __global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a) {
             else if (-d > dz) unb = 1.0;
         }
     };
-    if (wid < a.wsAT.nwarps) warp_rows<T>(a.wsAT, a.AT, a.y[v], wid, f);
+    PlainEpi<decltype(f)> epi{f};
+    warp_rows_all<T>(a.wsAT, a.AT, a.y[v], epi);
     double mx[2] = {dv, unb};
     block_max<2>(mx, smred);
     double sm2[2] = {op, od};

@@ -69,8 +69,8 @@ def test_fp64_fixed_budget_tracks_oracle_on_zipf(native, orc):
     algorithm (checks, restarts and all) lands on the same point."""
     from igaos_gb300 import capi
     lp, _ = make("zipf400x1000")
-    want = orc.pdhg_solve(orc.lp_from(lp), tolerance=1e-12, time_limit=0.0, max_iterations=3000)
-    got = capi.solve_lp(lp, tolerance=1e-12, time_limit=0.0, max_iterations=3000)
+    want = orc.pdhg_solve(orc.lp_from(lp), tolerance=1e-12, time_limit=1e9, max_iterations=3000)
+    got = capi.solve_lp(lp, tolerance=1e-12, time_limit=1e9, max_iterations=3000)
     assert got["iterations"] == want["iterations"] == 3000
     assert got["restarts"] == want["restarts"]
     assert rel(got["objective"], want["objective"]) <= 1e-6
@@ -95,8 +95,8 @@ def test_deterministic_repeat(native):
     from igaos_gb300 import capi
     lp, _ = make("zipf400x1000")
     with capi.Problem(lp) as P:
-        a = P.solve(tolerance=1e-12, time_limit=0.0, max_iterations=3000)
-        b = P.solve(tolerance=1e-12, time_limit=0.0, max_iterations=3000)
+        a = P.solve(tolerance=1e-12, time_limit=1e9, max_iterations=3000)
+        b = P.solve(tolerance=1e-12, time_limit=1e9, max_iterations=3000)
     assert a["objective"] == b["objective"] and a["iterations"] == b["iterations"]
     assert np.array_equal(a["x"], b["x"])
 
@@ -121,7 +121,7 @@ def test_iteration_limit_and_time_limit(native):
     from igaos_gb300 import capi
     lp, _ = make("rand200x500-s0")
     # max_iterations binds only without a finite time limit (src/pdhg/pdhg.cu:669-671)
-    r = capi.solve_lp(lp, tolerance=1e-12, time_limit=0.0, max_iterations=200)
+    r = capi.solve_lp(lp, tolerance=1e-12, time_limit=1e9, max_iterations=200)
     assert r["status_name"] == "iteration-limit" and r["iterations"] == 200
     r = capi.solve_lp(lp, tolerance=1e-14, time_limit=0.05)
     assert r["status_name"] == "time-limit"
@@ -133,7 +133,7 @@ def test_short_run_without_check_is_not_certified(native):
     (the reference would report its zero-initialised metrics as certified)."""
     from igaos_gb300 import capi
     lp, _ = make("rand200x500-s0")
-    r = capi.solve_lp(lp, tolerance=1e-8, time_limit=0.0, max_iterations=10)
+    r = capi.solve_lp(lp, tolerance=1e-8, time_limit=1e9, max_iterations=10)
     assert r["iterations"] == 10 and r["status_name"] == "iteration-limit"
 
 
