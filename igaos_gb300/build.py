@@ -55,24 +55,29 @@ def _deps():
     return hs
 
 
-def build_lib(force=False, verbose=False):
-    os.makedirs(BUILD, exist_ok=True)
+def build_lib(force=False, verbose=False, defines=(), out=None):
+    """Builds the engine library; `defines` (e.g. ["IGX_HOT_CTAS=7"]) and `out`
+    produce a variant library elsewhere (tuning sweeps)."""
+    out = out or LIB
+    objdir = BUILD if out == LIB else os.path.join(os.path.dirname(out), "_obj")
+    os.makedirs(objdir, exist_ok=True)
     deps = _deps()
     objs = []
     jobs = []
+    dflags = [f"-D{d}" for d in defines]
     for src in CU_SOURCES:
         s = os.path.join(CSRC, src)
-        o = os.path.join(BUILD, src + ".o")
+        o = os.path.join(objdir, src + ".o")
         objs.append(o)
         if force or _newer(o, [s] + deps):
-            jobs.append([_nvcc(), *NVFLAGS, "-c", s, "-o", o])
+            jobs.append([_nvcc(), *NVFLAGS, *dflags, "-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for r in ex.map(_run, jobs):
             if verbose and r.stderr:
                 print(r.stderr, file=sys.stderr)
-    if force or _newer(LIB, objs):
-        _run([_nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lcudart"])
-    return LIB
+    if force or _newer(out, objs):
+        _run([_nvcc(), *ARCH, "-shared", "-o", out, *objs, "-lcudart"])
+    return out
 
 
 def build_cli(force=False):

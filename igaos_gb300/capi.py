@@ -12,7 +12,8 @@ import os
 import numpy as np
 
 _PKG = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_PKG, "libigaos_pdhg.so")
+# IGAOS_PDHG_LIB selects another build of the same library (tuning variants)
+LIB_PATH = os.environ.get("IGAOS_PDHG_LIB") or os.path.join(_PKG, "libigaos_pdhg.so")
 
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_NODEVICE, ERR_NUMERIC, ERR_TIMEOUT = range(7)
 FP64, FP32_REFINE, FP32 = 0, 1, 2

@@ -23,6 +23,13 @@ namespace igx {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+// Resident CTAs per SM the hot kernels are compiled for (8 x 256 threads =
+// the SM's 64 warps: the gathers are latency-bound, so occupancy is what
+// keeps bytes in flight). Launch widths use the same figure.
+#ifndef IGX_HOT_CTAS
+#define IGX_HOT_CTAS 8
+#endif
+constexpr int kHotCtasPerSm = IGX_HOT_CTAS;
 
 template <typename T>
 struct Csr {

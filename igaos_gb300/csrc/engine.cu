@@ -151,7 +151,7 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         CU(cudaMemcpy(ax_, V.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
         int sms = 0;
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
-        const int resident = std::max(1, sms) * 6;
+        const int resident = std::max(1, sms) * kHotCtasPerSm;
         sA_ = upload_sched(ar_, P.data(), m, resident);
         permute_csr(n, cp, ci, acx, pc_, ipr_, P, I, V);
         CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));

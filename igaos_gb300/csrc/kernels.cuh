@@ -68,7 +68,7 @@ struct PrimalEpi {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_primal(PrimalArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_primal(PrimalArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
@@ -181,7 +181,7 @@ __device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cro
 // reduction of all partials (kern_dotfin, :99-125) and the step decision that
 // the reference made on the host after a blocking copy (:768-794).
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_dual(DualArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
@@ -212,9 +212,9 @@ __global__ void __launch_bounds__(kThreads) k_dual(DualArgs<T> a) {
 }
 
 // ------------------------------------------------------------- plain SpMV
-// y = A x (Spmv::mv, src/pdhg/pdhg.cu:143-157), optional skip flag.
+// y = A x (Spmv::mv, src/pdhg/pdhg.cu:143-157).
 template <typename T, typename TO>
-__global__ void __launch_bounds__(kThreads)
+__global__ void __launch_bounds__(kThreads, kHotCtasPerSm)
     k_spmv(WarpSched ws, Csr<T> A, const T* __restrict__ x, TO* __restrict__ y) {
     auto f = [&](int r, const Acc<T>& acc) { y[r] = (TO)acc.result_d(); };
     PlainEpi<decltype(f)> epi{f};
@@ -398,7 +398,7 @@ struct KktArgs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_rows(KktArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const int v = blockIdx.y;
     const T* __restrict__ yv = a.y[v];
@@ -441,7 +441,7 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a) {
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_cols(KktArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const int v = blockIdx.y;
     const T* __restrict__ xv = a.x[v];
