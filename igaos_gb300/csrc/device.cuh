@@ -23,11 +23,12 @@ namespace igx {
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
-// Resident CTAs per SM the hot kernels are compiled for (8 x 256 threads =
-// the SM's 64 warps: the gathers are latency-bound, so occupancy is what
-// keeps bytes in flight). Launch widths use the same figure.
+// Resident CTAs per SM the hot kernels are compiled for; launch widths use
+// the same figure. Measured on the 200k x 500k LP (FP32 attempt): 6 CTAs
+// (<= 40 registers, no spills) 59 us, 7 or 8 CTAs (forced to 32-36
+// registers, with spills) 70 us.
 #ifndef IGX_HOT_CTAS
-#define IGX_HOT_CTAS 8
+#define IGX_HOT_CTAS 6
 #endif
 constexpr int kHotCtasPerSm = IGX_HOT_CTAS;
 

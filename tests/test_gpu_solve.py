@@ -66,17 +66,17 @@ def test_fp64_tracks_oracle_pdhg(native, orc, name):
 
 def test_fp64_fixed_budget_tracks_oracle_on_zipf(native, orc):
     """On the shape where neither side converges, a fixed budget of the same
-    algorithm (checks, restarts and all) lands near the same point: a
-    restart check can flip on rounding-level differences over thousands of
-    iterations, so restarts may differ by one epoch and the objective by the
-    progress of a few hundred iterations."""
+    algorithm (checks, restarts and all) lands on the same point. The
+    trajectory there is chaotic -- a 1-ulp change of c moves the oracle's own
+    objective by 1e-7 after 256 iterations and by 4e-4 after 640 -- so the
+    budget is 256 iterations (four checks)."""
     from igaos_gb300 import capi
     lp, _ = make("zipf400x1000")
-    want = orc.pdhg_solve(orc.lp_from(lp), tolerance=1e-12, time_limit=1e9, max_iterations=3000)
-    got = capi.solve_lp(lp, tolerance=1e-12, time_limit=1e9, max_iterations=3000)
-    assert got["iterations"] == want["iterations"] == 3000
-    assert abs(got["restarts"] - want["restarts"]) <= 2
-    assert rel(got["objective"], want["objective"]) <= 2e-3
+    want = orc.pdhg_solve(orc.lp_from(lp), tolerance=1e-12, time_limit=1e9, max_iterations=256)
+    got = capi.solve_lp(lp, tolerance=1e-12, time_limit=1e9, max_iterations=256)
+    assert got["iterations"] == want["iterations"] == 256
+    assert got["restarts"] == want["restarts"]
+    assert rel(got["objective"], want["objective"]) <= 1e-5
 
 
 def test_solution_vectors_certify(native, orc):
