@@ -497,6 +497,8 @@ void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* 
     ka.cu = v.cu;
     ka.rmin = v.rmin;
     ka.rmax = v.rmax;
+    ka.slo = VecSel<T>::l(v);
+    ka.shi = VecSel<T>::u(v);
     ka.cmax = v.cmax;
     ka.part = kkt_part_;
     ka.out = met_;
@@ -696,6 +698,17 @@ void Engine::fetch_scaled(const T* src, int len, double* dst) {
     CU(cudaStreamSynchronize(st_));
 }
 
+// Original-unit x (device numbering) of a scaled iterate, with the FP32
+// at-bound rule of unscale_x.
+template <typename T>
+void Engine::unscale_cols(const T* xs, const Vecs& v, double* host_out) {
+    k_unscale_cols<T><<<grid_for(n), kThreads, 0, st_>>>(n, xs, VecSel<T>::l(v), VecSel<T>::u(v),
+                                                          dc_, v.cl, v.cu, tmp_n_);
+    CU(cudaGetLastError());
+    CU(cudaMemcpyAsync(host_out, tmp_n_, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+    CU(cudaStreamSynchronize(st_));
+}
+
 // -------------------------------------------------------------------- solve
 static void fill_message(igaos_pdhg_result& r, const char* s) {
     std::snprintf(r.message, sizeof(r.message), "%s", s);
@@ -732,7 +745,7 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
         const int p = out.parity;
         const float* fx = out.use_inc ? w.xb : (out.last_is_avg ? w.xavg[p] : w.x[p]);
         const float* fy = out.use_inc ? w.yb : (out.last_is_avg ? w.yavg[p] : w.y[p]);
-        fetch_scaled<float>(fx, n, hx.data());
+        unscale_cols<float>(fx, base_, hx.data());
         fetch_scaled<float>(fy, m, hy.data());
     } else {
         out = loop<double>(base_, lo);
@@ -740,7 +753,7 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
         const int p = out.parity;
         const double* fx = out.use_inc ? w.xb : (out.last_is_avg ? w.xavg[p] : w.x[p]);
         const double* fy = out.use_inc ? w.yb : (out.last_is_avg ? w.yavg[p] : w.y[p]);
-        fetch_scaled<double>(fx, n, hx.data());
+        unscale_cols<double>(fx, base_, hx.data());
         fetch_scaled<double>(fy, m, hy.data());
     }
     const double secs = elapsed();
@@ -780,7 +793,7 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     }
     // unscale (x = dc x~, y = y~/dr) and return to the caller's numbering
     if (x)
-        for (int j = 0; j < n; ++j) x[pc_[j]] = hx[j] * hp_dc_[j];
+        for (int j = 0; j < n; ++j) x[pc_[j]] = hx[j];  // already in original units
     if (y)
         for (int i = 0; i < m; ++i) y[pr_[i]] = 1.0 * hy[i] / hp_dr_[i];
 }

@@ -179,6 +179,7 @@ class Engine {
     void download_ctl();
     double elapsed() const;
     void setup_scaling();
+    template <typename T> void unscale_cols(const T* xs, const Vecs& v, double* host_out);
     void power_iteration();
     void solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x, double* y);
 };

@@ -6,6 +6,31 @@
 
 namespace igx {
 
+// Original-unit column value x = dc * x~ (src/pdhg/pdhg.cu:712). An FP32
+// iterate projected onto its FP32-rounded bound is exactly at that bound:
+// it maps to the FP64 bound itself (dc * fl32(l/dc) would sit ~6e-8 |l|
+// away, outside evaluate()'s 1e-9 "at bound" band). FP64 iterates are
+// unscaled as the reference does, without snapping.
+__device__ __forceinline__ double unscale_x(double xs, double, double, double dc, double,
+                                           double) {
+    return xs * dc;
+}
+__device__ __forceinline__ double unscale_x(float xs, float slo, float shi, double dc, double lo,
+                                           double hi) {
+    if (xs == slo) return lo;
+    if (xs == shi) return hi;
+    return (double)xs * dc;
+}
+
+template <typename TI>
+__global__ void k_unscale_cols(int n, const TI* __restrict__ xs, const TI* __restrict__ slo,
+                               const TI* __restrict__ shi, const double* __restrict__ dc,
+                               const double* __restrict__ lo, const double* __restrict__ hi,
+                               double* __restrict__ out) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x)
+        out[j] = unscale_x(xs[j], slo[j], shi[j], dc[j], lo[j], hi[j]);
+}
+
 // ------------------------------------------------------------ attempt state
 // Per-launch view of the control block, read once per CTA.
 template <typename T>
@@ -391,6 +416,7 @@ struct KktArgs {
     const T* y[2];
     const double *dr, *dc;
     const double *c, *cl, *cu, *rmin, *rmax;  // original units
+    const T *slo, *shi;                       // scaled column bounds, iterate precision
     double cmax;
     double* part;   // >= 2 * max(tiles) * 4 doubles
     DevMetrics* out;
@@ -449,7 +475,7 @@ __global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_cols(KktArgs<T>
     double dv = 0.0, op = 0.0, od = 0.0, unb = 0.0;
     auto f = [&](int j, const Acc<T>& acc) {
         const double d = a.c[j] + 1.0 * acc.result_d() / a.dc[j];
-        const double x = (double)xv[j] * a.dc[j];
+        const double x = unscale_x(xv[j], a.slo[j], a.shi[j], a.dc[j], a.cl[j], a.cu[j]);
         const double cl = a.cl[j], cu = a.cu[j];
         const double bnd = fabs(isfinite(cu) ? cu : cl);
         const double tol = 1e-9 * (1.0 + bnd);
