@@ -82,6 +82,8 @@ def lib():
         L.igaos_pdhg_iterate.argtypes = [C.c_void_p, C.c_int, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]
         L.igaos_pdhg_evaluate.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.igaos_pdhg_spmv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp]
+        # device-pointer entry point: every pointer is passed as an address
+        L.igaos_pdhg_evaluate_noalloc.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 15
         _LIB = L
     return _LIB
 

@@ -104,6 +104,11 @@ void transpose_host(int m, int n, const int* ap, const int* ai, const double* ax
 }
 }  // namespace
 
+int igx::igx_set_error(int code, const char* msg) {
+    if (code == IGAOS_PDHG_OK) return ok();
+    return fail(code, msg);
+}
+
 extern "C" {
 
 int igaos_pdhg_abi_version(void) { return IGAOS_PDHG_ABI_VERSION; }

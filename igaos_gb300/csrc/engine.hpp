@@ -19,6 +19,10 @@ struct CudaError : std::runtime_error {
 };
 
 void cuda_check(cudaError_t e, const char* what, int line);
+
+// Records the calling thread's last error (igaos_pdhg_last_error) and returns
+// `code`; IGAOS_PDHG_OK clears it.
+int igx_set_error(int code, const char* msg);
 #define CU(x) ::igx::cuda_check((x), #x, __LINE__)
 
 // Every device allocation of a problem, freed together.
@@ -175,11 +179,11 @@ class Engine {
     template <typename T> void spmv_dev(bool transpose, const T* x, T* y);
     template <typename T> LoopOut loop(const Vecs& v, const LoopOpts& o);
     template <typename T> void fetch_scaled(const T* src, int len, double* dst);
+    template <typename T> void unscale_cols(const T* xs, const Vecs& v, double* host_out);
     void upload_ctl();
     void download_ctl();
     double elapsed() const;
     void setup_scaling();
-    template <typename T> void unscale_cols(const T* xs, const Vecs& v, double* host_out);
     void power_iteration();
     void solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x, double* y);
 };

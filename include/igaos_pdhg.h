@@ -186,6 +186,30 @@ int igaos_pdhg_evaluate(igaos_pdhg_problem* p, const double* x,
 int igaos_pdhg_spmv(igaos_pdhg_problem* p, int transpose, int precision,
                     const double* x, double* y);
 
+/* Allocation-free FP64 KKT metrics, for callers that cannot call cudaMalloc
+ * (device memory owned by a framework allocator or a fixed pool, or loops
+ * where an allocation's device synchronisation is not acceptable). No
+ * counterpart in the reference. Every pointer is a DEVICE pointer owned by
+ * the caller: A in original units as CSR (ap, ai, ax) and CSC (cp, ci, acx),
+ * c, cl, cu (n), rmin, rmax (m), the candidate x (n), y (m), and out6, which
+ * receives {pinf, dinf, gap, op, od, prow} as evaluate() defines them
+ * (src/pdhg/pdhg.cu:173-254). Work is enqueued on `stream` (a cudaStream_t,
+ * NULL = default stream); the caller synchronises before reading out6.
+ * Scratch is a fixed 1 MiB array in device memory that every GPU loading the
+ * library holds until exit; m and n are limited to 4,194,304 (larger sizes
+ * return IGAOS_PDHG_ERR_INVALID). The first call on a device looks up that
+ * array's device address (no allocation); make that first call before any
+ * stream capture. All calls share the array: calls that overlap on the GPU
+ * (other streams, other threads) race and must be serialised by the caller.
+ * Nothing is allocated: no cudaMalloc, cudaFree or allocating library call. */
+int igaos_pdhg_evaluate_noalloc(int m, int n, const int* ap, const int* ai,
+                                const double* ax, const int* cp, const int* ci,
+                                const double* acx, const double* c,
+                                const double* cl, const double* cu,
+                                const double* rmin, const double* rmax,
+                                const double* x, const double* y, double* out6,
+                                void* stream);
+
 #ifdef __cplusplus
 }
 #endif
