@@ -352,6 +352,7 @@ template <> struct VecSel<double> {
     static const double* u(const Vecs& v) { return v.scu; }
     static const double* rl(const Vecs& v) { return v.srmin; }
     static const double* ru(const Vecs& v) { return v.srmax; }
+    static const double* yh(const Vecs&) { return nullptr; }
 };
 template <> struct VecSel<float> {
     static const float* c(const Vecs& v) { return v.fc; }
@@ -359,6 +360,7 @@ template <> struct VecSel<float> {
     static const float* u(const Vecs& v) { return v.fcu; }
     static const float* rl(const Vecs& v) { return v.frmin; }
     static const float* ru(const Vecs& v) { return v.frmax; }
+    static const float* yh(const Vecs& v) { return v.fyhat; }
 };
 
 // Enqueues `count` line-search attempts (2 launches each). With graphs the
@@ -395,6 +397,7 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     da.part = reinterpret_cast<Acc<T>*>(w.part_d);
     da.part_primal = reinterpret_cast<const Acc<T>*>(w.part_p);
     da.n_primal = sAT_.ctas;
+    da.yhat = VecSel<T>::yh(v);
     da.fac = fac_;
     da.n_fac = kFac;
     da.ctl = ctl_;
@@ -525,6 +528,14 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
     CU(cudaMemsetAsync(w.y[0], 0, mb, st_));
     CU(cudaMemsetAsync(w.yavg[0], 0, mb, st_));
     CU(cudaMemsetAsync(w.axc[0], 0, mb, st_));
+    // anchored FP32 iterations (FP32 + FP64 refinement): start at anchor 0
+    const bool anch = v.fyhat != nullptr;
+    if (anch) {
+        CU(cudaMemsetAsync(anc_.xh, 0, sizeof(double) * n, st_));
+        CU(cudaMemsetAsync(anc_.yh, 0, sizeof(double) * m, st_));
+        anchor_data();
+        out.spmvs += 2;
+    }
     std::memset(h_ctl_, 0, sizeof(DevCtl));
     h_ctl_->eta = o.eta_init;
     h_ctl_->omega = o.omega_init;
@@ -557,7 +568,12 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
         if (k_done % CHECK == 0) {
             ++out.checks;
             const int p = h_ctl_->parity;
-            kkt<T>(v, w.x[p], w.y[p], w.xavg[p], w.yavg[p], 2);
+            if (anch) {  // FP64 metrics of the full iterates anchor + delta
+                anchor_full(p);
+                kkt<double>(base_, anc_.xf[0], anc_.yf[0], anc_.xf[1], anc_.yf[1], 2);
+            } else {
+                kkt<T>(v, w.x[p], w.y[p], w.xavg[p], w.yavg[p], 2);
+            }
             const DevMetrics mc = h_met_[0], ma = h_met_[1];
             const double ec = mc.finite ? mc.err : kInf;
             const double ea = ma.finite ? ma.err : kInf;
@@ -580,23 +596,33 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
                     inc_src = cnd;
                 }
             }
-            if (inc_src >= 0) {
+            if (inc_src >= 0 && anch) {
+                CU(cudaMemcpyAsync(anc_.xb, anc_.xf[inc_src], sizeof(double) * n, cudaMemcpyDeviceToDevice, st_));
+                CU(cudaMemcpyAsync(anc_.yb, anc_.yf[inc_src], sizeof(double) * m, cudaMemcpyDeviceToDevice, st_));
+            } else if (inc_src >= 0) {
                 CU(cudaMemcpyAsync(w.xb, inc_src ? w.xavg[p] : w.x[p], nb, cudaMemcpyDeviceToDevice, st_));
                 CU(cudaMemcpyAsync(w.yb, inc_src ? w.yavg[p] : w.y[p], mb, cudaMemcpyDeviceToDevice, st_));
             }
             // rollback (src/pdhg/pdhg.cu:965-988)
             if (mc.pinf >= 0.5 && have_inc && k_done - last_rollback > 2000) {
-                CU(cudaMemcpyAsync(w.x[p], w.xb, nb, cudaMemcpyDeviceToDevice, st_));
-                CU(cudaMemcpyAsync(w.y[p], w.yb, mb, cudaMemcpyDeviceToDevice, st_));
-                CU(cudaMemcpyAsync(w.xavg[p], w.xb, nb, cudaMemcpyDeviceToDevice, st_));
-                CU(cudaMemcpyAsync(w.yavg[p], w.yb, mb, cudaMemcpyDeviceToDevice, st_));
+                if (anch) {
+                    anchor_to(anc_.xb, anc_.yb);
+                    anchor_zero(p);
+                    ++out.anchors;
+                    out.spmvs += 2;
+                } else {
+                    CU(cudaMemcpyAsync(w.x[p], w.xb, nb, cudaMemcpyDeviceToDevice, st_));
+                    CU(cudaMemcpyAsync(w.y[p], w.yb, mb, cudaMemcpyDeviceToDevice, st_));
+                    CU(cudaMemcpyAsync(w.xavg[p], w.xb, nb, cudaMemcpyDeviceToDevice, st_));
+                    CU(cudaMemcpyAsync(w.yavg[p], w.yb, mb, cudaMemcpyDeviceToDevice, st_));
+                    spmv_dev<T>(false, w.x[p], w.axc[p]);
+                    ++out.spmvs;
+                }
                 h_ctl_->eta = std::min(h_ctl_->eta, 0.5 * o.eta0);
                 h_ctl_->hn = 0;
                 epoch_start = k_done;
                 epoch_kkt = -1.0;
                 prev_cand = kInf;
-                spmv_dev<T>(false, w.x[p], w.axc[p]);
-                ++out.spmvs;
                 last_rollback = k_done;
             }
             // restart + primal weight (src/pdhg/pdhg.cu:1001-1075)
@@ -614,22 +640,35 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
             prev_cand = cand;
             if (restart_now) {
                 ++out.restarts;
-                if (ea < ec) {
-                    CU(cudaMemcpyAsync(w.x[p], w.xavg[p], nb, cudaMemcpyDeviceToDevice, st_));
-                    CU(cudaMemcpyAsync(w.y[p], w.yavg[p], mb, cudaMemcpyDeviceToDevice, st_));
+                if (anch) {
+                    // the restart point becomes the new FP64 anchor (A x and
+                    // the deltas restart from zero, residual data refreshed)
+                    anchor_to(anc_.xf[ea < ec ? 1 : 0], anc_.yf[ea < ec ? 1 : 0]);
+                    anchor_zero(p);
+                    ++out.anchors;
+                    out.spmvs += 2;
+                } else {
+                    if (ea < ec) {
+                        CU(cudaMemcpyAsync(w.x[p], w.xavg[p], nb, cudaMemcpyDeviceToDevice, st_));
+                        CU(cudaMemcpyAsync(w.y[p], w.yavg[p], mb, cudaMemcpyDeviceToDevice, st_));
+                    }
+                    CU(cudaMemcpyAsync(w.xavg[p], w.x[p], nb, cudaMemcpyDeviceToDevice, st_));
+                    CU(cudaMemcpyAsync(w.yavg[p], w.y[p], mb, cudaMemcpyDeviceToDevice, st_));
+                    spmv_dev<T>(false, w.x[p], w.axc[p]);
+                    ++out.spmvs;
                 }
-                CU(cudaMemcpyAsync(w.xavg[p], w.x[p], nb, cudaMemcpyDeviceToDevice, st_));
-                CU(cudaMemcpyAsync(w.yavg[p], w.y[p], mb, cudaMemcpyDeviceToDevice, st_));
                 h_ctl_->hn = 0;
                 epoch_start = k_done;
                 epoch_kkt = cand;
                 prev_cand = kInf;
-                spmv_dev<T>(false, w.x[p], w.axc[p]);
-                ++out.spmvs;
                 if (have_pe) {
                     ++launches_;
-                    k_diffnorms<T><<<red_blocks_, kThreads, 0, st_>>>(
-                        n, w.x[p], w.pesx, m, w.y[p], w.pesy, red_part_, scal_, ticket_ + 1);
+                    if (anch)
+                        k_diffnorms<double><<<red_blocks_, kThreads, 0, st_>>>(
+                            n, anc_.xh, anc_.pesx, m, anc_.yh, anc_.pesy, red_part_, scal_, ticket_ + 1);
+                    else
+                        k_diffnorms<T><<<red_blocks_, kThreads, 0, st_>>>(
+                            n, w.x[p], w.pesx, m, w.y[p], w.pesy, red_part_, scal_, ticket_ + 1);
                     CU(cudaGetLastError());
                     CU(cudaMemcpyAsync(h_scal_, scal_, 2 * sizeof(double), cudaMemcpyDeviceToHost, st_));
                     CU(cudaStreamSynchronize(st_));
@@ -641,8 +680,13 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
                     }
                 }
                 have_pe = true;
-                CU(cudaMemcpyAsync(w.pesx, w.x[p], nb, cudaMemcpyDeviceToDevice, st_));
-                CU(cudaMemcpyAsync(w.pesy, w.y[p], mb, cudaMemcpyDeviceToDevice, st_));
+                if (anch) {
+                    CU(cudaMemcpyAsync(anc_.pesx, anc_.xh, sizeof(double) * n, cudaMemcpyDeviceToDevice, st_));
+                    CU(cudaMemcpyAsync(anc_.pesy, anc_.yh, sizeof(double) * m, cudaMemcpyDeviceToDevice, st_));
+                } else {
+                    CU(cudaMemcpyAsync(w.pesx, w.x[p], nb, cudaMemcpyDeviceToDevice, st_));
+                    CU(cudaMemcpyAsync(w.pesy, w.y[p], mb, cudaMemcpyDeviceToDevice, st_));
+                }
                 if (o.verbosity > 1)
                     std::fprintf(stderr, "[pdhg-gb300] restart @k=%lld t=%lld r=%.3e eta=%.3e om=%.3e\n",
                                  k_done, t_epoch, cand, h_ctl_->eta, h_ctl_->omega);
@@ -666,7 +710,12 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
     if (!have_last && !out.numeric_failure) {
         // no check ran (fewer than CHECK iterations): evaluate the last iterate
         const int p = h_ctl_->parity;
-        kkt<T>(v, w.x[p], w.y[p], w.x[p], w.y[p], 1);
+        if (anch) {
+            anchor_full(p);
+            kkt<double>(base_, anc_.xf[0], anc_.yf[0], anc_.xf[0], anc_.yf[0], 1);
+        } else {
+            kkt<T>(v, w.x[p], w.y[p], w.x[p], w.y[p], 1);
+        }
         out.last = h_met_[0];
         out.last_is_avg = false;
         out.spmvs += 2;
@@ -947,11 +996,144 @@ void Engine::spmv(int transpose, int precision, const double* x_user, double* y_
 }  // namespace igx
 
 namespace igx {
-// FP32 iterates with FP64 residual refinement: filled in below the basic
-// loops once they are validated on the device.
-void Engine::solve_refine(const igaos_pdhg_options&, igaos_pdhg_result& r, double*, double*) {
-    r.status = IGAOS_STATUS_ERROR;
-    r.error_code = IGAOS_PDHG_ERR_INVALID;
-    std::snprintf(r.message, sizeof(r.message), "FP32_REFINE precision is not available yet");
+// ------------------------------------ FP32 iterations with FP64 refinement
+// The reference iteration (line search, averaging, checks, restarts, primal
+// weight) on FP32 deltas from an FP64 anchor: every restart (and rollback)
+// makes the restart point the new anchor, i.e. restarts PDHG on the residual
+// problem seen from it, whose data -- reduced costs c~ + A~^T yh, row bounds
+// minus A~ xh, the shifted box -- are formed in FP64 and rounded once. The
+// KKT checks, the incumbent and the answer are FP64 on anchor + delta, so the
+// attainable accuracy is set by FP64, while every attempt streams FP32.
+void Engine::ensure_anchor() {
+    if (have_anchor_) return;
+    anc_.xh = ar_.alloc<double>(n);
+    anc_.yh = ar_.alloc<double>(m);
+    for (int s = 0; s < 2; ++s) {
+        anc_.xf[s] = ar_.alloc<double>(n);
+        anc_.yf[s] = ar_.alloc<double>(m);
+    }
+    anc_.xb = ar_.alloc<double>(n);
+    anc_.yb = ar_.alloc<double>(m);
+    anc_.pesx = ar_.alloc<double>(n);
+    anc_.pesy = ar_.alloc<double>(m);
+    anc_.aty = ar_.alloc<double>(n);
+    anc_.ax = ar_.alloc<double>(m);
+    av_ = base_;  // original-unit vectors are the base LP's
+    av_.fc = ar_.alloc<float>(n);
+    av_.fcl = ar_.alloc<float>(n);
+    av_.fcu = ar_.alloc<float>(n);
+    av_.frmin = ar_.alloc<float>(m);
+    av_.frmax = ar_.alloc<float>(m);
+    av_.fyhat = ar_.alloc<float>(m);
+    have_anchor_ = true;
+}
+
+void Engine::anchor_data() {
+    spmv_dev<double>(false, anc_.xh, anc_.ax);
+    spmv_dev<double>(true, anc_.yh, anc_.aty);
+    k_anchor_cols<<<grid_for(n), kThreads, 0, st_>>>(n, base_.sc, base_.scl, base_.scu, anc_.aty,
+                                                     anc_.xh, av_.fc, av_.fcl, av_.fcu);
+    k_anchor_rows<<<grid_for(m), kThreads, 0, st_>>>(m, base_.srmin, base_.srmax, anc_.ax,
+                                                     anc_.yh, av_.frmin, av_.frmax, av_.fyhat);
+    launches_ += 2;
+    CU(cudaGetLastError());
+}
+
+void Engine::anchor_zero(int p) {
+    Work<float>& w = w32_;
+    CU(cudaMemsetAsync(w.x[p], 0, sizeof(float) * n, st_));
+    CU(cudaMemsetAsync(w.xavg[p], 0, sizeof(float) * n, st_));
+    CU(cudaMemsetAsync(w.y[p], 0, sizeof(float) * m, st_));
+    CU(cudaMemsetAsync(w.yavg[p], 0, sizeof(float) * m, st_));
+    CU(cudaMemsetAsync(w.axc[p], 0, sizeof(float) * m, st_));
+}
+
+void Engine::anchor_full(int p) {
+    Work<float>& w = w32_;
+    const int gn = grid_for(n), gm = grid_for(m);
+    k_anchor_full_cols<<<gn, kThreads, 0, st_>>>(n, anc_.xh, w.x[p], av_.fcl, av_.fcu, base_.scl,
+                                                 base_.scu, anc_.xf[0]);
+    k_anchor_full_cols<<<gn, kThreads, 0, st_>>>(n, anc_.xh, w.xavg[p], av_.fcl, av_.fcu,
+                                                 base_.scl, base_.scu, anc_.xf[1]);
+    k_anchor_full_rows<<<gm, kThreads, 0, st_>>>(m, anc_.yh, w.y[p], anc_.yf[0]);
+    k_anchor_full_rows<<<gm, kThreads, 0, st_>>>(m, anc_.yh, w.yavg[p], anc_.yf[1]);
+    launches_ += 4;
+    CU(cudaGetLastError());
+}
+
+void Engine::anchor_to(const double* x, const double* y) {
+    if (x != anc_.xh)
+        CU(cudaMemcpyAsync(anc_.xh, x, sizeof(double) * n, cudaMemcpyDeviceToDevice, st_));
+    if (y != anc_.yh)
+        CU(cudaMemcpyAsync(anc_.yh, y, sizeof(double) * m, cudaMemcpyDeviceToDevice, st_));
+    anchor_data();
+}
+
+void Engine::solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x, double* y) {
+    t0_ = std::chrono::steady_clock::now();
+    attempt_ms_ = 0;
+    launches_ = 0;
+    CU(cudaEventRecord(ev_[0], st_));
+    ensure_work<float>();
+    ensure_anchor();
+    LoopOpts lo;
+    lo.tol = o.tolerance;
+    const bool finite_tl = o.time_limit_s > 0 && o.time_limit_s < 1e6;
+    lo.deadline = o.time_limit_s;
+    lo.maxit = finite_tl ? 20000000LL : (long long)o.max_iterations;
+    lo.check = o.check_period > 0 ? o.check_period : 64;
+    lo.verbosity = o.verbosity;
+    lo.graphs = o.use_graphs != 0;
+    lo.eta_init = eta0;
+    lo.eta0 = eta0;
+    lo.omega_init = omega0;
+    LoopOut out = loop<float>(av_, lo);
+    // the answer: incumbent, or anchor + delta of the current / averaged iterate
+    const double *fx, *fy;
+    if (out.use_inc) {
+        fx = anc_.xb;
+        fy = anc_.yb;
+    } else {
+        anchor_full(out.parity);
+        fx = anc_.xf[out.last_is_avg ? 1 : 0];
+        fy = anc_.yf[out.last_is_avg ? 1 : 0];
+    }
+    std::vector<double> hx(n), hy(m);
+    CU(cudaMemcpyAsync(hx.data(), fx, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(hy.data(), fy, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
+    CU(cudaEventRecord(ev_[1], st_));
+    CU(cudaEventSynchronize(ev_[1]));
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, ev_[0], ev_[1]));
+    r.device_time_ms = ms;
+    r.attempt_time_ms = attempt_ms_;
+    r.launches = launches_;
+    r.solve_time_ms = elapsed() * 1000.0;
+    r.status = out.status;
+    r.objective = out.last.op + obj_const;
+    r.pinf = out.last.pinf;
+    r.dinf = out.last.dinf;
+    r.rel_gap = out.last.gap;
+    r.prow = out.last.prow;
+    r.iterations = out.iters;
+    r.attempts = out.attempts;
+    r.kkt_checks = out.checks;
+    r.restarts = out.restarts;
+    r.kkt_passes = out.spmvs / 2;
+    r.refinements = (int)out.anchors;
+    if (out.numeric_failure) {
+        r.error_code = IGAOS_PDHG_ERR_NUMERIC;
+        fill_message(r, "numerical failure: NaN/Inf in the PDHG iterates");
+    } else if (out.status == IGAOS_STATUS_NEAR_OPTIMAL) {
+        fill_message(r, "converged: residuals + duality gap @tol (FP32 iterates, FP64 refinement)");
+    } else if (out.status == IGAOS_STATUS_TIME_LIMIT) {
+        fill_message(r, "wall-clock budget exhausted");
+    } else {
+        fill_message(r, "iteration cap reached before tolerance");
+    }
+    if (x)
+        for (int j = 0; j < n; ++j) x[pc_[j]] = hx[j] * hp_dc_[j];
+    if (y)
+        for (int i = 0; i < m; ++i) y[pr_[i]] = 1.0 * hy[i] / hp_dr_[i];
 }
 }  // namespace igx

@@ -61,6 +61,17 @@ struct Vecs {
     double *sc, *scl, *scu, *srmin, *srmax; // scaled FP64
     float *fc, *fcl, *fcu, *frmin, *frmax;  // scaled FP32
     double cmax;
+    float* fyhat = nullptr;                 // anchored FP32 iterations: rounded y anchor
+};
+
+// FP64 anchor state of the FP32 + FP64-refinement mode (scaled units):
+// iterates are x = xh + dx, y = yh + dy with FP32 deltas in Work<float>.
+struct Anchor {
+    double *xh, *yh;       // anchor
+    double *xf[2], *yf[2]; // full current / averaged iterate at a check
+    double *xb, *yb;       // incumbent
+    double *pesx, *pesy;   // previous epoch start (= previous anchor)
+    double *aty, *ax;      // A~^T yh, A~ xh
 };
 
 template <typename T>
@@ -94,7 +105,7 @@ struct LoopOut {
     int status = IGAOS_STATUS_ERROR;
     DevMetrics last{};
     bool last_is_avg = false, use_inc = false;
-    long long iters = 0, attempts = 0, checks = 0, restarts = 0, spmvs = 0;
+    long long iters = 0, attempts = 0, checks = 0, restarts = 0, spmvs = 0, anchors = 0;
     double eta = 0, omega = 0;
     int parity = 0;
     bool numeric_failure = false;
@@ -180,6 +191,15 @@ class Engine {
     template <typename T> LoopOut loop(const Vecs& v, const LoopOpts& o);
     template <typename T> void fetch_scaled(const T* src, int len, double* dst);
     template <typename T> void unscale_cols(const T* xs, const Vecs& v, double* host_out);
+    // anchored (FP32 + FP64 refinement) iterations
+    Anchor anc_{};
+    Vecs av_{};
+    bool have_anchor_ = false;
+    void ensure_anchor();
+    void anchor_data();                                // av_ from (xh, yh)
+    void anchor_zero(int p);                           // deltas of slot p := 0
+    void anchor_full(int p);                           // xf/yf := anchor + deltas
+    void anchor_to(const double* x, const double* y);  // new anchor + its data
     void upload_ctl();
     void download_ctl();
     double elapsed() const;

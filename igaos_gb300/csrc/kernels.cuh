@@ -123,27 +123,34 @@ struct DualArgs {
     T* yavg[2];
     Acc<T>* part;           // per-CTA (||dy||^2, dy'A dx)
     const Acc<T>* part_primal;
+    const T* yhat;          // anchor of anchored iterations (rounded), or nullptr
     const double* fac;      // (1 - k^-0.3, 1 + k^-0.6) for k = ctl->fac_base + i
     int n_fac;
     int n_primal;
     DevCtl* ctl;
 };
 
+// Anchored iterations (FP32 + FP64 refinement) hold y = yhat + dy with an
+// FP64 anchor yhat; the dual projection must act on the full value, so the
+// clamp argument is (t + yhat)/sigma with t = dy + sigma A dxbar and the row
+// bounds shifted by the anchor's activity. yhat == nullptr: plain iterates.
 template <typename T>
 struct DualEpi {
-    const T *rmin, *rmax, *yc, *axc, *ya;
+    const T *rmin, *rmax, *yc, *axc, *ya, *yhat;
     T *yn_out, *axc_out, *ya_out;
     T sigma, w, dy2, cross;
     struct Pre {
-        T lo, hi, y, ax, ya;
+        T lo, hi, y, ax, ya, yh;
     };
     __device__ __forceinline__ Pre load(int i) const {
-        return Pre{__ldg(rmin + i), __ldg(rmax + i), yc[i], axc[i], ya[i]};
+        return Pre{__ldg(rmin + i), __ldg(rmax + i), yc[i], axc[i], ya[i],
+                   yhat ? __ldg(yhat + i) : T(0)};
     }
     __device__ __forceinline__ void apply(int i, const Acc<T>& acc, const Pre& v) {
         const T ab = acc.result();
         const T t = fma(sigma, ab, v.y);
-        const T yn = fma(-sigma, fmin(fmax(t / sigma, v.lo), v.hi), t);
+        const T arg = yhat ? (t + v.yh) / sigma : t / sigma;
+        const T yn = fma(-sigma, fmin(fmax(arg, v.lo), v.hi), t);
         yn_out[i] = yn;
         const T dy = yn - v.y;
         const T adx = (T)0.5 * (ab - v.ax);
@@ -211,7 +218,7 @@ __global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_dual(DualArgs<T> a)
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
     const int p = cv.parity, q = p ^ 1;
-    DualEpi<T> epi{a.rmin, a.rmax, a.y[p], a.axc[p], a.yavg[p], a.y[q], a.axc[q], a.yavg[q],
+    DualEpi<T> epi{a.rmin, a.rmax, a.y[p], a.axc[p], a.yavg[p], a.yhat, a.y[q], a.axc[q], a.yavg[q],
                    cv.sigma, cv.w, (T)0, (T)0};
     warp_rows_all<T>(a.ws, a.A, a.xbar, epi);
     T v[2] = {epi.dy2, epi.cross};
@@ -577,6 +584,54 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rowdual(KktArgs<T> a, int m) {
             o.err = smax(o.pinf, smax(o.dinf, g));
         }
     }
+}
+
+// ------------------------------------------------------ anchored iterations
+// The LP seen from an FP64 anchor (x^, y^) in scaled units, rounded to FP32
+// for the FP32 iteration on the deltas (x = x^ + dx, y = y^ + dy):
+//   columns: c' = c~ + A~^T y^ (the reduced cost at the anchor),
+//            l' = l~ - x^, u' = u~ - x^;
+//   rows:    [rmin~, rmax~] - A~ x^, and y^ itself for the dual projection.
+// Each value is formed in FP64 and rounded once, so it carries FP32 relative
+// error of the residual, not of the original data.
+__global__ void k_anchor_cols(int n, const double* __restrict__ sc, const double* __restrict__ scl,
+                              const double* __restrict__ scu, const double* __restrict__ aty,
+                              const double* __restrict__ xh, float* __restrict__ fc,
+                              float* __restrict__ fcl, float* __restrict__ fcu) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        fc[j] = (float)(sc[j] + aty[j]);
+        fcl[j] = (float)(scl[j] - xh[j]);
+        fcu[j] = (float)(scu[j] - xh[j]);
+    }
+}
+
+__global__ void k_anchor_rows(int m, const double* __restrict__ srmin,
+                              const double* __restrict__ srmax, const double* __restrict__ ax,
+                              const double* __restrict__ yh, float* __restrict__ frmin,
+                              float* __restrict__ frmax, float* __restrict__ yh32) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        frmin[i] = (float)(srmin[i] - ax[i]);
+        frmax[i] = (float)(srmax[i] - ax[i]);
+        yh32[i] = (float)yh[i];
+    }
+}
+
+// Full FP64 iterate anchor + delta. A primal delta sitting on its FP32
+// shifted bound is exactly at the bound (the same rule as unscale_x).
+__global__ void k_anchor_full_cols(int n, const double* __restrict__ xh, const float* __restrict__ dx,
+                                   const float* __restrict__ flo, const float* __restrict__ fhi,
+                                   const double* __restrict__ scl, const double* __restrict__ scu,
+                                   double* __restrict__ out) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const float d = dx[j];
+        out[j] = d == flo[j] ? scl[j] : (d == fhi[j] ? scu[j] : xh[j] + (double)d);
+    }
+}
+
+__global__ void k_anchor_full_rows(int m, const double* __restrict__ yh, const float* __restrict__ dy,
+                                   double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x)
+        out[i] = yh[i] + (double)dy[i];
 }
 
 }  // namespace igx

@@ -119,6 +119,30 @@ def test_fp32_reaches_its_tolerance(native):
     assert rel(r["objective"], ref) <= 1e-3
 
 
+@pytest.mark.parametrize("name", CONVERGING)
+def test_fp32_refine_matches_simplex(native, name):
+    """FP32 attempts with FP64 anchors reach the FP64 bar: 1e-8 relative KKT
+    and the reference simplex optimum to 1e-6."""
+    from igaos_gb300 import capi
+    lp, ref = make(name)
+    r = capi.solve_lp(lp, tolerance=1e-8, time_limit=60.0, precision="fp32-refine")
+    assert r["status_name"] == "near-optimal", r["message"]
+    assert rel(r["objective"], ref) <= 1e-6, (r["objective"], ref)
+    assert r["refinements"] >= 1
+
+
+def test_fp32_refine_vectors_certify(native, orc):
+    from igaos_gb300 import capi
+    lp, ref = make("mixed80x200-s2")
+    r = capi.solve_lp(lp, tolerance=1e-8, time_limit=60.0, precision="fp32-refine")
+    olp = orc.lp_from(lp)
+    Ax = orc.spmv(olp.ap, olp.ai, olp.ax, r["x"])
+    d = lp.c + orc.spmv(olp.cp, olp.ci, olp.acx, r["y"])
+    m = orc.evaluate(olp, r["x"], r["y"], Ax, d)
+    assert max(m["pinf"], m["prow"], m["dinf"], m["gap"]) <= 1e-8
+    assert rel(m["op"] + lp.obj_const, ref) <= 1e-6
+
+
 def test_iteration_limit_and_time_limit(native):
     from igaos_gb300 import capi
     lp, _ = make("rand200x500-s0")
