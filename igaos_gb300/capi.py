@@ -54,6 +54,15 @@ class Result(C.Structure):
         return d
 
 
+class BatchResult(C.Structure):
+    _fields_ = [
+        ("status", C.c_int), ("pad", C.c_int), ("objective", C.c_double),
+        ("pinf", C.c_double), ("dinf", C.c_double), ("rel_gap", C.c_double),
+        ("prow", C.c_double), ("iterations", C.c_int64), ("attempts", C.c_int64),
+        ("restarts", C.c_int64), ("kernel_time_ms", C.c_double), ("total_time_ms", C.c_double),
+    ]
+
+
 _LIB = None
 
 
@@ -82,6 +91,9 @@ def lib():
         L.igaos_pdhg_iterate.argtypes = [C.c_void_p, C.c_int, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]
         L.igaos_pdhg_evaluate.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.igaos_pdhg_spmv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp]
+        L.igaos_pdhg_solve_batch.argtypes = [
+            C.c_int, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(Options),
+            C.POINTER(BatchResult), _dp, _dp]
         # device-pointer entry point: every pointer is passed as an address
         L.igaos_pdhg_evaluate_noalloc.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 15
         _LIB = L
@@ -242,3 +254,38 @@ def solve_lp(lp, **opts):
     d["rc"] = rc
     d["x"], d["y"] = x, y
     return d
+
+
+def solve_batch(lps, want_solutions=True, **opts):
+    """Solves a list of LPs (objects with m, n, ap, ai, ax, c, cl, cu, rmin,
+    rmax) in one persistent launch (igaos_pdhg_solve_batch). Returns a list
+    of per-instance dicts (status_name, objective, iterations, ... and x, y
+    when requested)."""
+    count = len(lps)
+    i32 = lambda a: np.ascontiguousarray(a, dtype=np.int32)
+    f64 = lambda a: np.ascontiguousarray(a, dtype=np.float64)
+    m = i32([lp.m for lp in lps])
+    n = i32([lp.n for lp in lps])
+    cat = lambda k, f: f(np.concatenate([np.asarray(getattr(lp, k)) for lp in lps]))
+    ap, ai, ax = cat("ap", i32), cat("ai", i32), cat("ax", f64)
+    c, cl, cu, rmin, rmax = (cat(k, f64) for k in ("c", "cl", "cu", "rmin", "rmax"))
+    res = (BatchResult * count)()
+    x = np.zeros(int(n.sum())) if want_solutions else None
+    y = np.zeros(int(m.sum())) if want_solutions else None
+    o = default_options(**opts)
+    rc = lib().igaos_pdhg_solve_batch(count, _i(m), _i(n), _i(ap), _i(ai), _d(ax), _d(c), _d(cl),
+                                      _d(cu), _d(rmin), _d(rmax), C.byref(o), res, _d(x), _d(y))
+    _check(rc)
+    out = []
+    co = ro = 0
+    for b in range(count):
+        r = res[b]
+        d = {f: getattr(r, f) for f, _ in BatchResult._fields_ if f != "pad"}
+        d["status_name"] = STATUS_NAMES[r.status] if 0 <= r.status < 8 else "?"
+        if want_solutions:
+            d["x"] = x[co:co + lps[b].n]
+            d["y"] = y[ro:ro + lps[b].m]
+        co += lps[b].n
+        ro += lps[b].m
+        out.append(d)
+    return out

@@ -1,0 +1,807 @@
+// Batched PDHG: thousands of independent LPs of uneven sizes solved in one
+// persistent launch (igaos_pdhg_solve_batch).
+//
+// Each CTA takes instances from a work queue (largest first, an atomic
+// counter; no CTA waits on another) and runs one LP to the end on its own:
+// deterministic CSC build, Ruiz equilibration (src/pdhg/pdhg.cu:472-492),
+// power iteration (:605-631), and the reference iteration -- adaptive line
+// search (:751-794), averaging (:795-799), KKT checks every `check`
+// iterations with the termination test (:835-840), restarts and the
+// primal-weight update (:1001-1075) -- with per-instance restart and
+// termination. Iterates and matrices are FP32 with compensated row sums; the
+// termination metrics are accumulated with compensated FP32 sums and combined
+// in FP64. Incumbent/rollback and dual repair are not part of this path.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <numeric>
+#include <vector>
+
+#include "device.cuh"
+#include "engine.hpp"
+
+namespace igx {
+namespace {
+
+struct BatchDesc {
+    int m, n, nnz, pad;
+    long long ap_off, cp_off, nz_off, row_off, col_off;
+};
+
+struct BatchOut {
+    int status, pad;
+    double objective, pinf, dinf, gap, prow;
+    long long iterations, attempts, restarts;
+};
+
+constexpr int kFacTab = 1 << 16;  // tabulated 1 - k^-0.3, 1 + k^-0.6
+
+struct BatchArgs {
+    int count;
+    const int* order;
+    unsigned int* queue;
+    const BatchDesc* desc;
+    const int *ap, *ai;
+    const float* ax;
+    const double *c, *cl, *cu, *rmin, *rmax;
+    int *cp, *ci, *cnt;
+    float *cax, *sax, *scax;
+    float *dr, *dc, *sc, *scl, *scu, *srmin, *srmax;
+    float *x[2], *xa[2], *xbar, *pesx, *vt;
+    float *y[2], *ya[2], *axc[2], *pesy, *mt;
+    const float* fac;
+    double tol;
+    long long maxit;
+    int check;
+    double* x_out;
+    double* y_out;
+    BatchOut* out;
+};
+
+struct BatchShared {
+    Acc<float> acc[kWarps * 4];
+    float fmax_[kWarps * 8];
+    int part[kThreads];
+    int inst;
+    // line search / restart state (thread 0 writes, all read)
+    float tau, sigma, w;
+    int parity, accept;
+    long long kdone;
+};
+
+// ---- block-level helpers (all 256 threads call them) --------------------
+template <int NV>
+__device__ void bmerge(BatchShared& sh, Acc<float> (&v)[NV]) {
+    block_merge<float, NV>(v, sh.acc);
+}
+
+template <int NV>
+__device__ void bmaxf(BatchShared& sh, float (&v)[NV]) {
+    const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+        for (int o = 16; o > 0; o >>= 1) v[q] = fmaxf(v[q], __shfl_xor_sync(0xffffffffu, v[q], o));
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh.fmax_[wp * NV + q] = v[q];
+    __syncthreads();
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            float s = sh.fmax_[q];
+            for (int k = 1; k < kWarps; ++k) s = fmaxf(s, sh.fmax_[k * NV + q]);
+            v[q] = s;
+        }
+    __syncthreads();
+}
+
+// exclusive block scan of cnt[0..len) into out[0..len], out[len] = total
+__device__ void bscan(BatchShared& sh, const int* cnt, int* out, int len) {
+    const int t = threadIdx.x;
+    const int per = (len + kThreads - 1) / kThreads;
+    const int b = min(len, t * per), e = min(len, b + per);
+    int s = 0;
+    for (int j = b; j < e; ++j) s += cnt[j];
+    sh.part[t] = s;
+    __syncthreads();
+    if (t == 0) {
+        int run = 0;
+        for (int k = 0; k < kThreads; ++k) {
+            const int v = sh.part[k];
+            sh.part[k] = run;
+            run += v;
+        }
+        out[len] = run;
+    }
+    __syncthreads();
+    int run = sh.part[t];
+    for (int j = b; j < e; ++j) {
+        out[j] = run;
+        run += cnt[j];
+    }
+    __syncthreads();
+}
+
+struct Inst {
+    int m, n;
+    const int *ap, *ai;
+    const float* ax;
+    const double *c, *cl, *cu, *rmin, *rmax;
+    int *cp, *ci, *cnt;
+    float *cax, *sax, *scax;
+    float *dr, *dc, *sc, *scl, *scu, *srmin, *srmax;
+    float *x[2], *xa[2], *xbar, *pesx, *vt;
+    float *y[2], *ya[2], *axc[2], *pesy, *mt;
+};
+
+__device__ Inst make_inst(const BatchArgs& a, const BatchDesc& d) {
+    Inst I;
+    I.m = d.m;
+    I.n = d.n;
+    I.ap = a.ap + d.ap_off;
+    I.ai = a.ai + d.nz_off;
+    I.ax = a.ax + d.nz_off;
+    I.c = a.c + d.col_off;
+    I.cl = a.cl + d.col_off;
+    I.cu = a.cu + d.col_off;
+    I.rmin = a.rmin + d.row_off;
+    I.rmax = a.rmax + d.row_off;
+    I.cp = a.cp + d.cp_off;
+    I.ci = a.ci + d.nz_off;
+    I.cnt = a.cnt + d.col_off;
+    I.cax = a.cax + d.nz_off;
+    I.sax = a.sax + d.nz_off;
+    I.scax = a.scax + d.nz_off;
+    I.dr = a.dr + d.row_off;
+    I.srmin = a.srmin + d.row_off;
+    I.srmax = a.srmax + d.row_off;
+    I.dc = a.dc + d.col_off;
+    I.sc = a.sc + d.col_off;
+    I.scl = a.scl + d.col_off;
+    I.scu = a.scu + d.col_off;
+    for (int s = 0; s < 2; ++s) {
+        I.x[s] = a.x[s] + d.col_off;
+        I.xa[s] = a.xa[s] + d.col_off;
+        I.y[s] = a.y[s] + d.row_off;
+        I.ya[s] = a.ya[s] + d.row_off;
+        I.axc[s] = a.axc[s] + d.row_off;
+    }
+    I.xbar = a.xbar + d.col_off;
+    I.pesx = a.pesx + d.col_off;
+    I.vt = a.vt + d.col_off;
+    I.pesy = a.pesy + d.row_off;
+    I.mt = a.mt + d.row_off;
+    return I;
+}
+
+// y = M v over rows [0, rows) of a CSR (thread per row, compensated)
+__device__ __forceinline__ Acc<float> row_dot(const int* ptr, const int* idx, const float* val,
+                                              const float* v, int r) {
+    Acc<float> acc;
+    for (int p = ptr[r]; p < ptr[r + 1]; ++p) acc.add(val[p], v[idx[p]]);
+    return acc;
+}
+
+// ---- setup: CSC, Ruiz, scaled data, power iteration ----------------------
+__device__ void setup(BatchShared& sh, Inst& I, float& eta0, float& omega0) {
+    const int t = threadIdx.x, m = I.m, n = I.n;
+    // CSC by counting sort; each column's entries ordered by row afterwards
+    for (int j = t; j < n; j += kThreads) I.cnt[j] = 0;
+    __syncthreads();
+    for (int i = t; i < m; i += kThreads)
+        for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) atomicAdd(&I.cnt[I.ai[p]], 1);
+    __syncthreads();
+    bscan(sh, I.cnt, I.cp, n);
+    for (int j = t; j < n; j += kThreads) I.cnt[j] = I.cp[j];
+    __syncthreads();
+    for (int i = t; i < m; i += kThreads)
+        for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) {
+            const int q = atomicAdd(&I.cnt[I.ai[p]], 1);
+            I.ci[q] = i;
+            I.cax[q] = I.ax[p];
+        }
+    __syncthreads();
+    for (int j = t; j < n; j += kThreads) {  // insertion sort by row index
+        const int b = I.cp[j], e = I.cp[j + 1];
+        for (int q = b + 1; q < e; ++q) {
+            const int r = I.ci[q];
+            const float v = I.cax[q];
+            int k = q - 1;
+            while (k >= b && I.ci[k] > r) {
+                I.ci[k + 1] = I.ci[k];
+                I.cax[k + 1] = I.cax[k];
+                --k;
+            }
+            I.ci[k + 1] = r;
+            I.cax[k + 1] = v;
+        }
+    }
+    // Ruiz, 10 sweeps (FP32)
+    for (int i = t; i < m; i += kThreads) I.dr[i] = 1.f;
+    for (int j = t; j < n; j += kThreads) I.dc[j] = 1.f;
+    __syncthreads();
+    for (int sweep = 0; sweep < 10; ++sweep) {
+        for (int i = t; i < m; i += kThreads) {
+            float mx = 0.f;
+            for (int p = I.ap[i]; p < I.ap[i + 1]; ++p)
+                mx = fmaxf(mx, fabsf(I.ax[p]) * I.dc[I.ai[p]] / I.dr[i]);
+            if (mx > 0.f && isfinite(mx)) I.dr[i] *= sqrtf(mx);
+        }
+        __syncthreads();
+        for (int j = t; j < n; j += kThreads) {
+            float mx = 0.f;
+            for (int p = I.cp[j]; p < I.cp[j + 1]; ++p)
+                mx = fmaxf(mx, fabsf(I.cax[p]) / I.dr[I.ci[p]] * I.dc[j]);
+            if (mx > 0.f && isfinite(mx)) I.dc[j] /= sqrtf(mx);
+        }
+        __syncthreads();
+    }
+    // scaled problem
+    Acc<float> nq[2];
+    for (int i = t; i < m; i += kThreads) {
+        for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) I.sax[p] = I.ax[p] * I.dc[I.ai[p]] / I.dr[i];
+        const float lo = (float)I.rmin[i] / I.dr[i], hi = (float)I.rmax[i] / I.dr[i];
+        I.srmin[i] = lo;
+        I.srmax[i] = hi;
+        const float q = isfinite(hi) ? hi : (isfinite(lo) ? lo : 0.f);
+        nq[1].add(q, q);
+    }
+    for (int j = t; j < n; j += kThreads) {
+        for (int p = I.cp[j]; p < I.cp[j + 1]; ++p) I.scax[p] = I.cax[p] * I.dc[j] / I.dr[I.ci[p]];
+        const float cs = (float)I.c[j] * I.dc[j];
+        I.sc[j] = cs;
+        I.scl[j] = (float)I.cl[j] / I.dc[j];
+        I.scu[j] = (float)I.cu[j] / I.dc[j];
+        nq[0].add(cs, cs);
+    }
+    bmerge<2>(sh, nq);
+    if (t == 0) {
+        const double cn = nq[0].result_d(), qn = nq[1].result_d();
+        omega0 = (cn > 1e-24 && qn > 1e-24) ? fminf(3.f, fmaxf(0.3f, (float)sqrt(cn / qn))) : 1.f;
+    }
+    // power iteration for ||A~||_2^2
+    const float v0 = rsqrtf((float)n);
+    for (int j = t; j < n; j += kThreads) I.vt[j] = v0;
+    __syncthreads();
+    __shared__ float s_norm;
+    for (int it = 0; it < 31; ++it) {
+        for (int i = t; i < m; i += kThreads) I.mt[i] = row_dot(I.ap, I.ai, I.sax, I.vt, i).result();
+        __syncthreads();
+        if (it == 30) break;
+        Acc<float> nrm[1];
+        for (int j = t; j < n; j += kThreads) {
+            const float wv = row_dot(I.cp, I.ci, I.scax, I.mt, j).result();
+            I.xbar[j] = wv;
+            nrm[0].add(wv, wv);
+        }
+        bmerge<1>(sh, nrm);
+        if (t == 0) s_norm = sqrtf((float)nrm[0].result_d());
+        __syncthreads();
+        const float nw = s_norm;
+        if (!(nw > 1e-30f)) break;
+        for (int j = t; j < n; j += kThreads) I.vt[j] = I.xbar[j] / nw;
+        __syncthreads();
+    }
+    Acc<float> na[1];
+    for (int i = t; i < m; i += kThreads) na[0].add(I.mt[i], I.mt[i]);
+    bmerge<1>(sh, na);
+    if (t == 0) {
+        double lam = na[0].result_d();
+        if (!(lam > 0) || !isfinite(lam)) lam = 1.0;
+        eta0 = (float)(1.2 / sqrt(lam));
+    }
+    __syncthreads();
+}
+
+// ---- FP64-combined metrics of one candidate (original units) -------------
+struct BMetrics {
+    double pinf, dinf, gap, op, od, prow, err;
+    bool finite;
+};
+
+__device__ BMetrics metrics(BatchShared& sh, Inst& I, const float* xs, const float* ys,
+                            float cmax) {
+    const int t = threadIdx.x;
+    // rows: A x, ymax
+    float fr[4] = {0.f, 0.f, 0.f, 0.f};  // pv, pa, prow, ymax
+    for (int i = t; i < I.m; i += kThreads) {
+        const float Ax = (float)(row_dot(I.ap, I.ai, I.sax, xs, i).result_d() * (double)I.dr[i]);
+        const float lo = (float)I.rmin[i], hi = (float)I.rmax[i];
+        const float vi = fmaxf(lo - Ax, Ax - hi);
+        fr[0] = fmaxf(fr[0], vi);
+        fr[1] = fmaxf(fr[1], fabsf(fminf(fmaxf(Ax, lo), hi)));
+        float scv = fabsf(Ax);
+        if (isfinite(lo)) scv = fmaxf(scv, fabsf(lo));
+        if (isfinite(hi)) scv = fmaxf(scv, fabsf(hi));
+        fr[2] = fmaxf(fr[2], fmaxf(0.f, vi) / (1.f + scv));
+        fr[3] = fmaxf(fr[3], fabsf(ys[i] / I.dr[i]));
+    }
+    bmaxf<4>(sh, fr);
+    __shared__ float s_r[4];
+    if (t == 0)
+        for (int q = 0; q < 4; ++q) s_r[q] = fr[q];
+    __syncthreads();
+    const float yz = 1e-8f * (1.f + s_r[3]);
+    const float dz = 1e-8f * (1.f + cmax);
+    // columns: reduced costs, dinf, c'x, column part of the bound
+    float fc[2] = {0.f, 0.f};  // dv, unbounded
+    Acc<float> sums[3];        // op, od (columns), od (rows)
+    for (int j = t; j < I.n; j += kThreads) {
+        const float d = (float)I.c[j] + (float)(row_dot(I.cp, I.ci, I.scax, ys, j).result_d() / I.dc[j]);
+        const float xv = xs[j];
+        const float lo = (float)I.cl[j], hi = (float)I.cu[j];
+        const float x = xv == I.scl[j] ? lo : (xv == I.scu[j] ? hi : xv * I.dc[j]);
+        const float bnd = fabsf(isfinite(hi) ? hi : lo);
+        const float tol = 1e-9f * (1.f + bnd);
+        float e;
+        if (x <= lo + tol && d > 0) e = 0.f;
+        else if (x >= hi - tol && d < 0) e = 0.f;
+        else e = fabsf(d);
+        fc[0] = fmaxf(fc[0], e);
+        sums[0].add((float)I.c[j], x);
+        if (d >= 0) {
+            if (isfinite(lo)) sums[1].add(d, lo);
+            else if (d > dz) fc[1] = 1.f;
+        } else {
+            if (isfinite(hi)) sums[1].add(d, hi);
+            else if (-d > dz) fc[1] = 1.f;
+        }
+    }
+    for (int i = t; i < I.m; i += kThreads) {
+        const float yv = ys[i] / I.dr[i];
+        if (yv > yz) {
+            if (isfinite((float)I.rmax[i])) sums[2].add(-yv, (float)I.rmax[i]);
+            else fc[1] = 1.f;
+        } else if (yv < -yz) {
+            if (isfinite((float)I.rmin[i])) sums[2].add(-yv, (float)I.rmin[i]);
+            else fc[1] = 1.f;
+        }
+    }
+    bmaxf<2>(sh, fc);
+    bmerge<3>(sh, sums);
+    __shared__ BMetrics s_m;
+    if (t == 0) {
+        BMetrics mt;
+        mt.pinf = fmax((double)s_r[0], 0.0) / (1.0 + (double)s_r[1]);
+        mt.prow = s_r[2];
+        mt.dinf = (double)fc[0] / (1.0 + (double)cmax);
+        mt.op = sums[0].result_d();
+        const bool bounded = !(fc[1] > 0.f);
+        mt.od = bounded ? sums[1].result_d() + sums[2].result_d() : -CUDART_INF;
+        mt.gap = bounded ? fmax(0.0, mt.op - mt.od) / (1.0 + fabs(mt.op)) : CUDART_INF;
+        mt.finite = isfinite(mt.pinf) && isfinite(mt.dinf);
+        mt.err = fmax(mt.pinf, fmax(mt.dinf, isfinite(mt.gap) ? mt.gap : 0.0));
+        s_m = mt;
+    }
+    __syncthreads();
+    return s_m;
+}
+
+// ---- one LP --------------------------------------------------------------
+__device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& d, int b) {
+    Inst I = make_inst(a, d);
+    const int t = threadIdx.x, m = I.m, n = I.n;
+    __shared__ float s_eta0, s_omega0, s_cmax;
+    setup(sh, I, s_eta0, s_omega0);
+    {
+        float cm[1] = {0.f};
+        for (int j = t; j < n; j += kThreads) cm[0] = fmaxf(cm[0], fabsf((float)I.c[j]));
+        bmaxf<1>(sh, cm);
+        if (t == 0) s_cmax = cm[0];
+    }
+    for (int j = t; j < n; j += kThreads) I.x[0][j] = I.xa[0][j] = 0.f;
+    for (int i = t; i < m; i += kThreads) I.y[0][i] = I.ya[0][i] = I.axc[0][i] = 0.f;
+    // controller state (thread 0)
+    __shared__ double s_epoch_kkt, s_prev_cand, s_omega, s_eta;
+    __shared__ long long s_k, s_hn, s_epoch_start, s_attempts, s_restarts;
+    __shared__ int s_retries, s_have_pe, s_done, s_status, s_use_avg, s_restart, s_avg_better;
+    __shared__ BMetrics s_last;
+    if (t == 0) {
+        s_eta = s_eta0;
+        s_omega = s_omega0;
+        s_k = 1;
+        s_hn = 0;
+        s_epoch_kkt = -1.0;
+        s_prev_cand = CUDART_INF;
+        s_epoch_start = 0;
+        s_attempts = 0;
+        s_restarts = 0;
+        s_retries = 0;
+        s_have_pe = 0;
+        s_done = 0;
+        s_status = IGAOS_STATUS_ITERATION_LIMIT;
+        s_use_avg = 0;
+        sh.parity = 0;
+        s_last.pinf = s_last.dinf = CUDART_INF;
+        s_last.gap = CUDART_INF;
+        s_last.op = 0.0;
+        s_last.prow = CUDART_INF;
+    }
+    __syncthreads();
+    const long long maxit = a.maxit;
+    while (!s_done) {
+        if (t == 0) {
+            sh.tau = (float)(s_eta / s_omega);
+            sh.sigma = (float)(s_eta * s_omega);
+            sh.w = (float)(2.0 / ((double)s_hn + 2.0));
+        }
+        __syncthreads();
+        const int p = sh.parity, q = p ^ 1;
+        const float tau = sh.tau, sigma = sh.sigma, w = sh.w;
+        Acc<float> dots[3];
+        // primal step fused with A^T y (thread per column)
+        for (int j = t; j < n; j += kThreads) {
+            const float g = I.sc[j] + row_dot(I.cp, I.ci, I.scax, I.y[p], j).result();
+            const float xv = I.x[p][j];
+            const float xn = fminf(fmaxf(fmaf(-tau, g, xv), I.scl[j]), I.scu[j]);
+            I.x[q][j] = xn;
+            I.xbar[j] = fmaf(2.f, xn, -xv);
+            const float dx = xn - xv;
+            dots[0].add(dx, dx);
+            const float av = I.xa[p][j];
+            I.xa[q][j] = fmaf(w, xn - av, av);
+        }
+        __syncthreads();
+        // dual step fused with A xbar (thread per row)
+        for (int i = t; i < m; i += kThreads) {
+            const float ab = row_dot(I.ap, I.ai, I.sax, I.xbar, i).result();
+            const float yv = I.y[p][i];
+            const float tt = fmaf(sigma, ab, yv);
+            const float yn = fmaf(-sigma, fminf(fmaxf(tt / sigma, I.srmin[i]), I.srmax[i]), tt);
+            I.y[q][i] = yn;
+            const float dy = yn - yv;
+            const float ax = I.axc[p][i];
+            const float adx = 0.5f * (ab - ax);
+            I.axc[q][i] = ax + adx;
+            dots[1].add(dy, dy);
+            dots[2].add(dy, adx);
+            const float av = I.ya[p][i];
+            I.ya[q][i] = fmaf(w, yn - av, av);
+        }
+        bmerge<3>(sh, dots);
+        // step decision (src/pdhg/pdhg.cu:770-794)
+        if (t == 0) {
+            ++s_attempts;
+            const double dx2 = dots[0].result_d(), dy2 = dots[1].result_d(),
+                         cross = dots[2].result_d();
+            const double eta = s_eta, om = s_omega;
+            const double num = om * dx2 + dy2 / om;
+            const double etabar = (num > 0.0 && cross > 0.0) ? num / (2.0 * cross) : CUDART_INF;
+            const long long k = s_k;
+            const float flo = k < kFacTab ? a.fac[2 * k] : 1.f - powf((float)k, -0.3f);
+            const float fhi = k < kFacTab ? a.fac[2 * k + 1] : 1.f + powf((float)k, -0.6f);
+            const double eta_new =
+                isfinite(etabar) ? fmin((double)flo * etabar, (double)fhi * eta) : CUDART_INF;
+            bool acc_ = !(eta > etabar) || num <= 0.0 || cross <= 0.0;
+            if (!acc_) acc_ = ++s_retries > 20;
+            if (!isfinite(dx2) || !isfinite(dy2) || !isfinite(cross)) {
+                s_done = 1;
+                s_status = IGAOS_STATUS_ERROR;
+            }
+            if (acc_) {
+                if (isfinite(eta_new) && eta_new > 1e-12) s_eta = fmin(eta_new, 1e12);
+                sh.parity ^= 1;
+                ++s_hn;
+                s_retries = 0;
+                sh.kdone = s_k;  // index of the iteration just accepted
+                ++s_k;
+            } else {
+                s_eta = fmax(eta_new, 1e-12);
+            }
+            sh.accept = acc_;
+        }
+        __syncthreads();
+        if (!sh.accept || s_done) continue;
+        const long long k = sh.kdone;
+        const int pc = sh.parity;
+        if (k % a.check == 0 || k >= maxit) {
+            const BMetrics mc = metrics(sh, I, I.x[pc], I.y[pc], s_cmax);
+            const BMetrics ma = metrics(sh, I, I.xa[pc], I.ya[pc], s_cmax);
+            if (t == 0) {
+                auto passes = [&](const BMetrics& u) {
+                    return u.pinf <= a.tol && u.dinf <= a.tol && u.prow <= a.tol &&
+                           isfinite(u.gap) && u.gap <= a.tol;
+                };
+                const double ec = mc.finite ? mc.err : CUDART_INF;
+                const double ea = ma.finite ? ma.err : CUDART_INF;
+                s_last = (ec <= ea) ? mc : ma;
+                s_use_avg = ea < ec;
+                s_restart = 0;
+                if (passes(mc)) {
+                    s_last = mc;
+                    s_use_avg = 0;
+                    s_done = 1;
+                    s_status = IGAOS_STATUS_NEAR_OPTIMAL;
+                } else if (passes(ma)) {
+                    s_last = ma;
+                    s_use_avg = 1;
+                    s_done = 1;
+                    s_status = IGAOS_STATUS_NEAR_OPTIMAL;
+                } else if (k >= maxit) {
+                    s_done = 1;
+                } else {
+                    const double cand = fmin(ec, ea);
+                    if (s_epoch_kkt < 0.0) {
+                        s_epoch_kkt = cand;
+                        s_prev_cand = cand;
+                    }
+                    const long long te = k - s_epoch_start;
+                    s_restart = (isfinite(cand) && isfinite(s_epoch_kkt) && s_epoch_kkt > 0.0 &&
+                                 (cand <= 0.2 * s_epoch_kkt ||
+                                  (cand <= 0.8 * s_epoch_kkt && isfinite(s_prev_cand) &&
+                                   cand > s_prev_cand))) ||
+                                (double)te >= 0.36 * (double)k;
+                    s_prev_cand = cand;
+                    if (s_restart) {
+                        s_avg_better = ea < ec;
+                        s_hn = 0;
+                        s_epoch_start = k;
+                        s_epoch_kkt = cand;
+                        s_prev_cand = CUDART_INF;
+                        ++s_restarts;
+                    }
+                }
+            }
+            __syncthreads();
+            if (s_restart) {
+                const int r = pc;
+                if (s_avg_better) {
+                    for (int j = t; j < n; j += kThreads) I.x[r][j] = I.xa[r][j];
+                    for (int i = t; i < m; i += kThreads) I.y[r][i] = I.ya[r][i];
+                    __syncthreads();
+                }
+                Acc<float> dn[2];
+                for (int j = t; j < n; j += kThreads) {
+                    const float xv = I.x[r][j];
+                    I.xa[r][j] = xv;
+                    const float dd = xv - I.pesx[j];
+                    dn[0].add(dd, dd);
+                    I.pesx[j] = xv;
+                }
+                __syncthreads();
+                for (int i = t; i < m; i += kThreads) {
+                    const float yv = I.y[r][i];
+                    I.ya[r][i] = yv;
+                    const float dd = yv - I.pesy[i];
+                    dn[1].add(dd, dd);
+                    I.pesy[i] = yv;
+                    I.axc[r][i] = row_dot(I.ap, I.ai, I.sax, I.x[r], i).result();
+                }
+                bmerge<2>(sh, dn);
+                if (t == 0) {
+                    if (s_have_pe) {
+                        const double dxn = dn[0].result_d(), dyn = dn[1].result_d();
+                        if (dxn > 1e-24 && dyn > 1e-24) {
+                            const double om = sqrt(s_omega * sqrt(dyn / dxn));
+                            if (isfinite(om) && om > 0.0) s_omega = fmin(fmax(om, 1e-6), 1e6);
+                        }
+                    }
+                    s_have_pe = 1;
+                }
+                __syncthreads();
+            }
+        }
+    }
+    // answer: original units
+    const int pf = sh.parity;
+    const float* xs = s_use_avg ? I.xa[pf] : I.x[pf];
+    const float* ys = s_use_avg ? I.ya[pf] : I.y[pf];
+    double* xo = a.x_out ? a.x_out + d.col_off : nullptr;
+    double* yo = a.y_out ? a.y_out + d.row_off : nullptr;
+    if (xo)
+        for (int j = t; j < n; j += kThreads) {
+            const float xv = xs[j];
+            xo[j] = xv == I.scl[j] ? I.cl[j] : (xv == I.scu[j] ? I.cu[j] : (double)xv * I.dc[j]);
+        }
+    if (yo)
+        for (int i = t; i < m; i += kThreads) yo[i] = (double)ys[i] / (double)I.dr[i];
+    if (t == 0) {
+        BatchOut o;
+        o.status = s_status;
+        o.pad = 0;
+        o.objective = s_last.op;
+        o.pinf = s_last.pinf;
+        o.dinf = s_last.dinf;
+        o.gap = s_last.gap;
+        o.prow = s_last.prow;
+        o.iterations = s_k - 1;
+        o.attempts = s_attempts;
+        o.restarts = s_restarts;
+        a.out[b] = o;
+    }
+    __syncthreads();
+}
+
+__global__ void __launch_bounds__(kThreads) k_batch(BatchArgs a) {
+    __shared__ BatchShared sh;
+    for (;;) {
+        if (threadIdx.x == 0) sh.inst = (int)atomicAdd(a.queue, 1u);
+        __syncthreads();
+        const int qi = sh.inst;
+        __syncthreads();
+        if (qi >= a.count) break;
+        const int b = a.order[qi];
+        const BatchDesc d = a.desc[b];
+        if (d.m > 0 && d.n > 0) solve_one(a, sh, d, b);
+    }
+}
+
+__global__ void k_to_float(long long n, const double* __restrict__ in, float* __restrict__ out) {
+    for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+         i += (long long)gridDim.x * blockDim.x)
+        out[i] = (float)in[i];
+}
+
+}  // namespace
+}  // namespace igx
+
+// ---------------------------------------------------------------- C ABI
+extern "C" int igaos_pdhg_solve_batch(int count, const int* m, const int* n, const int* ap,
+                                      const int* ai, const double* ax, const double* c,
+                                      const double* cl, const double* cu, const double* rmin,
+                                      const double* rmax, const igaos_pdhg_options* opt,
+                                      igaos_pdhg_batch_result* res, double* x, double* y) {
+    using namespace igx;
+    if (count <= 0 || !m || !n || !ap || !ai || !ax || !c || !cl || !cu || !rmin || !rmax || !res)
+        return igx_set_error(IGAOS_PDHG_ERR_INVALID, "count must be positive and arrays non-NULL");
+    igaos_pdhg_options o;
+    if (opt) o = *opt;
+    else igaos_pdhg_default_options(&o);
+    if (!(o.tolerance > 0)) return igx_set_error(IGAOS_PDHG_ERR_INVALID, "tolerance must be positive");
+    try {
+        auto t_start = std::chrono::steady_clock::now();
+        // host descriptors, validation
+        std::vector<BatchDesc> desc(count);
+        long long ap_off = 0, nz = 0, rows = 0, cols = 0;
+        for (int b = 0; b < count; ++b) {
+            if (m[b] < 0 || n[b] < 0)
+                return igx_set_error(IGAOS_PDHG_ERR_INVALID, "negative instance size");
+            BatchDesc& d = desc[b];
+            d.m = m[b];
+            d.n = n[b];
+            const int* bap = ap + ap_off;
+            if (bap[0] != 0) return igx_set_error(IGAOS_PDHG_ERR_INVALID, "each instance's row pointer must start at 0");
+            for (int i = 0; i < d.m; ++i)
+                if (bap[i + 1] < bap[i])
+                    return igx_set_error(IGAOS_PDHG_ERR_INVALID, "row pointer must be non-decreasing");
+            d.nnz = bap[d.m];
+            for (int p = 0; p < d.nnz; ++p) {
+                const int j = ai[nz + p];
+                if (j < 0 || j >= d.n)
+                    return igx_set_error(IGAOS_PDHG_ERR_INVALID, "column index out of range");
+                if (!std::isfinite(ax[nz + p]))
+                    return igx_set_error(IGAOS_PDHG_ERR_INVALID, "matrix values must be finite");
+            }
+            d.ap_off = ap_off;
+            d.cp_off = cols + b;
+            d.nz_off = nz;
+            d.row_off = rows;
+            d.col_off = cols;
+            ap_off += d.m + 1;
+            nz += d.nnz;
+            rows += d.m;
+            cols += d.n;
+        }
+        for (long long j = 0; j < cols; ++j) {
+            if (!std::isfinite(c[j])) return igx_set_error(IGAOS_PDHG_ERR_INVALID, "cost must be finite");
+            if (std::isnan(cl[j]) || std::isnan(cu[j]) || cl[j] > cu[j])
+                return igx_set_error(IGAOS_PDHG_ERR_INVALID, "bad column bounds");
+        }
+        for (long long i = 0; i < rows; ++i)
+            if (std::isnan(rmin[i]) || std::isnan(rmax[i]) || rmin[i] > rmax[i])
+                return igx_set_error(IGAOS_PDHG_ERR_INVALID, "bad row bounds");
+        if (igaos_pdhg_device_count() == 0)
+            return igx_set_error(IGAOS_PDHG_ERR_NODEVICE, "no CUDA device: PDHG engine unavailable");
+        if (o.device >= 0) CU(cudaSetDevice(o.device));
+        // largest instances first
+        std::vector<int> order(count);
+        std::iota(order.begin(), order.end(), 0);
+        std::stable_sort(order.begin(), order.end(), [&](int p1, int p2) {
+            return (long long)desc[p1].nnz + desc[p1].m + desc[p1].n >
+                   (long long)desc[p2].nnz + desc[p2].m + desc[p2].n;
+        });
+        std::vector<float> fac(2 * kFacTab);
+        for (int k = 0; k < kFacTab; ++k) {
+            const double kk = k < 1 ? 1.0 : (double)k;
+            fac[2 * k] = (float)(1.0 - std::pow(kk, -0.3));
+            fac[2 * k + 1] = (float)(1.0 + std::pow(kk, -0.6));
+        }
+        cudaStream_t st;
+        CU(cudaStreamCreateWithFlags(&st, cudaStreamNonBlocking));
+        struct StreamGuard {
+            cudaStream_t s;
+            ~StreamGuard() { cudaStreamDestroy(s); }
+        } sg{st};
+        Arena ar;
+        auto up = [&](const auto* h, size_t len) {
+            using V = std::remove_const_t<std::remove_pointer_t<decltype(h)>>;
+            V* dp = ar.alloc<V>(len);
+            CU(cudaMemcpyAsync(dp, h, sizeof(V) * len, cudaMemcpyHostToDevice, st));
+            return dp;
+        };
+        BatchArgs A{};
+        A.count = count;
+        A.order = up(order.data(), order.size());
+        A.desc = up(desc.data(), desc.size());
+        A.queue = ar.alloc<unsigned int>(1);
+        CU(cudaMemsetAsync(A.queue, 0, sizeof(unsigned int), st));
+        A.ap = up(ap, (size_t)ap_off);
+        A.ai = up(ai, (size_t)nz);
+        double* axd = up(ax, (size_t)nz);
+        float* axf = ar.alloc<float>(nz);
+        k_to_float<<<1216, 256, 0, st>>>(nz, axd, axf);
+        A.ax = axf;
+        A.c = up(c, cols);
+        A.cl = up(cl, cols);
+        A.cu = up(cu, cols);
+        A.rmin = up(rmin, rows);
+        A.rmax = up(rmax, rows);
+        A.cp = ar.alloc<int>(cols + count);
+        A.ci = ar.alloc<int>(nz);
+        A.cnt = ar.alloc<int>(cols);
+        A.cax = ar.alloc<float>(nz);
+        A.sax = ar.alloc<float>(nz);
+        A.scax = ar.alloc<float>(nz);
+        float** colv[] = {&A.dc, &A.sc, &A.scl, &A.scu, &A.x[0], &A.x[1], &A.xa[0], &A.xa[1],
+                          &A.xbar, &A.pesx, &A.vt};
+        for (float** v : colv) *v = ar.alloc<float>(cols);
+        float** rowv[] = {&A.dr, &A.srmin, &A.srmax, &A.y[0], &A.y[1], &A.ya[0], &A.ya[1],
+                          &A.axc[0], &A.axc[1], &A.pesy, &A.mt};
+        for (float** v : rowv) *v = ar.alloc<float>(rows);
+        CU(cudaMemsetAsync(A.pesx, 0, sizeof(float) * cols, st));
+        CU(cudaMemsetAsync(A.pesy, 0, sizeof(float) * rows, st));
+        A.fac = up(fac.data(), fac.size());
+        A.tol = o.tolerance;
+        // per-instance iteration cap (the kernel has no wall clock)
+        A.maxit = (long long)std::max<int64_t>(1, o.max_iterations);
+        A.check = o.check_period > 0 ? o.check_period : 64;
+        A.x_out = x ? ar.alloc<double>(cols) : nullptr;
+        A.y_out = y ? ar.alloc<double>(rows) : nullptr;
+        A.out = ar.alloc<BatchOut>(count);
+        int sms = 0, dev = 0, per_sm = 0;
+        CU(cudaGetDevice(&dev));
+        CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kThreads, 0));
+        const int grid = std::max(1, std::min(count, sms * std::max(1, per_sm)));
+        cudaEvent_t e0, e1;
+        CU(cudaEventCreate(&e0));
+        CU(cudaEventCreate(&e1));
+        CU(cudaEventRecord(e0, st));
+        k_batch<<<grid, kThreads, 0, st>>>(A);
+        CU(cudaGetLastError());
+        CU(cudaEventRecord(e1, st));
+        std::vector<BatchOut> out(count);
+        CU(cudaMemcpyAsync(out.data(), A.out, sizeof(BatchOut) * count, cudaMemcpyDeviceToHost, st));
+        if (x) CU(cudaMemcpyAsync(x, A.x_out, sizeof(double) * cols, cudaMemcpyDeviceToHost, st));
+        if (y) CU(cudaMemcpyAsync(y, A.y_out, sizeof(double) * rows, cudaMemcpyDeviceToHost, st));
+        CU(cudaStreamSynchronize(st));
+        float kms = 0.f;
+        CU(cudaEventElapsedTime(&kms, e0, e1));
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+        const double wall = std::chrono::duration<double, std::milli>(
+                                std::chrono::steady_clock::now() - t_start).count();
+        for (int b = 0; b < count; ++b) {
+            igaos_pdhg_batch_result& r = res[b];
+            const BatchOut& q = out[b];
+            r.status = (desc[b].m > 0 && desc[b].n > 0) ? q.status : IGAOS_STATUS_ERROR;
+            r.objective = q.objective;
+            r.pinf = q.pinf;
+            r.dinf = q.dinf;
+            r.rel_gap = q.gap;
+            r.prow = q.prow;
+            r.iterations = q.iterations;
+            r.attempts = q.attempts;
+            r.restarts = q.restarts;
+            r.kernel_time_ms = kms;
+            r.total_time_ms = wall;
+        }
+    } catch (const CudaError& e) {
+        return igx_set_error(e.code, e.what());
+    } catch (const std::exception& e) {
+        return igx_set_error(IGAOS_PDHG_ERR_CUDA, e.what());
+    }
+    return igx_set_error(IGAOS_PDHG_OK, "");
+}

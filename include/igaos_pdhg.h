@@ -186,6 +186,36 @@ int igaos_pdhg_evaluate(igaos_pdhg_problem* p, const double* x,
 int igaos_pdhg_spmv(igaos_pdhg_problem* p, int transpose, int precision,
                     const double* x, double* y);
 
+/* ---- batched solve ------------------------------------------------------
+ * Per-instance outcome of igaos_pdhg_solve_batch. */
+typedef struct igaos_pdhg_batch_result {
+    int status;              /* IGAOS_STATUS_* */
+    int pad;
+    double objective;        /* c^T x of the instance */
+    double pinf, dinf, rel_gap, prow;
+    int64_t iterations, attempts, restarts;
+    double kernel_time_ms;   /* the whole batch's persistent kernel (same for all) */
+    double total_time_ms;    /* the whole call: upload, kernel, download */
+} igaos_pdhg_batch_result;
+
+/* Solves `count` independent LPs of uneven sizes in one persistent kernel
+ * launch: instance b is m[b] x n[b]; its CSR row pointer (m[b]+1 entries,
+ * starting at 0) follows the previous instance's in `ap`, its column indices
+ * (local, 0..n[b]-1, no duplicate (row, column) entries) and values follow in
+ * `ai`/`ax`, its c/cl/cu in the concatenated n-vectors and rmin/rmax in the
+ * concatenated m-vectors. Each instance runs the engine's iteration (Ruiz,
+ * power iteration, adaptive line search, averaging, restarts, primal weight;
+ * FP32 iterates, termination metrics combined in FP64) to `tolerance` or
+ * `max_iterations` on its own, with its own restarts and termination; the
+ * reference has no batched path (its engine is one LP per call,
+ * src/pdhg/pdhg.hpp:9). x (sum n) and y (sum m) may be NULL. */
+int igaos_pdhg_solve_batch(int count, const int* m, const int* n,
+                           const int* ap, const int* ai, const double* ax,
+                           const double* c, const double* cl, const double* cu,
+                           const double* rmin, const double* rmax,
+                           const igaos_pdhg_options* opt,
+                           igaos_pdhg_batch_result* res, double* x, double* y);
+
 /* Allocation-free FP64 KKT metrics, for callers that cannot call cudaMalloc
  * (device memory owned by a framework allocator or a fixed pool, or loops
  * where an allocation's device synchronisation is not acceptable). No

@@ -1,0 +1,88 @@
+"""Batched solves (igaos_pdhg_solve_batch): thousands of uneven LPs in one
+persistent launch, each with its own restarts and termination.
+
+* Every golden LP solved inside one batch reaches the reference simplex
+  optimum (tests/golden, made by the reference's own simplex) within 1e-5 at
+  1e-6 relative KKT (FP32 iterates).
+* C3-shaped instances (m log-uniform, n = 2.5 m, Bernoulli pattern, box
+  [0,5]) agree with the single-LP engine (FP64, 1e-8).
+* Per-instance results do not depend on the batch's composition or order
+  (CTAs never share an instance) and repeat bit for bit.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from igaos_gb300 import generators as G
+
+pytestmark = pytest.mark.gpu
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = json.load(open(os.path.join(HERE, "golden", "lp_objectives.json")))
+
+
+def golden_lps():
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    from make_golden import make_lp
+    names = sorted(k for k in GOLD if not k.startswith("zipf"))
+    return names, [make_lp(GOLD[k]["generator"], GOLD[k]["kwargs"]) for k in names]
+
+
+def rel(a, b):
+    return abs(a - b) / max(1.0, abs(b))
+
+
+def c3_like(count, seed, m_hi=400):
+    rng = np.random.default_rng(seed)
+    ms = np.rint(np.exp(rng.uniform(np.log(20), np.log(m_hi), count))).astype(int)
+    return [G.bernoulli_lp(rng, int(m), int(round(2.5 * m)), 0.01 if m >= 100 else 0.05, 5.0)
+            for m in ms]
+
+
+def test_batch_reaches_simplex_optimum(native):
+    from igaos_gb300 import capi
+    names, lps = golden_lps()
+    out = capi.solve_batch(lps, tolerance=1e-6, max_iterations=400000)
+    for name, lp, r in zip(names, lps, out):
+        assert r["status_name"] == "near-optimal", (name, r)
+        assert rel(r["objective"], GOLD[name]["simplex_objective"]) <= 1e-5, (name, r["objective"])
+        assert max(r["pinf"], r["dinf"], r["rel_gap"], r["prow"]) <= 1e-6
+
+
+def test_batch_matches_single_lp_engine(native):
+    from igaos_gb300 import capi
+    lps = c3_like(48, 3)
+    out = capi.solve_batch(lps, tolerance=1e-6, max_iterations=400000)
+    for lp, r in zip(lps, out):
+        assert r["status_name"] == "near-optimal"
+        single = capi.solve_lp(lp, tolerance=1e-8, time_limit=60.0)
+        assert single["status_name"] == "near-optimal"
+        assert rel(r["objective"], single["objective"]) <= 2e-5
+
+
+def test_batch_order_independent_and_deterministic(native):
+    from igaos_gb300 import capi
+    lps = c3_like(40, 9)
+    a = capi.solve_batch(lps, tolerance=1e-6, max_iterations=400000)
+    b = capi.solve_batch(lps, tolerance=1e-6, max_iterations=400000)
+    perm = np.random.default_rng(1).permutation(len(lps))
+    c = capi.solve_batch([lps[i] for i in perm], tolerance=1e-6, max_iterations=400000)
+    for i in range(len(lps)):
+        assert a[i]["objective"] == b[i]["objective"] and a[i]["iterations"] == b[i]["iterations"]
+        assert np.array_equal(a[i]["x"], b[i]["x"])
+    for k, i in enumerate(perm):
+        assert c[k]["objective"] == a[i]["objective"] and c[k]["iterations"] == a[i]["iterations"]
+
+
+def test_batch_iteration_cap_and_validation(native):
+    from igaos_gb300 import capi
+    lps = c3_like(4, 5)
+    out = capi.solve_batch(lps, tolerance=1e-12, max_iterations=100)
+    assert all(r["status_name"] == "iteration-limit" and r["iterations"] == 100 for r in out)
+    bad = G.random_lp(10, 20, 10, 0)
+    bad.ai = bad.ai.copy()
+    bad.ai[0] = 99
+    with pytest.raises(capi.EngineError, match="column index out of range"):
+        capi.solve_batch([bad])
