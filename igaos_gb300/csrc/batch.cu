@@ -8,14 +8,18 @@
 // search (:751-794), averaging (:795-799), KKT checks every `check`
 // iterations with the termination test (:835-840), restarts and the
 // primal-weight update (:1001-1075) -- with per-instance restart and
-// termination. Iterates and matrices are FP32 with compensated row sums; the
-// termination metrics are accumulated with compensated FP32 sums and combined
-// in FP64. Incumbent/rollback and dual repair are not part of this path.
+// termination. Attempts stream FP32 (compensated row sums); the iterates are
+// FP32 deltas from an FP64 anchor that every restart re-sets, with the
+// residual data (reduced costs, shifted row bounds and box) formed in FP64
+// from the original FP64 values, so the termination metrics -- evaluated in
+// FP64 on anchor + delta -- reach FP64-level accuracy. Incumbent/rollback and
+// dual repair are not part of this path.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <numeric>
+#include <type_traits>
 #include <vector>
 
 #include "device.cuh"
@@ -43,13 +47,16 @@ struct BatchArgs {
     unsigned int* queue;
     const BatchDesc* desc;
     const int *ap, *ai;
-    const float* ax;
+    const float* ax;     // original values, FP32 (Ruiz, scaled FP32 copies)
+    const double* axd;   // original values, FP64 (anchor residuals)
     const double *c, *cl, *cu, *rmin, *rmax;
     int *cp, *ci, *cnt;
     float *cax, *sax, *scax;
-    float *dr, *dc, *sc, *scl, *scu, *srmin, *srmax;
-    float *x[2], *xa[2], *xbar, *pesx, *vt;
-    float *y[2], *ya[2], *axc[2], *pesy, *mt;
+    double* cax64;       // original values in CSC order, FP64
+    float *dr, *dc, *sc, *scl, *scu, *srmin, *srmax, *yh32;
+    float *x[2], *xa[2], *xbar, *vt;
+    float *y[2], *ya[2], *axc[2], *mt;
+    double *xh, *yh, *pesx, *pesy, *axh, *atyh;
     const float* fac;
     double tol;
     long long maxit;
@@ -61,10 +68,10 @@ struct BatchArgs {
 
 struct BatchShared {
     Acc<float> acc[kWarps * 4];
+    double dred[kWarps * 8];
     float fmax_[kWarps * 8];
     int part[kThreads];
     int inst;
-    // line search / restart state (thread 0 writes, all read)
     float tau, sigma, w;
     int parity, accept;
     long long kdone;
@@ -128,12 +135,15 @@ struct Inst {
     int m, n;
     const int *ap, *ai;
     const float* ax;
+    const double* axd;
     const double *c, *cl, *cu, *rmin, *rmax;
     int *cp, *ci, *cnt;
     float *cax, *sax, *scax;
-    float *dr, *dc, *sc, *scl, *scu, *srmin, *srmax;
-    float *x[2], *xa[2], *xbar, *pesx, *vt;
-    float *y[2], *ya[2], *axc[2], *pesy, *mt;
+    double* cax64;
+    float *dr, *dc, *sc, *scl, *scu, *srmin, *srmax, *yh32;
+    float *x[2], *xa[2], *xbar, *vt;
+    float *y[2], *ya[2], *axc[2], *mt;
+    double *xh, *yh, *pesx, *pesy, *axh, *atyh;
 };
 
 __device__ Inst make_inst(const BatchArgs& a, const BatchDesc& d) {
@@ -143,6 +153,7 @@ __device__ Inst make_inst(const BatchArgs& a, const BatchDesc& d) {
     I.ap = a.ap + d.ap_off;
     I.ai = a.ai + d.nz_off;
     I.ax = a.ax + d.nz_off;
+    I.axd = a.axd + d.nz_off;
     I.c = a.c + d.col_off;
     I.cl = a.cl + d.col_off;
     I.cu = a.cu + d.col_off;
@@ -152,11 +163,13 @@ __device__ Inst make_inst(const BatchArgs& a, const BatchDesc& d) {
     I.ci = a.ci + d.nz_off;
     I.cnt = a.cnt + d.col_off;
     I.cax = a.cax + d.nz_off;
+    I.cax64 = a.cax64 + d.nz_off;
     I.sax = a.sax + d.nz_off;
     I.scax = a.scax + d.nz_off;
     I.dr = a.dr + d.row_off;
     I.srmin = a.srmin + d.row_off;
     I.srmax = a.srmax + d.row_off;
+    I.yh32 = a.yh32 + d.row_off;
     I.dc = a.dc + d.col_off;
     I.sc = a.sc + d.col_off;
     I.scl = a.scl + d.col_off;
@@ -169,19 +182,63 @@ __device__ Inst make_inst(const BatchArgs& a, const BatchDesc& d) {
         I.axc[s] = a.axc[s] + d.row_off;
     }
     I.xbar = a.xbar + d.col_off;
-    I.pesx = a.pesx + d.col_off;
     I.vt = a.vt + d.col_off;
-    I.pesy = a.pesy + d.row_off;
     I.mt = a.mt + d.row_off;
+    I.xh = a.xh + d.col_off;
+    I.pesx = a.pesx + d.col_off;
+    I.atyh = a.atyh + d.col_off;
+    I.yh = a.yh + d.row_off;
+    I.pesy = a.pesy + d.row_off;
+    I.axh = a.axh + d.row_off;
     return I;
 }
 
-// y = M v over rows [0, rows) of a CSR (thread per row, compensated)
+// one row of a CSR times v (thread per row, compensated FP32)
 __device__ __forceinline__ Acc<float> row_dot(const int* ptr, const int* idx, const float* val,
                                               const float* v, int r) {
     Acc<float> acc;
     for (int p = ptr[r]; p < ptr[r + 1]; ++p) acc.add(val[p], v[idx[p]]);
     return acc;
+}
+
+// Full FP64 column value of delta dx (scaled units), with the at-bound rule:
+// a delta on its FP32 shifted bound is exactly at the bound.
+__device__ __forceinline__ double full_x(const Inst& I, int j, float dx) {
+    if (dx == I.scl[j]) return I.cl[j] / (double)I.dc[j];
+    if (dx == I.scu[j]) return I.cu[j] / (double)I.dc[j];
+    return I.xh[j] + (double)dx;
+}
+
+// Residual data of the LP seen from the anchor (xh, yh), FP64 -> FP32:
+// sc = c~ + A~^T yh, [scl, scu] = box~ - xh, [srmin, srmax] = rows~ - A~ xh,
+// with A~_ij = a_ij dc_j / dr_i formed in FP64 from the FP64 values.
+__device__ void anchor_data(Inst& I) {
+    const int t = threadIdx.x;
+    for (int i = t; i < I.m; i += kThreads) {
+        const double dri = I.dr[i];
+        double s = 0.0;
+        for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) {
+            const int j = I.ai[p];
+            s = fma(I.axd[p] * (double)I.dc[j] / dri, I.xh[j], s);
+        }
+        I.axh[i] = s;
+        I.srmin[i] = (float)(I.rmin[i] / dri - s);
+        I.srmax[i] = (float)(I.rmax[i] / dri - s);
+        I.yh32[i] = (float)I.yh[i];
+    }
+    for (int j = t; j < I.n; j += kThreads) {
+        const double dcj = I.dc[j];
+        double s = 0.0;
+        for (int p = I.cp[j]; p < I.cp[j + 1]; ++p) {
+            const int i = I.ci[p];
+            s = fma(I.cax64[p] * dcj / (double)I.dr[i], I.yh[i], s);
+        }
+        I.atyh[j] = s;
+        I.sc[j] = (float)(I.c[j] * dcj + s);
+        I.scl[j] = (float)(I.cl[j] / dcj - I.xh[j]);
+        I.scu[j] = (float)(I.cu[j] / dcj - I.xh[j]);
+    }
+    __syncthreads();
 }
 
 // ---- setup: CSC, Ruiz, scaled data, power iteration ----------------------
@@ -200,25 +257,26 @@ __device__ void setup(BatchShared& sh, Inst& I, float& eta0, float& omega0) {
         for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) {
             const int q = atomicAdd(&I.cnt[I.ai[p]], 1);
             I.ci[q] = i;
-            I.cax[q] = I.ax[p];
+            I.cax64[q] = I.axd[p];
         }
     __syncthreads();
     for (int j = t; j < n; j += kThreads) {  // insertion sort by row index
         const int b = I.cp[j], e = I.cp[j + 1];
         for (int q = b + 1; q < e; ++q) {
             const int r = I.ci[q];
-            const float v = I.cax[q];
+            const double v = I.cax64[q];
             int k = q - 1;
             while (k >= b && I.ci[k] > r) {
                 I.ci[k + 1] = I.ci[k];
-                I.cax[k + 1] = I.cax[k];
+                I.cax64[k + 1] = I.cax64[k];
                 --k;
             }
             I.ci[k + 1] = r;
-            I.cax[k + 1] = v;
+            I.cax64[k + 1] = v;
         }
+        for (int q = b; q < e; ++q) I.cax[q] = (float)I.cax64[q];
     }
-    // Ruiz, 10 sweeps (FP32)
+    // Ruiz, 10 sweeps (FP32 factors)
     for (int i = t; i < m; i += kThreads) I.dr[i] = 1.f;
     for (int j = t; j < n; j += kThreads) I.dc[j] = 1.f;
     __syncthreads();
@@ -238,22 +296,17 @@ __device__ void setup(BatchShared& sh, Inst& I, float& eta0, float& omega0) {
         }
         __syncthreads();
     }
-    // scaled problem
+    // scaled FP32 matrix; initial weight from the scaled cost and row bounds
     Acc<float> nq[2];
     for (int i = t; i < m; i += kThreads) {
         for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) I.sax[p] = I.ax[p] * I.dc[I.ai[p]] / I.dr[i];
         const float lo = (float)I.rmin[i] / I.dr[i], hi = (float)I.rmax[i] / I.dr[i];
-        I.srmin[i] = lo;
-        I.srmax[i] = hi;
         const float q = isfinite(hi) ? hi : (isfinite(lo) ? lo : 0.f);
         nq[1].add(q, q);
     }
     for (int j = t; j < n; j += kThreads) {
         for (int p = I.cp[j]; p < I.cp[j + 1]; ++p) I.scax[p] = I.cax[p] * I.dc[j] / I.dr[I.ci[p]];
         const float cs = (float)I.c[j] * I.dc[j];
-        I.sc[j] = cs;
-        I.scl[j] = (float)I.cl[j] / I.dc[j];
-        I.scu[j] = (float)I.cu[j] / I.dc[j];
         nq[0].add(cs, cs);
     }
     bmerge<2>(sh, nq);
@@ -295,84 +348,83 @@ __device__ void setup(BatchShared& sh, Inst& I, float& eta0, float& omega0) {
     __syncthreads();
 }
 
-// ---- FP64-combined metrics of one candidate (original units) -------------
+// ---- FP64 metrics of one candidate (anchor + delta, original units) -----
 struct BMetrics {
     double pinf, dinf, gap, op, od, prow, err;
     bool finite;
 };
 
 __device__ BMetrics metrics(BatchShared& sh, Inst& I, const float* xs, const float* ys,
-                            float cmax) {
+                            double cmax) {
     const int t = threadIdx.x;
-    // rows: A x, ymax
-    float fr[4] = {0.f, 0.f, 0.f, 0.f};  // pv, pa, prow, ymax
+    double r4[4] = {0.0, 0.0, 0.0, 0.0};  // pv, pa, prow, ymax
     for (int i = t; i < I.m; i += kThreads) {
-        const float Ax = (float)(row_dot(I.ap, I.ai, I.sax, xs, i).result_d() * (double)I.dr[i]);
-        const float lo = (float)I.rmin[i], hi = (float)I.rmax[i];
-        const float vi = fmaxf(lo - Ax, Ax - hi);
-        fr[0] = fmaxf(fr[0], vi);
-        fr[1] = fmaxf(fr[1], fabsf(fminf(fmaxf(Ax, lo), hi)));
-        float scv = fabsf(Ax);
-        if (isfinite(lo)) scv = fmaxf(scv, fabsf(lo));
-        if (isfinite(hi)) scv = fmaxf(scv, fabsf(hi));
-        fr[2] = fmaxf(fr[2], fmaxf(0.f, vi) / (1.f + scv));
-        fr[3] = fmaxf(fr[3], fabsf(ys[i] / I.dr[i]));
+        const double Ax = (I.axh[i] + row_dot(I.ap, I.ai, I.sax, xs, i).result_d()) * (double)I.dr[i];
+        const double lo = I.rmin[i], hi = I.rmax[i];
+        const double vi = smax(lo - Ax, Ax - hi);
+        r4[0] = smax(r4[0], vi);
+        r4[1] = smax(r4[1], fabs(smin(smax(Ax, lo), hi)));
+        double scv = fabs(Ax);
+        if (isfinite(lo)) scv = smax(scv, fabs(lo));
+        if (isfinite(hi)) scv = smax(scv, fabs(hi));
+        r4[2] = smax(r4[2], smax(0.0, vi) / (1.0 + scv));
+        r4[3] = smax(r4[3], fabs((I.yh[i] + (double)ys[i]) / (double)I.dr[i]));
     }
-    bmaxf<4>(sh, fr);
-    __shared__ float s_r[4];
+    block_max<4>(r4, sh.dred);
+    __shared__ double s_r[4];
     if (t == 0)
-        for (int q = 0; q < 4; ++q) s_r[q] = fr[q];
+        for (int q = 0; q < 4; ++q) s_r[q] = r4[q];
     __syncthreads();
-    const float yz = 1e-8f * (1.f + s_r[3]);
-    const float dz = 1e-8f * (1.f + cmax);
-    // columns: reduced costs, dinf, c'x, column part of the bound
-    float fc[2] = {0.f, 0.f};  // dv, unbounded
-    Acc<float> sums[3];        // op, od (columns), od (rows)
+    const double yz = 1e-8 * (1.0 + s_r[3]);
+    const double dz = 1e-8 * (1.0 + cmax);
+    double mx[2] = {0.0, 0.0};  // dv, unbounded
+    double sm[3] = {0.0, 0.0, 0.0};  // op, od (columns), od (rows)
     for (int j = t; j < I.n; j += kThreads) {
-        const float d = (float)I.c[j] + (float)(row_dot(I.cp, I.ci, I.scax, ys, j).result_d() / I.dc[j]);
+        const double aty = I.atyh[j] + row_dot(I.cp, I.ci, I.scax, ys, j).result_d();
+        const double d = I.c[j] + aty / (double)I.dc[j];
+        const double lo = I.cl[j], hi = I.cu[j];
         const float xv = xs[j];
-        const float lo = (float)I.cl[j], hi = (float)I.cu[j];
-        const float x = xv == I.scl[j] ? lo : (xv == I.scu[j] ? hi : xv * I.dc[j]);
-        const float bnd = fabsf(isfinite(hi) ? hi : lo);
-        const float tol = 1e-9f * (1.f + bnd);
-        float e;
-        if (x <= lo + tol && d > 0) e = 0.f;
-        else if (x >= hi - tol && d < 0) e = 0.f;
-        else e = fabsf(d);
-        fc[0] = fmaxf(fc[0], e);
-        sums[0].add((float)I.c[j], x);
+        const double x = xv == I.scl[j] ? lo : (xv == I.scu[j] ? hi : (I.xh[j] + (double)xv) * (double)I.dc[j]);
+        const double bnd = fabs(isfinite(hi) ? hi : lo);
+        const double tol = 1e-9 * (1.0 + bnd);
+        double e;
+        if (x <= lo + tol && d > 0) e = 0.0;
+        else if (x >= hi - tol && d < 0) e = 0.0;
+        else e = fabs(d);
+        mx[0] = smax(mx[0], e);
+        sm[0] += I.c[j] * x;
         if (d >= 0) {
-            if (isfinite(lo)) sums[1].add(d, lo);
-            else if (d > dz) fc[1] = 1.f;
+            if (isfinite(lo)) sm[1] += d * lo;
+            else if (d > dz) mx[1] = 1.0;
         } else {
-            if (isfinite(hi)) sums[1].add(d, hi);
-            else if (-d > dz) fc[1] = 1.f;
+            if (isfinite(hi)) sm[1] += d * hi;
+            else if (-d > dz) mx[1] = 1.0;
         }
     }
     for (int i = t; i < I.m; i += kThreads) {
-        const float yv = ys[i] / I.dr[i];
+        const double yv = (I.yh[i] + (double)ys[i]) / (double)I.dr[i];
         if (yv > yz) {
-            if (isfinite((float)I.rmax[i])) sums[2].add(-yv, (float)I.rmax[i]);
-            else fc[1] = 1.f;
+            if (isfinite(I.rmax[i])) sm[2] -= yv * I.rmax[i];
+            else mx[1] = 1.0;
         } else if (yv < -yz) {
-            if (isfinite((float)I.rmin[i])) sums[2].add(-yv, (float)I.rmin[i]);
-            else fc[1] = 1.f;
+            if (isfinite(I.rmin[i])) sm[2] -= yv * I.rmin[i];
+            else mx[1] = 1.0;
         }
     }
-    bmaxf<2>(sh, fc);
-    bmerge<3>(sh, sums);
+    block_max<2>(mx, sh.dred);
+    block_sum<3>(sm, sh.dred);
     __shared__ BMetrics s_m;
     if (t == 0) {
         BMetrics mt;
-        mt.pinf = fmax((double)s_r[0], 0.0) / (1.0 + (double)s_r[1]);
+        mt.pinf = smax(s_r[0], 0.0) / (1.0 + s_r[1]);
         mt.prow = s_r[2];
-        mt.dinf = (double)fc[0] / (1.0 + (double)cmax);
-        mt.op = sums[0].result_d();
-        const bool bounded = !(fc[1] > 0.f);
-        mt.od = bounded ? sums[1].result_d() + sums[2].result_d() : -CUDART_INF;
-        mt.gap = bounded ? fmax(0.0, mt.op - mt.od) / (1.0 + fabs(mt.op)) : CUDART_INF;
+        mt.dinf = mx[0] / (1.0 + cmax);
+        mt.op = sm[0];
+        const bool bounded = !(mx[1] > 0.0);
+        mt.od = bounded ? sm[1] + sm[2] : -CUDART_INF;
+        mt.gap = bounded ? smax(0.0, mt.op - mt.od) / (1.0 + fabs(mt.op)) : CUDART_INF;
         mt.finite = isfinite(mt.pinf) && isfinite(mt.dinf);
-        mt.err = fmax(mt.pinf, fmax(mt.dinf, isfinite(mt.gap) ? mt.gap : 0.0));
+        mt.err = smax(mt.pinf, smax(mt.dinf, isfinite(mt.gap) ? mt.gap : 0.0));
         s_m = mt;
     }
     __syncthreads();
@@ -383,12 +435,16 @@ __device__ BMetrics metrics(BatchShared& sh, Inst& I, const float* xs, const flo
 __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& d, int b) {
     Inst I = make_inst(a, d);
     const int t = threadIdx.x, m = I.m, n = I.n;
-    __shared__ float s_eta0, s_omega0, s_cmax;
+    __shared__ float s_eta0, s_omega0;
+    __shared__ double s_cmax;
+    for (int j = t; j < n; j += kThreads) I.xh[j] = I.pesx[j] = 0.0;
+    for (int i = t; i < m; i += kThreads) I.yh[i] = I.pesy[i] = 0.0;
     setup(sh, I, s_eta0, s_omega0);
+    anchor_data(I);
     {
-        float cm[1] = {0.f};
-        for (int j = t; j < n; j += kThreads) cm[0] = fmaxf(cm[0], fabsf((float)I.c[j]));
-        bmaxf<1>(sh, cm);
+        double cm[1] = {0.0};
+        for (int j = t; j < n; j += kThreads) cm[0] = smax(cm[0], fabs(I.c[j]));
+        block_max<1>(cm, sh.dred);
         if (t == 0) s_cmax = cm[0];
     }
     for (int j = t; j < n; j += kThreads) I.x[0][j] = I.xa[0][j] = 0.f;
@@ -431,7 +487,7 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
         const int p = sh.parity, q = p ^ 1;
         const float tau = sh.tau, sigma = sh.sigma, w = sh.w;
         Acc<float> dots[3];
-        // primal step fused with A^T y (thread per column)
+        // primal step fused with A^T y (thread per column), on the deltas
         for (int j = t; j < n; j += kThreads) {
             const float g = I.sc[j] + row_dot(I.cp, I.ci, I.scax, I.y[p], j).result();
             const float xv = I.x[p][j];
@@ -444,12 +500,14 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
             I.xa[q][j] = fmaf(w, xn - av, av);
         }
         __syncthreads();
-        // dual step fused with A xbar (thread per row)
+        // dual step fused with A xbar (thread per row); the projection acts
+        // on the full value, so the anchor enters its argument
         for (int i = t; i < m; i += kThreads) {
             const float ab = row_dot(I.ap, I.ai, I.sax, I.xbar, i).result();
             const float yv = I.y[p][i];
             const float tt = fmaf(sigma, ab, yv);
-            const float yn = fmaf(-sigma, fminf(fmaxf(tt / sigma, I.srmin[i]), I.srmax[i]), tt);
+            const float arg = (tt + I.yh32[i]) / sigma;
+            const float yn = fmaf(-sigma, fminf(fmaxf(arg, I.srmin[i]), I.srmax[i]), tt);
             I.y[q][i] = yn;
             const float dy = yn - yv;
             const float ax = I.axc[p][i];
@@ -546,45 +604,47 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
             }
             __syncthreads();
             if (s_restart) {
-                const int r = pc;
-                if (s_avg_better) {
-                    for (int j = t; j < n; j += kThreads) I.x[r][j] = I.xa[r][j];
-                    for (int i = t; i < m; i += kThreads) I.y[r][i] = I.ya[r][i];
-                    __syncthreads();
-                }
-                Acc<float> dn[2];
+                // the restart point becomes the new FP64 anchor; deltas restart
+                // at zero; primal weight from the anchors' movement
+                const float* dxs = s_avg_better ? I.xa[pc] : I.x[pc];
+                const float* dys = s_avg_better ? I.ya[pc] : I.y[pc];
+                double dn[2] = {0.0, 0.0};
                 for (int j = t; j < n; j += kThreads) {
-                    const float xv = I.x[r][j];
-                    I.xa[r][j] = xv;
-                    const float dd = xv - I.pesx[j];
-                    dn[0].add(dd, dd);
-                    I.pesx[j] = xv;
+                    const double nx = full_x(I, j, dxs[j]);
+                    const double dd = nx - I.pesx[j];
+                    dn[0] = fma(dd, dd, dn[0]);
+                    I.pesx[j] = nx;
                 }
-                __syncthreads();
                 for (int i = t; i < m; i += kThreads) {
-                    const float yv = I.y[r][i];
-                    I.ya[r][i] = yv;
-                    const float dd = yv - I.pesy[i];
-                    dn[1].add(dd, dd);
-                    I.pesy[i] = yv;
-                    I.axc[r][i] = row_dot(I.ap, I.ai, I.sax, I.x[r], i).result();
+                    const double ny = I.yh[i] + (double)dys[i];
+                    const double dd = ny - I.pesy[i];
+                    dn[1] = fma(dd, dd, dn[1]);
+                    I.pesy[i] = ny;
                 }
-                bmerge<2>(sh, dn);
-                if (t == 0) {
-                    if (s_have_pe) {
-                        const double dxn = dn[0].result_d(), dyn = dn[1].result_d();
-                        if (dxn > 1e-24 && dyn > 1e-24) {
-                            const double om = sqrt(s_omega * sqrt(dyn / dxn));
-                            if (isfinite(om) && om > 0.0) s_omega = fmin(fmax(om, 1e-6), 1e6);
-                        }
+                block_sum<2>(dn, sh.dred);
+                if (t == 0 && s_have_pe) {
+                    const double dxn = dn[0], dyn = dn[1];
+                    if (dxn > 1e-24 && dyn > 1e-24) {
+                        const double om = sqrt(s_omega * sqrt(dyn / dxn));
+                        if (isfinite(om) && om > 0.0) s_omega = fmin(fmax(om, 1e-6), 1e6);
                     }
-                    s_have_pe = 1;
+                }
+                if (t == 0) s_have_pe = 1;
+                // the new anchor is the restart point (held in pes)
+                for (int j = t; j < n; j += kThreads) {
+                    I.xh[j] = I.pesx[j];
+                    I.x[pc][j] = I.xa[pc][j] = 0.f;
+                }
+                for (int i = t; i < m; i += kThreads) {
+                    I.yh[i] = I.pesy[i];
+                    I.y[pc][i] = I.ya[pc][i] = I.axc[pc][i] = 0.f;
                 }
                 __syncthreads();
+                anchor_data(I);
             }
         }
     }
-    // answer: original units
+    // answer: anchor + delta of the chosen candidate, original units
     const int pf = sh.parity;
     const float* xs = s_use_avg ? I.xa[pf] : I.x[pf];
     const float* ys = s_use_avg ? I.ya[pf] : I.y[pf];
@@ -593,10 +653,11 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
     if (xo)
         for (int j = t; j < n; j += kThreads) {
             const float xv = xs[j];
-            xo[j] = xv == I.scl[j] ? I.cl[j] : (xv == I.scu[j] ? I.cu[j] : (double)xv * I.dc[j]);
+            xo[j] = xv == I.scl[j] ? I.cl[j]
+                                   : (xv == I.scu[j] ? I.cu[j] : (I.xh[j] + (double)xv) * (double)I.dc[j]);
         }
     if (yo)
-        for (int i = t; i < m; i += kThreads) yo[i] = (double)ys[i] / (double)I.dr[i];
+        for (int i = t; i < m; i += kThreads) yo[i] = (I.yh[i] + (double)ys[i]) / (double)I.dr[i];
     if (t == 0) {
         BatchOut o;
         o.status = s_status;
@@ -662,7 +723,8 @@ extern "C" int igaos_pdhg_solve_batch(int count, const int* m, const int* n, con
             d.m = m[b];
             d.n = n[b];
             const int* bap = ap + ap_off;
-            if (bap[0] != 0) return igx_set_error(IGAOS_PDHG_ERR_INVALID, "each instance's row pointer must start at 0");
+            if (bap[0] != 0)
+                return igx_set_error(IGAOS_PDHG_ERR_INVALID, "each instance's row pointer must start at 0");
             for (int i = 0; i < d.m; ++i)
                 if (bap[i + 1] < bap[i])
                     return igx_set_error(IGAOS_PDHG_ERR_INVALID, "row pointer must be non-decreasing");
@@ -733,6 +795,7 @@ extern "C" int igaos_pdhg_solve_batch(int count, const int* m, const int* n, con
         float* axf = ar.alloc<float>(nz);
         k_to_float<<<1216, 256, 0, st>>>(nz, axd, axf);
         A.ax = axf;
+        A.axd = axd;
         A.c = up(c, cols);
         A.cl = up(cl, cols);
         A.cu = up(cu, cols);
@@ -742,16 +805,19 @@ extern "C" int igaos_pdhg_solve_batch(int count, const int* m, const int* n, con
         A.ci = ar.alloc<int>(nz);
         A.cnt = ar.alloc<int>(cols);
         A.cax = ar.alloc<float>(nz);
+        A.cax64 = ar.alloc<double>(nz);
         A.sax = ar.alloc<float>(nz);
         A.scax = ar.alloc<float>(nz);
         float** colv[] = {&A.dc, &A.sc, &A.scl, &A.scu, &A.x[0], &A.x[1], &A.xa[0], &A.xa[1],
-                          &A.xbar, &A.pesx, &A.vt};
+                          &A.xbar, &A.vt};
         for (float** v : colv) *v = ar.alloc<float>(cols);
-        float** rowv[] = {&A.dr, &A.srmin, &A.srmax, &A.y[0], &A.y[1], &A.ya[0], &A.ya[1],
-                          &A.axc[0], &A.axc[1], &A.pesy, &A.mt};
+        float** rowv[] = {&A.dr, &A.srmin, &A.srmax, &A.yh32, &A.y[0], &A.y[1], &A.ya[0],
+                          &A.ya[1], &A.axc[0], &A.axc[1], &A.mt};
         for (float** v : rowv) *v = ar.alloc<float>(rows);
-        CU(cudaMemsetAsync(A.pesx, 0, sizeof(float) * cols, st));
-        CU(cudaMemsetAsync(A.pesy, 0, sizeof(float) * rows, st));
+        double** col64[] = {&A.xh, &A.pesx, &A.atyh};
+        for (double** v : col64) *v = ar.alloc<double>(cols);
+        double** row64[] = {&A.yh, &A.pesy, &A.axh};
+        for (double** v : row64) *v = ar.alloc<double>(rows);
         A.fac = up(fac.data(), fac.size());
         A.tol = o.tolerance;
         // per-instance iteration cap (the kernel has no wall clock)
@@ -787,6 +853,7 @@ extern "C" int igaos_pdhg_solve_batch(int count, const int* m, const int* n, con
             igaos_pdhg_batch_result& r = res[b];
             const BatchOut& q = out[b];
             r.status = (desc[b].m > 0 && desc[b].n > 0) ? q.status : IGAOS_STATUS_ERROR;
+            r.pad = 0;
             r.objective = q.objective;
             r.pinf = q.pinf;
             r.dinf = q.dinf;
