@@ -25,7 +25,7 @@ CLI = os.path.join(PKG, "igaos")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", INC, "-I", CSRC] + ARCH
-CU_SOURCES = ["engine.cu", "capi.cu", "batch.cu", "kkt_noalloc.cu"]
+CU_SOURCES = ["engine.cu", "capi.cu", "batch.cu", "kkt_noalloc.cu", "unrolled.cu"]
 CXX_HOST = ["model.cpp", "pdhg_solve.cpp"]
 
 

@@ -63,6 +63,19 @@ class BatchResult(C.Structure):
     ]
 
 
+class UnrolledLayout(C.Structure):
+    """igaos_pdhg_unrolled_layout: sizes plus DEVICE addresses of the
+    concatenated CSR / CSC index arrays of a batch (differentiable layer)."""
+    _fields_ = [
+        ("count", C.c_int), ("precision", C.c_int), ("iterations", C.c_int),
+        ("checkpoint", C.c_int), ("ridge", C.c_double), ("max_m", C.c_int), ("max_n", C.c_int),
+        ("max_nnz", C.c_int64), ("total_m", C.c_int64), ("total_n", C.c_int64), ("total_nnz", C.c_int64),
+        ("row_off", C.c_void_p), ("col_off", C.c_void_p), ("nz_off", C.c_void_p),
+        ("ap", C.c_void_p), ("ai", C.c_void_p), ("cp", C.c_void_p), ("ci", C.c_void_p),
+        ("cperm", C.c_void_p),
+    ]
+
+
 _LIB = None
 
 
@@ -96,6 +109,15 @@ def lib():
             C.POINTER(BatchResult), _dp, _dp]
         # device-pointer entry point: every pointer is passed as an address
         L.igaos_pdhg_evaluate_noalloc.argtypes = [C.c_int, C.c_int] + [C.c_void_p] * 15
+        _lp = C.POINTER(UnrolledLayout)
+        L.igaos_pdhg_unrolled_checkpoint_elems.argtypes = [_lp]
+        L.igaos_pdhg_unrolled_checkpoint_elems.restype = C.c_int64
+        L.igaos_pdhg_unrolled_workspace_bytes.argtypes = [_lp]
+        L.igaos_pdhg_unrolled_workspace_bytes.restype = C.c_int64
+        L.igaos_pdhg_unrolled_steps.argtypes = [_lp, C.c_void_p, C.c_double, C.c_void_p,
+                                                C.c_void_p, C.c_void_p]
+        L.igaos_pdhg_unrolled_forward.argtypes = [_lp] + [C.c_void_p] * 13
+        L.igaos_pdhg_unrolled_backward.argtypes = [_lp] + [C.c_void_p] * 21
         _LIB = L
     return _LIB
 

@@ -240,6 +240,68 @@ int igaos_pdhg_evaluate_noalloc(int m, int n, const int* ap, const int* ai,
                                 const double* x, const double* y, double* out6,
                                 void* stream);
 
+/* ---- Differentiable LP layer: K unrolled PDHG iterations ----------------
+ * No counterpart in the reference (its engine has no gradient path). A batch
+ * of ridge-regularised LPs
+ *     min c^T x + ridge ||x||^2   s.t.  rmin <= A x <= rmax,  cl <= x <= cu
+ * is run for exactly K PDHG iterations with fixed steps (tau, sigma) per
+ * instance, from x0 = clamp(0, cl, cu), y0 = 0, in the reference's sign
+ * convention (reduced cost d = c + A^T y, src/pdhg/pdhg.cu:33-58):
+ *     x+ = clamp((x - tau (c + A^T y)) / (1 + 2 ridge tau), cl, cu)
+ *     t  = y + sigma A (2 x+ - x),   y+ = t - sigma clamp(t / sigma, rmin, rmax)
+ * The outputs are x_K, y_K and obj = c^T x_K + ridge ||x_K||^2. The backward
+ * entry is the exact reverse mode of those K iterations (clamps
+ * differentiated almost everywhere: the gradient passes where the argument is
+ * strictly inside the bounds), replaying each `checkpoint`-long segment from
+ * its stored iterate. Every pointer is a DEVICE pointer owned by the caller;
+ * value arrays hold float (precision IGAOS_PDHG_FP32) or double
+ * (IGAOS_PDHG_FP64). Work is enqueued on `stream`; nothing is allocated. */
+typedef struct igaos_pdhg_unrolled_layout {
+    int count;          /* instances (one CTA each) */
+    int precision;      /* IGAOS_PDHG_FP32 or IGAOS_PDHG_FP64 */
+    int iterations;     /* K >= 1 */
+    int checkpoint;     /* checkpoint interval >= 1 */
+    double ridge;       /* >= 0 */
+    int max_m, max_n;   /* largest instance (shared-memory sizing) */
+    int64_t max_nnz;    /* most nonzeros of one instance */
+    int64_t total_m, total_n, total_nnz;
+    const int* row_off; /* count+1 prefix offsets into the m-vectors */
+    const int* col_off; /* count+1 prefix offsets into the n-vectors */
+    const int* nz_off;  /* count+1 prefix offsets into the nonzeros */
+    const int* ap;      /* local row pointers, instance b at row_off[b] + b */
+    const int* ai;      /* local column indices, instance b at nz_off[b] */
+    const int* cp;      /* local column pointers, instance b at col_off[b] + b */
+    const int* ci;      /* local row index of each CSC entry, at nz_off[b] */
+    const int* cperm;   /* local CSR position of each CSC entry, at nz_off[b] */
+} igaos_pdhg_unrolled_layout;
+
+/* Elements (of the layout's type) of the checkpoint buffer the forward fills
+ * and the backward reads: ceil(K / checkpoint) * (total_n + total_m). */
+int64_t igaos_pdhg_unrolled_checkpoint_elems(const igaos_pdhg_unrolled_layout* L);
+/* Bytes of backward scratch: checkpoint * (total_n + total_m) * (size + 1). */
+int64_t igaos_pdhg_unrolled_workspace_bytes(const igaos_pdhg_unrolled_layout* L);
+/* Fixed steps per instance: tau = eta / omega, sigma = eta * omega with
+ * eta = 0.9 / ||A||_2 (power iteration, 100 products of A^T A). */
+int igaos_pdhg_unrolled_steps(const igaos_pdhg_unrolled_layout* L, const void* ax,
+                              double omega, void* tau, void* sigma, void* stream);
+/* x (total_n), y (total_m), obj (count), ckpt (checkpoint_elems). */
+int igaos_pdhg_unrolled_forward(const igaos_pdhg_unrolled_layout* L, const void* c,
+                                const void* cl, const void* cu, const void* rmin,
+                                const void* rmax, const void* ax, const void* tau,
+                                const void* sigma, void* x, void* y, void* obj,
+                                void* ckpt, void* stream);
+/* Gradients of <gx, x_K> + <gy, y_K> + <gobj, obj> with respect to c, cl,
+ * cu, rmin, rmax and the CSR values ax (each overwritten). gx, gy, gobj may
+ * be NULL (zero). x is the forward's x_K; ckpt its checkpoints; work holds
+ * workspace_bytes. Steps are constants (no gradient through tau, sigma). */
+int igaos_pdhg_unrolled_backward(const igaos_pdhg_unrolled_layout* L, const void* c,
+                                 const void* cl, const void* cu, const void* rmin,
+                                 const void* rmax, const void* ax, const void* tau,
+                                 const void* sigma, const void* ckpt, const void* x,
+                                 const void* gx, const void* gy, const void* gobj,
+                                 void* gc, void* gcl, void* gcu, void* grmin,
+                                 void* grmax, void* gax, void* work, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
