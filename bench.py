@@ -11,6 +11,11 @@ Also reported (extra keys): time to 1e-8 relative KKT on the small random LP
 (m=2,000, n=5,000) for FP32+refine vs plain FP64 and the CPU oracle, where
 all of them converge; the large LP is not solved to 1e-8 by either
 precision in a bench-sized budget (see --tol-probe).
+`time_to_1e-8_multicommodity_lp`: the same comparison on the 1.08M x 2.87M
+multicommodity-flow LP. `batched_small_lps`:
+4,096 uneven small LPs solved to 1e-6 in one persistent launch vs
+sequential single-LP solves. `differentiable_layer`: forward and adjoint
+backward through 1,000 unrolled iterations of 256 ridge-regularised LPs.
 
 value: SpMV GB/s -- algorithmic bytes of every fused A^T y / A xbar attempt
 of the solve divided by the solve's CUDA-event device time (checks, restarts
@@ -167,6 +172,70 @@ def run_reference(args, lp, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def batch_probe(capi, G, sample=24):
+    """The batch of 4,096 uneven LPs (m log-uniform in [20, 2000], n = 2.5 m,
+    1% density, box [0,5]; seed 0) solved to 1e-6 relative KKT in one
+    persistent launch, against sequential single-LP solves (FP64 engine, one
+    C-ABI call each with host buffers) of a seeded random sample of it."""
+    lps = G.config3(seed=0)
+    capi.solve_batch(lps[:64], tolerance=1e-6, max_iterations=200000, want_solutions=False)
+    t0 = time.perf_counter()
+    out = capi.solve_batch(lps, tolerance=1e-6, max_iterations=200000, want_solutions=False)
+    wall = time.perf_counter() - t0
+    st = {}
+    for r in out:
+        st[r["status_name"]] = st.get(r["status_name"], 0) + 1
+    idx = np.random.default_rng(0).choice(len(lps), sample, replace=False)
+    capi.solve_lp(lps[idx[0]], tolerance=1e-6, time_limit=60.0, precision="fp64")
+    seq = []
+    for i in idx:
+        t1 = time.perf_counter()
+        capi.solve_lp(lps[i], tolerance=1e-6, time_limit=60.0, precision="fp64")
+        seq.append(time.perf_counter() - t1)
+    kms = out[0]["kernel_time_ms"]
+    return {
+        "workload": "4096 uneven LPs (m 20..2000 log-uniform, n=2.5m, 1% density, box [0,5], "
+                    f"seed 0, sum nnz {sum(lp.nnz for lp in lps)}), tol 1e-6",
+        "status": st, "kernel_ms": kms, "call_s": wall,
+        "lps_per_s": len(lps) / wall, "lps_per_s_kernel": len(lps) / (kms / 1e3),
+        "sequential_sample": sample, "sequential_s_per_lp": statistics.mean(seq),
+        "sequential_lps_per_s": 1.0 / statistics.mean(seq),
+        "speedup_vs_sequential": (len(lps) / wall) * statistics.mean(seq),
+        "iterations_median": float(np.median([r["iterations"] for r in out])),
+    }
+
+
+def layer_probe(torch, G, reps=3):
+    """The differentiable layer on 256 ridge-regularised LPs (m=500, n=1000,
+    2% density, box [0,10], ridge 0.005; seed 0): FP32 forward through 1,000
+    PDHG iterations and the adjoint backward (checkpoints every 50),
+    CUDA-event time on the current stream."""
+    from igaos_gb300.layer import BatchPattern, UnrolledPDHG, pdhg_steps, stack_lps
+    lps = G.config4(seed=0, count=256)
+    P = BatchPattern.from_lps(lps, "cuda")
+    data = [t.clone().requires_grad_(True) for t in stack_lps(lps, torch.float32, "cuda")]
+    tau, sigma = pdhg_steps(P, data[5].detach())
+    fw, bw = [], []
+    for rep in range(reps + 2):
+        for t in data:
+            t.grad = None
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        torch.cuda.synchronize()
+        e[0].record()
+        x, y, obj = UnrolledPDHG.apply(*data, tau, sigma, P, 1000, 50, 0.005)
+        e[1].record()
+        (obj.sum() + x.sum()).backward()
+        e[2].record()
+        torch.cuda.synchronize()
+        if rep >= 2:
+            fw.append(e[0].elapsed_time(e[1]))
+            bw.append(e[1].elapsed_time(e[2]))
+    f, b = statistics.median(fw), statistics.median(bw)
+    return {"workload": "256 ridge LPs m=500 n=1000 2% density, K=1000, checkpoints every 50, "
+                        "FP32", "forward_ms": f, "backward_ms": b,
+            "lp_gradients_per_s": 256 / ((f + b) / 1e3)}
+
+
 def config_dict(lp, args):
     return {"workload": "large sparse LP (m=200k, n=500k, ~5.2M nnz, Zipf(1.5) column "
                         "degrees, |A_ij| log-uniform [1e-3,1e3], box [0,10]); one solve of "
@@ -190,6 +259,9 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the LP (testing only)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--no-c5", action="store_true", help="skip the multicommodity time-to-1e-8")
+    ap.add_argument("--no-batch", action="store_true", help="skip the batched-LP comparison")
+    ap.add_argument("--no-layer", action="store_true", help="skip the differentiable layer")
     ap.add_argument("--tol-probe", type=float, default=0.0,
                     help="also report time-to-tolerance probes within this many seconds")
     args = ap.parse_args()
@@ -274,6 +346,31 @@ def main():
                           threads=os.cpu_count() or 1)
         small["cpu_oracle_fp64"] = {"status": rr["status_name"], "s": rr["seconds"],
                                     "iterations": rr["iterations"], "cores": os.cpu_count()}
+    # Time to 1e-8 on the multicommodity-flow LP (300 x 300 grid, 8
+    # commodities: m=1,078,800, n=2,870,400, nnz=8,611,200), where both
+    # precisions reach it within the bench's budget.
+    c5 = None
+    if not args.no_c5 and rank == 0:
+        flp = G.config5(seed=0)
+        c5 = {"workload": f"multicommodity flow m={flp.m} n={flp.n} nnz={flp.nnz} (seed 0), "
+                          "tol 1e-8, device-resident, CUDA-event time"}
+        with capi.Problem(flp, device=local) as P:
+            for prec in ("fp32-refine", "fp64"):
+                r = P.solve(precision=prec, tolerance=1e-8, time_limit=240.0)
+                c5[prec] = {"status": r["status_name"], "s": r["device_time_ms"] / 1e3,
+                            "iterations": r["iterations"], "attempts": r["attempts"],
+                            "objective": r["objective"], "pinf": r["pinf"], "dinf": r["dinf"],
+                            "rel_gap": r["rel_gap"], "prow": r["prow"]}
+        if c5["fp64"]["status"] == c5["fp32-refine"]["status"] == "near-optimal":
+            c5["speedup_fp32_refine_vs_fp64"] = c5["fp64"]["s"] / c5["fp32-refine"]["s"]
+            c5["objective_rel_diff"] = abs(c5["fp64"]["objective"] - c5["fp32-refine"]["objective"]) / \
+                max(1.0, abs(c5["fp64"]["objective"]))
+    batch = None
+    if not args.no_batch and rank == 0:
+        batch = batch_probe(capi, G)
+    layer = None
+    if not args.no_layer and rank == 0:
+        layer = layer_probe(torch, G)
     probes = {}
     if args.tol_probe > 0:
         with capi.Problem(lp, device=local) as P:
@@ -320,6 +417,12 @@ def main():
     }
     if small:
         line["time_to_1e-8_small_lp"] = small
+    if c5:
+        line["time_to_1e-8_multicommodity_lp"] = c5
+    if batch:
+        line["batched_small_lps"] = batch
+    if layer:
+        line["differentiable_layer"] = layer
     if probes:
         line["time_to_tol"] = probes
     print(json.dumps(line), flush=True)
