@@ -172,37 +172,42 @@ def run_reference(args, lp, ws, rank):
     print(json.dumps(line), flush=True)
 
 
-def batch_probe(capi, G, sample=24):
+def batch_probe(capi, G, sample=24, count=4096, warm=True):
     """The batch of 4,096 uneven LPs (m log-uniform in [20, 2000], n = 2.5 m,
     1% density, box [0,5]; seed 0) solved to 1e-6 relative KKT in one
     persistent launch, against sequential single-LP solves (FP64 engine, one
-    C-ABI call each with host buffers) of a seeded random sample of it."""
-    lps = G.config3(seed=0)
-    capi.solve_batch(lps[:64], tolerance=1e-6, max_iterations=200000, want_solutions=False)
+    C-ABI call each with host buffers) of a seeded random sample of it
+    (`sample` = 0 skips them; `warm` = False makes the timed launch the
+    first one, for profiling)."""
+    lps = G.config3(seed=0, count=count)
+    if warm:
+        capi.solve_batch(lps[:64], tolerance=1e-6, max_iterations=200000, want_solutions=False)
     t0 = time.perf_counter()
     out = capi.solve_batch(lps, tolerance=1e-6, max_iterations=200000, want_solutions=False)
     wall = time.perf_counter() - t0
     st = {}
     for r in out:
         st[r["status_name"]] = st.get(r["status_name"], 0) + 1
-    idx = np.random.default_rng(0).choice(len(lps), sample, replace=False)
-    capi.solve_lp(lps[idx[0]], tolerance=1e-6, time_limit=60.0, precision="fp64")
-    seq = []
-    for i in idx:
-        t1 = time.perf_counter()
-        capi.solve_lp(lps[i], tolerance=1e-6, time_limit=60.0, precision="fp64")
-        seq.append(time.perf_counter() - t1)
     kms = out[0]["kernel_time_ms"]
-    return {
-        "workload": "4096 uneven LPs (m 20..2000 log-uniform, n=2.5m, 1% density, box [0,5], "
+    res = {
+        "workload": f"{count} uneven LPs (m 20..2000 log-uniform, n=2.5m, 1% density, box [0,5], "
                     f"seed 0, sum nnz {sum(lp.nnz for lp in lps)}), tol 1e-6",
         "status": st, "kernel_ms": kms, "call_s": wall,
         "lps_per_s": len(lps) / wall, "lps_per_s_kernel": len(lps) / (kms / 1e3),
-        "sequential_sample": sample, "sequential_s_per_lp": statistics.mean(seq),
-        "sequential_lps_per_s": 1.0 / statistics.mean(seq),
-        "speedup_vs_sequential": (len(lps) / wall) * statistics.mean(seq),
         "iterations_median": float(np.median([r["iterations"] for r in out])),
     }
+    if sample > 0:
+        idx = np.random.default_rng(0).choice(len(lps), min(sample, len(lps)), replace=False)
+        capi.solve_lp(lps[idx[0]], tolerance=1e-6, time_limit=60.0, precision="fp64")
+        seq = []
+        for i in idx:
+            t1 = time.perf_counter()
+            capi.solve_lp(lps[i], tolerance=1e-6, time_limit=60.0, precision="fp64")
+            seq.append(time.perf_counter() - t1)
+        res.update({"sequential_sample": len(idx), "sequential_s_per_lp": statistics.mean(seq),
+                    "sequential_lps_per_s": 1.0 / statistics.mean(seq),
+                    "speedup_vs_sequential": (len(lps) / wall) * statistics.mean(seq)})
+    return res
 
 
 def layer_probe(torch, G, reps=3):
@@ -259,6 +264,12 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the LP (testing only)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
+    ap.add_argument("--probe", choices=["batch", "layer"], default=None,
+                    help="run only that extra workload and print its JSON (profiling)")
+    ap.add_argument("--batch-count", type=int, default=4096,
+                    help="LPs in the batched workload (smaller for profiling)")
+    ap.add_argument("--batch-sample", type=int, default=24,
+                    help="sequential single-LP solves timed beside the batch (0: none)")
     ap.add_argument("--no-c5", action="store_true", help="skip the multicommodity time-to-1e-8")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-LP comparison")
     ap.add_argument("--no-layer", action="store_true", help="skip the differentiable layer")
@@ -283,6 +294,11 @@ def main():
         td.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     from igaos_gb300 import capi
+    if args.probe:  # one extra workload alone (profiling runs)
+        res = batch_probe(capi, G, sample=args.batch_sample, count=args.batch_count,
+                          warm=False) if args.probe == "batch" else layer_probe(torch, G)
+        print(json.dumps(res), flush=True)
+        return
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
     opts = dict(precision=args.precision, tolerance=1e-12, time_limit=1e9,
                 max_iterations=args.iters, device=local)
@@ -367,7 +383,7 @@ def main():
                 max(1.0, abs(c5["fp64"]["objective"]))
     batch = None
     if not args.no_batch and rank == 0:
-        batch = batch_probe(capi, G)
+        batch = batch_probe(capi, G, sample=args.batch_sample, count=args.batch_count)
     layer = None
     if not args.no_layer and rank == 0:
         layer = layer_probe(torch, G)

@@ -25,7 +25,10 @@ CLI = os.path.join(PKG, "igaos")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", INC, "-I", CSRC] + ARCH
-CU_SOURCES = ["engine.cu", "capi.cu", "batch.cu", "kkt_noalloc.cu", "unrolled.cu"]
+CU_SOURCES = ["engine.cu", "capi.cu", "batch.cu", "kkt_noalloc.cu", "unrolled.cu", "repair.cu"]
+# host code whose arithmetic must not be contracted into FMAs on any host
+# (dual repair: bit-identical to the reference host code on x86 and Arm)
+EXTRA_FLAGS = {"repair.cu": ["-Xcompiler", "-ffp-contract=off"]}
 CXX_HOST = ["model.cpp", "pdhg_solve.cpp"]
 
 
@@ -70,7 +73,7 @@ def build_lib(force=False, verbose=False, defines=(), out=None):
         o = os.path.join(objdir, src + ".o")
         objs.append(o)
         if force or _newer(o, [s] + deps):
-            jobs.append([_nvcc(), *NVFLAGS, *dflags, "-c", s, "-o", o])
+            jobs.append([_nvcc(), *NVFLAGS, *dflags, *EXTRA_FLAGS.get(src, []), "-c", s, "-o", o])
     with ThreadPoolExecutor(max_workers=max(1, len(jobs))) as ex:
         for r in ex.map(_run, jobs):
             if verbose and r.stderr:

@@ -104,6 +104,8 @@ def lib():
         L.igaos_pdhg_iterate.argtypes = [C.c_void_p, C.c_int, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]
         L.igaos_pdhg_evaluate.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.igaos_pdhg_spmv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp]
+        L.igaos_pdhg_dual_repair.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, _dp,
+                                             C.POINTER(C.c_int)]
         L.igaos_pdhg_solve_batch.argtypes = [
             C.c_int, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(Options),
             C.POINTER(BatchResult), _dp, _dp]
@@ -251,6 +253,16 @@ class Problem:
         out = np.zeros(6)
         _check(lib().igaos_pdhg_evaluate(self.h, _d(x), _d(y), _d(out)))
         return dict(zip(("pinf", "dinf", "gap", "op", "od", "prow"), out.tolist()))
+
+    def dual_repair(self, x, Ax, y_it, col_tol):
+        """(certified, y): the engine's dual repair at candidate x (A x = Ax)
+        from the dual estimate y_it, original units (m <= 4096)."""
+        a = [np.ascontiguousarray(v, np.float64) for v in (x, Ax, y_it)]
+        y = np.zeros(self.m)
+        ok = C.c_int(0)
+        _check(lib().igaos_pdhg_dual_repair(self.h, *[_d(v) for v in a], C.c_double(col_tol),
+                                            _d(y), C.byref(ok)))
+        return bool(ok.value), y
 
     def spmv(self, x, transpose=False, precision="fp64"):
         x = np.ascontiguousarray(x, np.float64)

@@ -266,6 +266,14 @@ int igaos_pdhg_evaluate(igaos_pdhg_problem* p, const double* x, const double* y,
     return guarded([&] { p->eng->evaluate(x, y, out6); });
 }
 
+int igaos_pdhg_dual_repair(igaos_pdhg_problem* p, const double* x, const double* Ax,
+                           const double* y_it, double col_tol, double* y, int* certified) {
+    if (!p || !p->eng || !x || !Ax || !y_it || !y || !certified)
+        return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (!(col_tol >= 0.0)) return fail(IGAOS_PDHG_ERR_INVALID, "col_tol must be >= 0");
+    return guarded([&] { *certified = p->eng->repair(x, Ax, y_it, col_tol, y) ? 1 : 0; });
+}
+
 int igaos_pdhg_spmv(igaos_pdhg_problem* p, int transpose, int precision, const double* x,
                     double* y) {
     if (!p || !p->eng || !x || !y) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");

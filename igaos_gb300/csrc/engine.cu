@@ -174,6 +174,23 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     base_.rmax = vec(rmax, pr_);
     base_.cmax = 0.0;
     for (int j = 0; j < n; ++j) base_.cmax = std::max(base_.cmax, std::fabs(c[j]));
+    if (m <= kRepairMaxRows) {  // host copy for dual repair (original units and order)
+        hlp_.reset(new HostLP());
+        HostLP& h = *hlp_;
+        h.m = m;
+        h.n = n;
+        h.ap.assign(ap, ap + m + 1);
+        h.ai.assign(ai, ai + nnz);
+        h.ax.assign(ax, ax + nnz);
+        h.cp.assign(cp, cp + n + 1);
+        h.ci.assign(ci, ci + nnz);
+        h.acx.assign(acx, acx + nnz);
+        h.c.assign(c, c + n);
+        h.cl.assign(cl, cl + n);
+        h.cu.assign(cu, cu + n);
+        h.rmin.assign(rmin, rmin + m);
+        h.rmax.assign(rmax, rmax + m);
+    }
     base_.sc = ar_.alloc<double>(n);
     base_.scl = ar_.alloc<double>(n);
     base_.scu = ar_.alloc<double>(n);
@@ -516,6 +533,96 @@ void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* 
 }
 
 // The reference iteration loop with its 64-iteration checks: termination,
+// Dual repair from the solve loop (src/pdhg/pdhg.cu:854-931): candidates are
+// the averaged iterate (its x and y) and the incumbent (its x with the
+// current y, as the reference takes them), tried when they pass pinf and
+// prow, have dinf <= 10 tol and no certified gap; col_tol tiers 1e-6 then
+// 1e-1; a repaired pair is accepted on pinf, prow and a finite gap <= tol.
+template <typename T>
+bool Engine::try_repair(const Vecs& v, int p, bool anch, const DevMetrics& ma,
+                        const DevMetrics* inc, double tol, int verbosity, long long k,
+                        LoopOut& out) {
+    Work<T>& w = work<T>();
+    for (int cnd = 1; cnd <= 2; ++cnd) {
+        const DevMetrics* t = cnd == 1 ? &ma : inc;
+        if (!t) break;
+        if (!(t->pinf <= tol && t->prow <= tol && t->dinf <= 10.0 * tol &&
+              !(std::isfinite(t->gap) && t->gap <= tol)))
+            continue;
+        if (verbosity > 1)
+            std::fprintf(stderr, "[pdhg-gb300] dual repair @k=%lld candidate %d (pinf %.2e prow %.2e "
+                                 "dinf %.2e)\n", k, cnd, t->pinf, t->prow, t->dinf);
+        // candidate in original units, device numbering
+        std::vector<double> hx(n), hy(m);
+        if (anch) {  // full FP64 iterates of this check (anchor + delta)
+            const double* sx = cnd == 1 ? anc_.xf[1] : anc_.xb;
+            const double* sy = cnd == 1 ? anc_.yf[1] : anc_.yf[0];
+            CU(cudaMemcpyAsync(hx.data(), sx, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+            CU(cudaMemcpyAsync(hy.data(), sy, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
+            CU(cudaStreamSynchronize(st_));
+            for (int j = 0; j < n; ++j) hx[j] *= hp_dc_[j];
+        } else {
+            unscale_cols<T>(cnd == 1 ? w.xavg[p] : w.xb, v, hx.data());
+            fetch_scaled<T>(cnd == 1 ? w.yavg[p] : w.y[p], m, hy.data());
+        }
+        for (int i = 0; i < m; ++i) hy[i] = 1.0 * hy[i] / hp_dr_[i];
+        std::vector<double> rx(n), ry_it(m), rAx(m, 0.0);
+        for (int j = 0; j < n; ++j) rx[pc_[j]] = hx[j];
+        for (int i = 0; i < m; ++i) ry_it[pr_[i]] = hy[i];
+        const HostLP& lp = *hlp_;
+        for (int j = 0; j < n; ++j)
+            for (int q = lp.cp[j]; q < lp.cp[j + 1]; ++q) rAx[lp.ci[q]] += lp.acx[q] * rx[j];
+        for (const double col_tol : {1e-6, 1e-1}) {
+            std::vector<double> ry;
+            if (!dual_repair(lp, rx.data(), rAx.data(), ry_it.data(), col_tol, ry)) continue;
+            std::vector<double> rd(n);
+            for (int j = 0; j < n; ++j) {
+                double d = lp.c[j];
+                for (int q = lp.cp[j]; q < lp.cp[j + 1]; ++q) d += lp.acx[q] * ry[lp.ci[q]];
+                rd[j] = d;
+            }
+            const HostMetrics hm = host_evaluate(lp, rx.data(), ry.data(), rAx.data(), rd.data());
+            if (verbosity > 1)
+                std::fprintf(stderr, "[pdhg-gb300] dual repair col_tol %.0e: gap %.3e\n", col_tol,
+                             hm.gap);
+            // a repaired pair is certified by pinf, prow and the gap: the gap
+            // is a valid weak-duality bound for any dual in the cone
+            if (hm.pinf <= tol && hm.prow <= tol && std::isfinite(hm.gap) && hm.gap <= tol) {
+                DevMetrics mt{};
+                mt.pinf = hm.pinf;
+                mt.dinf = hm.dinf;
+                mt.gap = hm.gap;
+                mt.op = hm.op;
+                mt.od = hm.od;
+                mt.prow = hm.prow;
+                mt.err = std::max(hm.pinf, std::max(hm.dinf, hm.gap));
+                mt.finite = 1;
+                out.last = mt;
+                out.last_is_avg = cnd == 1;
+                out.use_inc = false;
+                out.repaired = true;
+                out.rx = std::move(rx);
+                out.ry = std::move(ry);
+                out.status = IGAOS_STATUS_NEAR_OPTIMAL;
+                return true;
+            }
+        }
+    }
+    return false;
+}
+
+bool Engine::repair(const double* x, const double* Ax, const double* y_it, double col_tol,
+                    double* y) {
+    if (!hlp_)
+        throw CudaError(IGAOS_PDHG_ERR_INVALID,
+                        "dual repair keeps a dense m x m factor: limited to m <= 4096 rows");
+    std::vector<double> out;
+    const bool ok = dual_repair(*hlp_, x, Ax, y_it, col_tol, out);
+    if ((int)out.size() == m) std::memcpy(y, out.data(), sizeof(double) * m);
+    else for (int i = 0; i < m; ++i) y[i] = std::numeric_limits<double>::quiet_NaN();
+    return ok;
+}
+
 // incumbent, rollback, restart and primal weight (src/pdhg/pdhg.cu:665-1085).
 template <typename T>
 LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
@@ -547,6 +654,7 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
 
     double epoch_kkt = -1.0, prev_cand = kInf;
     long long epoch_start = 0, last_rollback = 0;
+    long long next_repair = 5000, repair_spacing = 2000;  // src/pdhg/pdhg.cu:741-743
     bool have_pe = false, have_last = false, have_inc = false;
     double inc_op = 0.0;
     DevMetrics inc{};
@@ -585,6 +693,15 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
                              out.last.pinf, out.last.dinf, out.last.gap);
             if (passes(mc)) { out.last = mc; out.last_is_avg = false; out.status = IGAOS_STATUS_NEAR_OPTIMAL; break; }
             if (passes(ma)) { out.last = ma; out.last_is_avg = true; out.status = IGAOS_STATUS_NEAR_OPTIMAL; break; }
+            // dual repair of a converged candidate whose dual bound is not
+            // certified (src/pdhg/pdhg.cu:854-931), on the reference's schedule
+            if (hlp_ && k_done >= 5000 && k_done >= next_repair) {
+                next_repair = k_done + repair_spacing;
+                repair_spacing = std::min(repair_spacing * 3, 30000LL);
+                if (try_repair<T>(v, p, anch, ma, have_inc ? &inc : nullptr, o.tol, o.verbosity,
+                                  k_done, out))
+                    break;
+            }
             // incumbent (src/pdhg/pdhg.cu:937-958)
             int inc_src = -1;
             for (int cnd = 0; cnd < 2; ++cnd) {
@@ -845,6 +962,15 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
         for (int j = 0; j < n; ++j) x[pc_[j]] = hx[j];  // already in original units
     if (y)
         for (int i = 0; i < m; ++i) y[pr_[i]] = 1.0 * hy[i] / hp_dr_[i];
+    emit_repaired(out, r, x, y);
+}
+
+// A pair certified by dual repair is the answer as the repair produced it.
+void Engine::emit_repaired(const LoopOut& out, igaos_pdhg_result& r, double* x, double* y) {
+    if (!out.repaired) return;
+    fill_message(r, "converged: residuals @tol, duality gap certified by dual repair");
+    if (x) std::memcpy(x, out.rx.data(), sizeof(double) * n);
+    if (y) std::memcpy(y, out.ry.data(), sizeof(double) * m);
 }
 
 // ------------------------------------------------------- numbering helpers
@@ -1135,5 +1261,6 @@ void Engine::solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, dou
         for (int j = 0; j < n; ++j) x[pc_[j]] = hx[j] * hp_dc_[j];
     if (y)
         for (int i = 0; i < m; ++i) y[pr_[i]] = 1.0 * hy[i] / hp_dr_[i];
+    emit_repaired(out, r, x, y);
 }
 }  // namespace igx

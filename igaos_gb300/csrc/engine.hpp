@@ -10,6 +10,9 @@
 
 #include "igaos_pdhg.h"
 #include "device.cuh"
+#include "repair.hpp"
+
+#include <memory>
 
 namespace igx {
 
@@ -109,6 +112,8 @@ struct LoopOut {
     double eta = 0, omega = 0;
     int parity = 0;
     bool numeric_failure = false;
+    bool repaired = false;            // certified by dual repair: answer in rx, ry
+    std::vector<double> rx, ry;       // original units, caller's numbering
 };
 
 class Engine {
@@ -133,6 +138,10 @@ class Engine {
                  double* yavg, double* axc, double* st6);
     void evaluate(const double* x, const double* y, double* out6);
     void spmv(int transpose, int precision, const double* x, double* y);
+    // dual repair on the host copy of the LP (m <= kRepairMaxRows); original
+    // units, caller's numbering
+    bool repair(const double* x, const double* Ax, const double* y_it, double col_tol,
+                double* y);
 
    private:
     int device_ = 0;
@@ -192,6 +201,12 @@ class Engine {
     template <typename T> void fetch_scaled(const T* src, int len, double* dst);
     template <typename T> void unscale_cols(const T* xs, const Vecs& v, double* host_out);
     // anchored (FP32 + FP64 refinement) iterations
+    // host copy of the original LP for dual repair (small m only)
+    std::unique_ptr<HostLP> hlp_;
+    void emit_repaired(const LoopOut& out, igaos_pdhg_result& r, double* x, double* y);
+    template <typename T>
+    bool try_repair(const Vecs& v, int p, bool anch, const DevMetrics& ma, const DevMetrics* inc,
+                    double tol, int verbosity, long long k, LoopOut& out);
     Anchor anc_{};
     Vecs av_{};
     bool have_anchor_ = false;

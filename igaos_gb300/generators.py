@@ -294,3 +294,32 @@ def mixed_bounds_lp(m: int, n: int, extra_nnz: int, seed: int) -> LPData:
     lp.rmin, lp.rmax = rmin, rmax
     lp.meta = dict(seed=seed)
     return lp
+
+
+def free_cost_lp(m: int, n: int, extra_nnz: int, seed: int) -> LPData:
+    """The bound and row structure of mixed_bounds_lp, with costs that give
+    free and one-sided columns nonzero reduced-cost pressure: c = -A^T y* + s
+    for a dual point y* in the row cone (y* >= 0 on <= rows, <= 0 on >=
+    rows) and s = 0 (free), s >= 0 (lower bound only), s <= 0 (upper bound
+    only), s ~ N(0,1) (boxed, fixed). Primal feasible around x*, dual
+    feasible at y*, so bounded. The dual objective stays -inf until the
+    iterate's reduced costs of the columns with an infinite bound are within
+    1e-8 (1 + max|c|) of their sign -- the case dual_repair certifies."""
+    lp = mixed_bounds_lp(m, n, extra_nnz, seed)
+    rng = np.random.default_rng(seed + 7919)
+    fin_lo, fin_hi = np.isfinite(lp.rmin), np.isfinite(lp.rmax)
+    ys = rng.standard_normal(m)
+    ys[fin_hi & ~fin_lo] = np.abs(ys[fin_hi & ~fin_lo])
+    ys[fin_lo & ~fin_hi] = -np.abs(ys[fin_lo & ~fin_hi])
+    ys[~fin_lo & ~fin_hi] = 0.0
+    aty = np.zeros(n)
+    rows = np.repeat(np.arange(m), np.diff(lp.ap))
+    np.add.at(aty, lp.ai, lp.ax * ys[rows])
+    lo_f, up_f = np.isfinite(lp.cl), np.isfinite(lp.cu)
+    s = rng.standard_normal(n)
+    s[~lo_f & ~up_f] = 0.0
+    s[lo_f & ~up_f] = np.abs(s[lo_f & ~up_f])
+    s[~lo_f & up_f] = -np.abs(s[~lo_f & up_f])
+    lp.c = -aty + s
+    lp.name = f"freecost-{seed}"
+    return lp

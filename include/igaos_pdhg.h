@@ -173,6 +173,19 @@ int igaos_pdhg_iterate(igaos_pdhg_problem* p, int precision, int64_t iters,
                        double* x, double* y, double* xavg, double* yavg,
                        double* axcur, double* state6);
 
+/* Dual repair (the reference's dual_repair, src/pdhg/pdhg.cu:257-448): for a
+ * primal candidate x with Ax = A x (ORIGINAL units, the caller's numbering)
+ * and a dual estimate y_it, alternating projections onto {A_J^T y = -c_J}
+ * (columns strictly inside their bounds by col_tol), the sign half-spaces of
+ * columns with an infinite bound and the row cone. *certified = 1 when a
+ * dual with a finite duality gap was found (y = the smallest-gap one), else
+ * 0 (y = the point of least sign violation, or NaN when the dense
+ * factorisation failed). Dense m x m normal equations on the host: problems
+ * with m > 4096 return IGAOS_PDHG_ERR_INVALID. The solve loop runs the same
+ * step from k = 5000 on (spacing 2000, x3 up to 30000), as the reference. */
+int igaos_pdhg_dual_repair(igaos_pdhg_problem* p, const double* x, const double* Ax,
+                           const double* y_it, double col_tol, double* y, int* certified);
+
 /* FP64 KKT metrics of (x, y) given in ORIGINAL units, evaluated on the
  * device (the fused pass replacing src/pdhg/pdhg.cu:173-254 + :698-733).
  * out6 = {pinf, dinf, gap, op, od, prow}. */

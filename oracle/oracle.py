@@ -250,8 +250,8 @@ def iterate(lp: LP, sd, state: dict, iters: int, threads=1):
 
 
 def pdhg_solve(lp: LP, tolerance=1e-4, time_limit=120.0, max_iterations=500000,
-               threads=1, check_period=64):
-    o = orc_options(time_limit, tolerance, max_iterations, check_period, threads, 0)
+               threads=1, check_period=64, verbosity=0):
+    o = orc_options(time_limit, tolerance, max_iterations, check_period, threads, verbosity)
     r = orc_result()
     x = np.zeros(lp.n); y = np.zeros(lp.m)
     s = lp.as_c()
@@ -283,6 +283,27 @@ def ref_evaluate(rmin, rmax, cl, cu, c, x, y, Ax, d):
     out = np.zeros(6)
     _ref_eval().ref_evaluate(len(arrs[0]), len(arrs[2]), *[_d(a) for a in arrs], _d(out))
     return dict(zip(("pinf", "dinf", "gap", "op", "od", "prow"), out.tolist()))
+
+
+def dual_repair(lp: LP, x, Ax, y_it, col_tol):
+    """The oracle's restatement of the reference dual_repair: (certified, y)."""
+    y = np.zeros(lp.m)
+    s = lp.as_c()
+    ok = lib().orc_dual_repair(C.byref(s), _d(f64(x)), _d(f64(Ax)), _d(f64(y_it)),
+                               C.c_double(col_tol), _d(y))
+    return bool(ok), y
+
+
+def ref_dual_repair(lp: LP, x, Ax, y_it, col_tol):
+    """The reference's own dual_repair (compiled from its sources): (certified, y)."""
+    y = np.zeros(lp.m)
+    L = _ref_eval()
+    L.ref_dual_repair.restype = C.c_int
+    ok = L.ref_dual_repair(lp.m, lp.n, _i(lp.ap), _i(lp.ai), _d(lp.ax), _i(lp.cp), _i(lp.ci),
+                           _d(lp.acx), _d(lp.c), _d(lp.cl), _d(lp.cu), _d(lp.rmin),
+                           _d(lp.rmax), _d(f64(x)), _d(f64(Ax)), _d(f64(y_it)),
+                           C.c_double(col_tol), _d(y))
+    return bool(ok), y
 
 
 def ref_counting_sort(ti, tj, tv, rows, cols):

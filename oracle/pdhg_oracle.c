@@ -18,6 +18,7 @@
 #include "pdhg_oracle.h"
 
 #include <math.h>
+#include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
 #include <time.h>
@@ -504,6 +505,11 @@ int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
         orc_metrics mc, ma;
         METRICS_OF(st.x, st.y, mc);
         METRICS_OF(st.xavg, st.yavg, ma);
+        if (opt->verbosity > 1)
+            fprintf(stderr, "[oracle] k=%lld cur pinf=%.2e dinf=%.2e gap=%.2e prow=%.2e | "
+                            "avg pinf=%.2e dinf=%.2e gap=%.2e prow=%.2e\n",
+                    (long long)k, mc.pinf, mc.dinf, mc.gap, mc.prow, ma.pinf, ma.dinf, ma.gap,
+                    ma.prow);
         const double ec = metrics_finite(&mc) ? metrics_err(&mc) : ORC_INF;
         const double ea = metrics_finite(&ma) ? metrics_err(&ma) : ORC_INF;
         last = (ec <= ea) ? mc : ma;
@@ -647,4 +653,182 @@ int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
     free(dr); free(dc); free(sax); free(sacx);
     free(sc); free(scl); free(scu); free(srmin); free(srmax);
     return 0;
+}
+
+/* ------------------------------------------------------------ dual repair
+ * reference src/pdhg/pdhg.cu:257-448. Host code of the reference: no FMA. */
+static int chol_factor(double* G, int nr) {
+    for (int i = 0; i < nr; ++i)
+        for (int j = 0; j <= i; ++j) {
+            double s = G[(size_t)i * nr + j];
+            for (int t = 0; t < j; ++t) s -= G[(size_t)i * nr + t] * G[(size_t)j * nr + t];
+            if (i == j) {
+                if (!(s > 0)) return 0;
+                G[(size_t)i * nr + i] = sqrt(s);
+            } else {
+                G[(size_t)i * nr + j] = s / G[(size_t)j * nr + j];
+            }
+        }
+    return 1;
+}
+
+static void chol_apply(const double* G, int nr, double* rhs) {
+    for (int i = 0; i < nr; ++i) {
+        double s = rhs[i];
+        for (int t = 0; t < i; ++t) s -= G[(size_t)i * nr + t] * rhs[t];
+        rhs[i] = s / G[(size_t)i * nr + i];
+    }
+    for (int i = nr - 1; i >= 0; --i) {
+        double s = rhs[i];
+        for (int t = i + 1; t < nr; ++t) s -= G[(size_t)t * nr + i] * rhs[t];
+        rhs[i] = s / G[(size_t)i * nr + i];
+    }
+}
+
+static double btol(double tol, double b) { return tol * (1.0 + (isfinite(b) ? fabs(b) : 0.0)); }
+
+static double col_d(const orc_lp* lp, int j, const double* y) {
+    double dj = lp->c[j];
+    for (int p = lp->cp[j]; p < lp->cp[j + 1]; ++p) dj += lp->acx[p] * y[lp->ci[p]];
+    return dj;
+}
+
+int orc_dual_repair(const orc_lp* lp, const double* x, const double* Ax,
+                    const double* y_it, double col_tol, double* y) {
+    const int m = lp->m, n = lp->n;
+    double* lo = (double*)malloc(sizeof(double) * (size_t)m);
+    double* hi = (double*)malloc(sizeof(double) * (size_t)m);
+    for (int i = 0; i < m; ++i) {
+        const int fl = isfinite(lp->rmin[i]), fh = isfinite(lp->rmax[i]);
+        if (fl && fh) { lo[i] = -ORC_INF; hi[i] = ORC_INF; }
+        else if (fh) { lo[i] = 0.0; hi[i] = ORC_INF; }
+        else if (fl) { lo[i] = -ORC_INF; hi[i] = 0.0; }
+        else { lo[i] = hi[i] = 0.0; }
+    }
+    /* column types: 0 d>=0 (cu=inf), 1 d<=0 (cl=-inf), 2 d==0, 3 free */
+    char* ct = (char*)malloc((size_t)n);
+    double* cn2 = (double*)calloc((size_t)n, sizeof(double));
+    int* ji = (int*)malloc(sizeof(int) * (size_t)(n > 0 ? n : 1));
+    int k = 0;
+    for (int j = 0; j < n; ++j) {
+        const int up_inf = !isfinite(lp->cu[j]), lo_inf = !isfinite(lp->cl[j]);
+        ct[j] = (up_inf && lo_inf) ? 2 : up_inf ? 0 : lo_inf ? 1 : 3;
+        for (int p = lp->cp[j]; p < lp->cp[j + 1]; ++p) cn2[j] += lp->acx[p] * lp->acx[p];
+        if (x[j] - lp->cl[j] > btol(col_tol, lp->cl[j]) &&
+            lp->cu[j] - x[j] > btol(col_tol, lp->cu[j]))
+            ji[k++] = j;
+    }
+    double* G = NULL;
+    int ok = 1;
+    if (k > 0) {
+        G = (double*)calloc((size_t)m * (size_t)m, sizeof(double));
+        for (int jj = 0; jj < k; ++jj) {
+            const int j = ji[jj];
+            for (int p = lp->cp[j]; p < lp->cp[j + 1]; ++p) {
+                const int i1 = lp->ci[p];
+                const double v1 = lp->acx[p];
+                for (int q = lp->cp[j]; q < lp->cp[j + 1]; ++q)
+                    G[(size_t)i1 * m + lp->ci[q]] += v1 * lp->acx[q];
+            }
+        }
+        double tr = 0.0;
+        for (int i = 0; i < m; ++i) tr += G[(size_t)i * m + i];
+        double ridge = tr > 0 ? 1e-10 * tr / m : 1e-14;
+        double* Gc = (double*)malloc(sizeof(double) * (size_t)m * (size_t)m);
+        ok = 0;
+        for (int att = 0; att < 6 && !ok; ++att) {
+            memcpy(Gc, G, sizeof(double) * (size_t)m * (size_t)m);
+            for (int i = 0; i < m; ++i) Gc[(size_t)i * m + i] += ridge;
+            ok = chol_factor(Gc, m);
+            if (ok) memcpy(G, Gc, sizeof(double) * (size_t)m * (size_t)m);
+            else ridge = ridge > 0 ? ridge * 100.0 : 1e-14;
+        }
+        free(Gc);
+    }
+    int have = 0;
+    if (!ok) {
+        for (int i = 0; i < m; ++i) y[i] = NAN;
+    } else {
+        double best_gap = ORC_INF, best_viol = ORC_INF;
+        double* d = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+        double* rhs = (double*)malloc(sizeof(double) * (size_t)m);
+        double* yc = (double*)malloc(sizeof(double) * (size_t)m);
+        double* ybest = (double*)malloc(sizeof(double) * (size_t)m);
+        double* yviol = (double*)malloc(sizeof(double) * (size_t)m);
+        for (int anch = 0; anch < 2; ++anch) {
+            for (int i = 0; i < m; ++i) {
+                yc[i] = anch == 0 ? y_it[i] : 0.0;
+                yc[i] = smin(smax(yc[i], lo[i]), hi[i]);
+            }
+            double vref = -1.0;
+            for (int it = 0; it < 300; ++it) {
+                if (k > 0) {  /* affine projection e = G^-1 (-A_J d_J) */
+                    memset(rhs, 0, sizeof(double) * (size_t)m);
+                    double res2 = 0.0;
+                    for (int jj = 0; jj < k; ++jj) {
+                        const int j = ji[jj];
+                        const double dj = col_d(lp, j, yc);
+                        res2 += dj * dj;
+                        if (dj != 0.0)
+                            for (int p = lp->cp[j]; p < lp->cp[j + 1]; ++p)
+                                rhs[lp->ci[p]] -= lp->acx[p] * dj;
+                    }
+                    if (res2 > 0.0) {
+                        chol_apply(G, m, rhs);
+                        for (int i = 0; i < m; ++i) yc[i] += rhs[i];
+                    }
+                }
+                /* Hildreth half-space fixes of the sign-constrained columns */
+                for (int j = 0; j < n; ++j) {
+                    if (ct[j] == 3 || cn2[j] == 0.0) continue;
+                    const double dj = col_d(lp, j, yc);
+                    double v = 0.0;
+                    if (ct[j] == 0 && dj < 0.0) v = -dj;
+                    else if (ct[j] == 1 && dj > 0.0) v = -dj;
+                    else if (ct[j] == 2 && dj != 0.0) v = -dj;
+                    if (v != 0.0) {
+                        const double st = v / cn2[j];
+                        for (int p = lp->cp[j]; p < lp->cp[j + 1]; ++p) yc[lp->ci[p]] += st * lp->acx[p];
+                    }
+                }
+                for (int i = 0; i < m; ++i) yc[i] = smin(smax(yc[i], lo[i]), hi[i]);
+                for (int j = 0; j < n; ++j) d[j] = col_d(lp, j, yc);
+                if (it % 25 == 0) {
+                    double viol = 0.0;
+                    for (int j = 0; j < n; ++j) {
+                        if (ct[j] == 3) continue;
+                        double v = 0.0;
+                        if (ct[j] == 0 && d[j] < 0) v = -d[j];
+                        else if (ct[j] == 1 && d[j] > 0) v = d[j];
+                        else if (ct[j] == 2) v = fabs(d[j]);
+                        viol = smax(viol, v);
+                    }
+                    for (int i = 0; i < m; ++i) {
+                        double v = 0.0;
+                        if (lo[i] == 0.0 && hi[i] == 0.0) v = fabs(yc[i]);
+                        else if (hi[i] == 0.0 && yc[i] > 0) v = yc[i];
+                        else if (lo[i] == 0.0 && yc[i] < 0) v = -yc[i];
+                        viol = smax(viol, v);
+                    }
+                    if (it == 25) vref = viol;
+                    if (viol < best_viol) {
+                        best_viol = viol;
+                        memcpy(yviol, yc, sizeof(double) * (size_t)m);
+                    }
+                    if (it == 100 && vref > 0 && viol > 0.25 * vref) break;
+                }
+                orc_metrics t;
+                orc_evaluate(m, n, lp->rmin, lp->rmax, lp->cl, lp->cu, lp->c, x, yc, Ax, d, &t);
+                if (isfinite(t.gap) && t.gap < best_gap) {
+                    best_gap = t.gap;
+                    memcpy(ybest, yc, sizeof(double) * (size_t)m);
+                    have = 1;
+                }
+            }
+        }
+        memcpy(y, have ? ybest : yviol, sizeof(double) * (size_t)m);
+        free(d); free(rhs); free(yc); free(ybest); free(yviol);
+    }
+    free(lo); free(hi); free(ct); free(cn2); free(ji); free(G);
+    return have;
 }

@@ -126,6 +126,13 @@ int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
 
 void orc_default_options(orc_options* o);
 
+/* reference src/pdhg/pdhg.cu:257-448: certifiable dual near y_it for the
+ * primal candidate x (original units, Ax = A x). Returns 1 when a dual with a
+ * finite gap was found (y = the best-gap one), else 0 (y = the point of least
+ * sign violation, or NaN when the dense factorisation failed). */
+int orc_dual_repair(const orc_lp* lp, const double* x, const double* Ax,
+                    const double* y_it, double col_tol, double* y);
+
 #ifdef __cplusplus
 }
 #endif

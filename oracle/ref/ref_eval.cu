@@ -82,4 +82,34 @@ void ref_fetch_model(int* ap, int* ai, double* ax, int* cp, int* ci,
     std::memcpy(rmax, M.rmax.data(), sizeof(double) * M.rmax.size());
 }
 
+// The reference's dual_repair (internal to the pdhg.cu unit) on a model
+// given by arrays; returns its certified flag, y receives its output.
+int ref_dual_repair(int m, int n, const int* ap, const int* ai, const double* ax,
+                    const int* cp, const int* ci, const double* acx, const double* c,
+                    const double* cl, const double* cu, const double* rmin,
+                    const double* rmax, const double* x, const double* Ax,
+                    const double* y_it, double col_tol, double* y) {
+    igaos::io::Model M;
+    M.m = m;
+    M.n = n;
+    const int nnz = ap[m];
+    M.ap.assign(ap, ap + m + 1);
+    M.ai.assign(ai, ai + nnz);
+    M.ax.assign(ax, ax + nnz);
+    M.cp.assign(cp, cp + n + 1);
+    M.ci.assign(ci, ci + nnz);
+    M.acx.assign(acx, acx + nnz);
+    M.c.assign(c, c + n);
+    M.cl.assign(cl, cl + n);
+    M.cu.assign(cu, cu + n);
+    M.rmin.assign(rmin, rmin + m);
+    M.rmax.assign(rmax, rmax + m);
+    std::vector<double> vx(x, x + n), vAx(Ax, Ax + m), vy(y_it, y_it + m), out;
+    const bool ok = igaos::pdhg::dual_repair(M, vx, vAx, vy, col_tol, out);
+    // the reference leaves its output untouched when the factorisation fails
+    if ((int)out.size() == m) std::memcpy(y, out.data(), sizeof(double) * m);
+    else for (int i = 0; i < m; ++i) y[i] = std::numeric_limits<double>::quiet_NaN();
+    return ok ? 1 : 0;
+}
+
 }  // extern "C"

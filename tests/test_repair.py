@@ -1,0 +1,98 @@
+"""Dual repair (reference src/pdhg/pdhg.cu:257-448, called at :854-931).
+
+* The oracle's restatement and the engine's host implementation both
+  reproduce the reference's own dual_repair bit for bit on the golden cases
+  (tests/golden/dual_repair_cases.npz, made by make_repair_golden.py from the
+  reference compiled from its sources): certified flag and dual vector.
+* In a solve, LPs whose free and one-sided columns keep the dual bound at
+  -inf are certified by the repair step, with the optimum of an independent
+  LP solver.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from igaos_gb300 import generators as G
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+GOLD = np.load(os.path.join(HERE, "golden", "dual_repair_cases.npz"))
+
+
+def cases():
+    for k in range(int(GOLD["count"])):
+        m, n, e, seed = (int(v) for v in GOLD[f"lp_{k}"])
+        yield k, G.free_cost_lp(m, n, e, seed), {f: GOLD[f"{f}_{k}"] for f in
+                                                  ("x", "Ax", "y_it", "tol", "ok", "y")}
+
+
+def test_oracle_restatement_matches_reference_golden():
+    from oracle import oracle as O
+    for k, lp, g in cases():
+        ok, y = O.dual_repair(O.lp_from(lp), g["x"], g["Ax"], g["y_it"], float(g["tol"]))
+        assert ok == bool(g["ok"]), k
+        assert np.array_equal(y, g["y"], equal_nan=True), (k, np.abs(y - g["y"]).max())
+
+
+def test_golden_cases_cover_both_outcomes():
+    oks = [bool(g["ok"]) for _, _, g in cases()]
+    assert any(oks) and not all(oks)
+
+
+@pytest.mark.gpu
+def test_engine_repair_matches_reference_golden(native):
+    from igaos_gb300 import capi
+    for k, lp, g in cases():
+        with capi.Problem(lp) as P:
+            ok, y = P.dual_repair(g["x"], g["Ax"], g["y_it"], float(g["tol"]))
+        assert ok == bool(g["ok"]), k
+        assert np.array_equal(y, g["y"], equal_nan=True), (k, np.abs(y - g["y"]).max())
+
+
+@pytest.mark.gpu
+def test_engine_repair_refuses_large_m(native):
+    from igaos_gb300 import capi
+    lp = G.random_lp(4100, 4200, 4300, 0)
+    with capi.Problem(lp) as P:
+        with pytest.raises(capi.EngineError, match="m <= 4096"):
+            P.dual_repair(np.zeros(lp.n), np.zeros(lp.m), np.zeros(lp.m), 1e-6)
+
+
+def linprog_optimum(lp):
+    scipy_opt = pytest.importorskip("scipy.optimize")
+    import scipy.sparse as sp
+    A = sp.csr_matrix((lp.ax, lp.ai, lp.ap), shape=(lp.m, lp.n))
+    fin_hi, fin_lo = np.isfinite(lp.rmax), np.isfinite(lp.rmin)
+    eq = fin_hi & fin_lo & (lp.rmin == lp.rmax)
+    ub_hi = fin_hi & ~eq
+    ub_lo = fin_lo & ~eq
+    A_ub = sp.vstack([A[ub_hi], -A[ub_lo]])
+    b_ub = np.concatenate([lp.rmax[ub_hi], -lp.rmin[ub_lo]])
+    bounds = [(None if not np.isfinite(l) else l, None if not np.isfinite(u) else u)
+              for l, u in zip(lp.cl, lp.cu)]
+    r = scipy_opt.linprog(lp.c, A_ub=A_ub, b_ub=b_ub, A_eq=A[eq], b_eq=lp.rmin[eq],
+                          bounds=bounds, method="highs")
+    assert r.status == 0
+    return r.fun
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("precision", ["fp64", "fp32-refine"])
+@pytest.mark.parametrize("tol", [1e-2, 1e-4])
+def test_solve_with_infinite_bounds(native, precision, tol):
+    """The dual bound of this LP stays -inf until the reduced costs of its
+    free columns are within 1e-8 of zero (about 31k-37k iterations). With
+    FP32 + refinement at 1e-2 the repair step certifies the k = 13,120
+    candidate (gap 4.5e-4) instead; the FP64 run's scheduled candidates
+    (k = 5,056 / 7,104 / 13,120) repair only to gaps of ~4e-2 and it
+    terminates by itself."""
+    from igaos_gb300 import capi
+    lp = G.free_cost_lp(80, 200, 400, 3)
+    ref = linprog_optimum(lp)
+    r = capi.solve_lp(lp, tolerance=tol, time_limit=60.0, precision=precision, verbosity=2)
+    print(precision, tol, r["iterations"], r["message"])
+    assert r["status_name"] == "near-optimal", r
+    assert abs(r["objective"] - ref) <= 10 * tol * max(1.0, abs(ref)), (r["objective"], ref)
+    assert max(r["pinf"], r["prow"], r["rel_gap"]) <= tol
+    if tol == 1e-2 and precision == "fp32-refine":
+        assert "dual repair" in r["message"] and r["iterations"] < 20000, r
