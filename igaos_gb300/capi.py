@@ -60,6 +60,7 @@ class BatchResult(C.Structure):
         ("pinf", C.c_double), ("dinf", C.c_double), ("rel_gap", C.c_double),
         ("prow", C.c_double), ("iterations", C.c_int64), ("attempts", C.c_int64),
         ("restarts", C.c_int64), ("kernel_time_ms", C.c_double), ("total_time_ms", C.c_double),
+        ("instance_time_ms", C.c_double),
     ]
 
 

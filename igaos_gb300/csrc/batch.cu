@@ -28,6 +28,11 @@
 namespace igx {
 namespace {
 
+// threads per instance (one CTA): big instances are latency-bound per
+// iteration, so the whole CTA's width goes to one LP
+constexpr int kBT = 512;
+constexpr int kBW = kBT / 32;
+
 struct BatchDesc {
     int m, n, nnz, pad;
     long long ap_off, cp_off, nz_off, row_off, col_off;
@@ -37,7 +42,14 @@ struct BatchOut {
     int status, pad;
     double objective, pinf, dinf, gap, prow;
     long long iterations, attempts, restarts;
+    long long ns;  // device time of the instance (global timer)
 };
+
+__device__ __forceinline__ long long global_ns() {
+    long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
 
 constexpr int kFacTab = 1 << 16;  // tabulated 1 - k^-0.3, 1 + k^-0.6
 
@@ -67,20 +79,20 @@ struct BatchArgs {
 };
 
 struct BatchShared {
-    Acc<float> acc[kWarps * 4];
-    double dred[kWarps * 8];
-    float fmax_[kWarps * 8];
-    int part[kThreads];
+    Acc<float> acc[kBW * 4];
+    double dred[kBW * 8];
+    float fmax_[kBW * 8];
+    int part[kBT];
     int inst;
     float tau, sigma, w;
     int parity, accept;
     long long kdone;
 };
 
-// ---- block-level helpers (all 256 threads call them) --------------------
+// ---- block-level helpers (every thread of the CTA calls them) -----------
 template <int NV>
 __device__ void bmerge(BatchShared& sh, Acc<float> (&v)[NV]) {
-    block_merge<float, NV>(v, sh.acc);
+    block_merge<float, NV, kBW>(v, sh.acc);
 }
 
 template <int NV>
@@ -98,7 +110,7 @@ __device__ void bmaxf(BatchShared& sh, float (&v)[NV]) {
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
             float s = sh.fmax_[q];
-            for (int k = 1; k < kWarps; ++k) s = fmaxf(s, sh.fmax_[k * NV + q]);
+            for (int k = 1; k < kBW; ++k) s = fmaxf(s, sh.fmax_[k * NV + q]);
             v[q] = s;
         }
     __syncthreads();
@@ -107,7 +119,7 @@ __device__ void bmaxf(BatchShared& sh, float (&v)[NV]) {
 // exclusive block scan of cnt[0..len) into out[0..len], out[len] = total
 __device__ void bscan(BatchShared& sh, const int* cnt, int* out, int len) {
     const int t = threadIdx.x;
-    const int per = (len + kThreads - 1) / kThreads;
+    const int per = (len + kBT - 1) / kBT;
     const int b = min(len, t * per), e = min(len, b + per);
     int s = 0;
     for (int j = b; j < e; ++j) s += cnt[j];
@@ -115,7 +127,7 @@ __device__ void bscan(BatchShared& sh, const int* cnt, int* out, int len) {
     __syncthreads();
     if (t == 0) {
         int run = 0;
-        for (int k = 0; k < kThreads; ++k) {
+        for (int k = 0; k < kBT; ++k) {
             const int v = sh.part[k];
             sh.part[k] = run;
             run += v;
@@ -214,7 +226,7 @@ __device__ __forceinline__ double full_x(const Inst& I, int j, float dx) {
 // with A~_ij = a_ij dc_j / dr_i formed in FP64 from the FP64 values.
 __device__ void anchor_data(Inst& I) {
     const int t = threadIdx.x;
-    for (int i = t; i < I.m; i += kThreads) {
+    for (int i = t; i < I.m; i += kBT) {
         const double dri = I.dr[i];
         double s = 0.0;
         for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) {
@@ -226,7 +238,7 @@ __device__ void anchor_data(Inst& I) {
         I.srmax[i] = (float)(I.rmax[i] / dri - s);
         I.yh32[i] = (float)I.yh[i];
     }
-    for (int j = t; j < I.n; j += kThreads) {
+    for (int j = t; j < I.n; j += kBT) {
         const double dcj = I.dc[j];
         double s = 0.0;
         for (int p = I.cp[j]; p < I.cp[j + 1]; ++p) {
@@ -245,22 +257,22 @@ __device__ void anchor_data(Inst& I) {
 __device__ void setup(BatchShared& sh, Inst& I, float& eta0, float& omega0) {
     const int t = threadIdx.x, m = I.m, n = I.n;
     // CSC by counting sort; each column's entries ordered by row afterwards
-    for (int j = t; j < n; j += kThreads) I.cnt[j] = 0;
+    for (int j = t; j < n; j += kBT) I.cnt[j] = 0;
     __syncthreads();
-    for (int i = t; i < m; i += kThreads)
+    for (int i = t; i < m; i += kBT)
         for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) atomicAdd(&I.cnt[I.ai[p]], 1);
     __syncthreads();
     bscan(sh, I.cnt, I.cp, n);
-    for (int j = t; j < n; j += kThreads) I.cnt[j] = I.cp[j];
+    for (int j = t; j < n; j += kBT) I.cnt[j] = I.cp[j];
     __syncthreads();
-    for (int i = t; i < m; i += kThreads)
+    for (int i = t; i < m; i += kBT)
         for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) {
             const int q = atomicAdd(&I.cnt[I.ai[p]], 1);
             I.ci[q] = i;
             I.cax64[q] = I.axd[p];
         }
     __syncthreads();
-    for (int j = t; j < n; j += kThreads) {  // insertion sort by row index
+    for (int j = t; j < n; j += kBT) {  // insertion sort by row index
         const int b = I.cp[j], e = I.cp[j + 1];
         for (int q = b + 1; q < e; ++q) {
             const int r = I.ci[q];
@@ -277,18 +289,18 @@ __device__ void setup(BatchShared& sh, Inst& I, float& eta0, float& omega0) {
         for (int q = b; q < e; ++q) I.cax[q] = (float)I.cax64[q];
     }
     // Ruiz, 10 sweeps (FP32 factors)
-    for (int i = t; i < m; i += kThreads) I.dr[i] = 1.f;
-    for (int j = t; j < n; j += kThreads) I.dc[j] = 1.f;
+    for (int i = t; i < m; i += kBT) I.dr[i] = 1.f;
+    for (int j = t; j < n; j += kBT) I.dc[j] = 1.f;
     __syncthreads();
     for (int sweep = 0; sweep < 10; ++sweep) {
-        for (int i = t; i < m; i += kThreads) {
+        for (int i = t; i < m; i += kBT) {
             float mx = 0.f;
             for (int p = I.ap[i]; p < I.ap[i + 1]; ++p)
                 mx = fmaxf(mx, fabsf(I.ax[p]) * I.dc[I.ai[p]] / I.dr[i]);
             if (mx > 0.f && isfinite(mx)) I.dr[i] *= sqrtf(mx);
         }
         __syncthreads();
-        for (int j = t; j < n; j += kThreads) {
+        for (int j = t; j < n; j += kBT) {
             float mx = 0.f;
             for (int p = I.cp[j]; p < I.cp[j + 1]; ++p)
                 mx = fmaxf(mx, fabsf(I.cax[p]) / I.dr[I.ci[p]] * I.dc[j]);
@@ -298,13 +310,13 @@ __device__ void setup(BatchShared& sh, Inst& I, float& eta0, float& omega0) {
     }
     // scaled FP32 matrix; initial weight from the scaled cost and row bounds
     Acc<float> nq[2];
-    for (int i = t; i < m; i += kThreads) {
+    for (int i = t; i < m; i += kBT) {
         for (int p = I.ap[i]; p < I.ap[i + 1]; ++p) I.sax[p] = I.ax[p] * I.dc[I.ai[p]] / I.dr[i];
         const float lo = (float)I.rmin[i] / I.dr[i], hi = (float)I.rmax[i] / I.dr[i];
         const float q = isfinite(hi) ? hi : (isfinite(lo) ? lo : 0.f);
         nq[1].add(q, q);
     }
-    for (int j = t; j < n; j += kThreads) {
+    for (int j = t; j < n; j += kBT) {
         for (int p = I.cp[j]; p < I.cp[j + 1]; ++p) I.scax[p] = I.cax[p] * I.dc[j] / I.dr[I.ci[p]];
         const float cs = (float)I.c[j] * I.dc[j];
         nq[0].add(cs, cs);
@@ -316,15 +328,15 @@ __device__ void setup(BatchShared& sh, Inst& I, float& eta0, float& omega0) {
     }
     // power iteration for ||A~||_2^2
     const float v0 = rsqrtf((float)n);
-    for (int j = t; j < n; j += kThreads) I.vt[j] = v0;
+    for (int j = t; j < n; j += kBT) I.vt[j] = v0;
     __syncthreads();
     __shared__ float s_norm;
     for (int it = 0; it < 31; ++it) {
-        for (int i = t; i < m; i += kThreads) I.mt[i] = row_dot(I.ap, I.ai, I.sax, I.vt, i).result();
+        for (int i = t; i < m; i += kBT) I.mt[i] = row_dot(I.ap, I.ai, I.sax, I.vt, i).result();
         __syncthreads();
         if (it == 30) break;
         Acc<float> nrm[1];
-        for (int j = t; j < n; j += kThreads) {
+        for (int j = t; j < n; j += kBT) {
             const float wv = row_dot(I.cp, I.ci, I.scax, I.mt, j).result();
             I.xbar[j] = wv;
             nrm[0].add(wv, wv);
@@ -334,11 +346,11 @@ __device__ void setup(BatchShared& sh, Inst& I, float& eta0, float& omega0) {
         __syncthreads();
         const float nw = s_norm;
         if (!(nw > 1e-30f)) break;
-        for (int j = t; j < n; j += kThreads) I.vt[j] = I.xbar[j] / nw;
+        for (int j = t; j < n; j += kBT) I.vt[j] = I.xbar[j] / nw;
         __syncthreads();
     }
     Acc<float> na[1];
-    for (int i = t; i < m; i += kThreads) na[0].add(I.mt[i], I.mt[i]);
+    for (int i = t; i < m; i += kBT) na[0].add(I.mt[i], I.mt[i]);
     bmerge<1>(sh, na);
     if (t == 0) {
         double lam = na[0].result_d();
@@ -358,7 +370,7 @@ __device__ BMetrics metrics(BatchShared& sh, Inst& I, const float* xs, const flo
                             double cmax) {
     const int t = threadIdx.x;
     double r4[4] = {0.0, 0.0, 0.0, 0.0};  // pv, pa, prow, ymax
-    for (int i = t; i < I.m; i += kThreads) {
+    for (int i = t; i < I.m; i += kBT) {
         const double Ax = (I.axh[i] + row_dot(I.ap, I.ai, I.sax, xs, i).result_d()) * (double)I.dr[i];
         const double lo = I.rmin[i], hi = I.rmax[i];
         const double vi = smax(lo - Ax, Ax - hi);
@@ -370,7 +382,7 @@ __device__ BMetrics metrics(BatchShared& sh, Inst& I, const float* xs, const flo
         r4[2] = smax(r4[2], smax(0.0, vi) / (1.0 + scv));
         r4[3] = smax(r4[3], fabs((I.yh[i] + (double)ys[i]) / (double)I.dr[i]));
     }
-    block_max<4>(r4, sh.dred);
+    block_max<4, kBW>(r4, sh.dred);
     __shared__ double s_r[4];
     if (t == 0)
         for (int q = 0; q < 4; ++q) s_r[q] = r4[q];
@@ -379,7 +391,7 @@ __device__ BMetrics metrics(BatchShared& sh, Inst& I, const float* xs, const flo
     const double dz = 1e-8 * (1.0 + cmax);
     double mx[2] = {0.0, 0.0};  // dv, unbounded
     double sm[3] = {0.0, 0.0, 0.0};  // op, od (columns), od (rows)
-    for (int j = t; j < I.n; j += kThreads) {
+    for (int j = t; j < I.n; j += kBT) {
         const double aty = I.atyh[j] + row_dot(I.cp, I.ci, I.scax, ys, j).result_d();
         const double d = I.c[j] + aty / (double)I.dc[j];
         const double lo = I.cl[j], hi = I.cu[j];
@@ -401,7 +413,7 @@ __device__ BMetrics metrics(BatchShared& sh, Inst& I, const float* xs, const flo
             else if (-d > dz) mx[1] = 1.0;
         }
     }
-    for (int i = t; i < I.m; i += kThreads) {
+    for (int i = t; i < I.m; i += kBT) {
         const double yv = (I.yh[i] + (double)ys[i]) / (double)I.dr[i];
         if (yv > yz) {
             if (isfinite(I.rmax[i])) sm[2] -= yv * I.rmax[i];
@@ -411,8 +423,8 @@ __device__ BMetrics metrics(BatchShared& sh, Inst& I, const float* xs, const flo
             else mx[1] = 1.0;
         }
     }
-    block_max<2>(mx, sh.dred);
-    block_sum<3>(sm, sh.dred);
+    block_max<2, kBW>(mx, sh.dred);
+    block_sum<3, kBW>(sm, sh.dred);
     __shared__ BMetrics s_m;
     if (t == 0) {
         BMetrics mt;
@@ -433,22 +445,23 @@ __device__ BMetrics metrics(BatchShared& sh, Inst& I, const float* xs, const flo
 
 // ---- one LP --------------------------------------------------------------
 __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& d, int b) {
+    const long long t_begin = global_ns();
     Inst I = make_inst(a, d);
     const int t = threadIdx.x, m = I.m, n = I.n;
     __shared__ float s_eta0, s_omega0;
     __shared__ double s_cmax;
-    for (int j = t; j < n; j += kThreads) I.xh[j] = I.pesx[j] = 0.0;
-    for (int i = t; i < m; i += kThreads) I.yh[i] = I.pesy[i] = 0.0;
+    for (int j = t; j < n; j += kBT) I.xh[j] = I.pesx[j] = 0.0;
+    for (int i = t; i < m; i += kBT) I.yh[i] = I.pesy[i] = 0.0;
     setup(sh, I, s_eta0, s_omega0);
     anchor_data(I);
     {
         double cm[1] = {0.0};
-        for (int j = t; j < n; j += kThreads) cm[0] = smax(cm[0], fabs(I.c[j]));
-        block_max<1>(cm, sh.dred);
+        for (int j = t; j < n; j += kBT) cm[0] = smax(cm[0], fabs(I.c[j]));
+        block_max<1, kBW>(cm, sh.dred);
         if (t == 0) s_cmax = cm[0];
     }
-    for (int j = t; j < n; j += kThreads) I.x[0][j] = I.xa[0][j] = 0.f;
-    for (int i = t; i < m; i += kThreads) I.y[0][i] = I.ya[0][i] = I.axc[0][i] = 0.f;
+    for (int j = t; j < n; j += kBT) I.x[0][j] = I.xa[0][j] = 0.f;
+    for (int i = t; i < m; i += kBT) I.y[0][i] = I.ya[0][i] = I.axc[0][i] = 0.f;
     // controller state (thread 0)
     __shared__ double s_epoch_kkt, s_prev_cand, s_omega, s_eta;
     __shared__ long long s_k, s_hn, s_epoch_start, s_attempts, s_restarts;
@@ -488,7 +501,7 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
         const float tau = sh.tau, sigma = sh.sigma, w = sh.w;
         Acc<float> dots[3];
         // primal step fused with A^T y (thread per column), on the deltas
-        for (int j = t; j < n; j += kThreads) {
+        for (int j = t; j < n; j += kBT) {
             const float g = I.sc[j] + row_dot(I.cp, I.ci, I.scax, I.y[p], j).result();
             const float xv = I.x[p][j];
             const float xn = fminf(fmaxf(fmaf(-tau, g, xv), I.scl[j]), I.scu[j]);
@@ -502,7 +515,7 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
         __syncthreads();
         // dual step fused with A xbar (thread per row); the projection acts
         // on the full value, so the anchor enters its argument
-        for (int i = t; i < m; i += kThreads) {
+        for (int i = t; i < m; i += kBT) {
             const float ab = row_dot(I.ap, I.ai, I.sax, I.xbar, i).result();
             const float yv = I.y[p][i];
             const float tt = fmaf(sigma, ab, yv);
@@ -609,19 +622,19 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
                 const float* dxs = s_avg_better ? I.xa[pc] : I.x[pc];
                 const float* dys = s_avg_better ? I.ya[pc] : I.y[pc];
                 double dn[2] = {0.0, 0.0};
-                for (int j = t; j < n; j += kThreads) {
+                for (int j = t; j < n; j += kBT) {
                     const double nx = full_x(I, j, dxs[j]);
                     const double dd = nx - I.pesx[j];
                     dn[0] = fma(dd, dd, dn[0]);
                     I.pesx[j] = nx;
                 }
-                for (int i = t; i < m; i += kThreads) {
+                for (int i = t; i < m; i += kBT) {
                     const double ny = I.yh[i] + (double)dys[i];
                     const double dd = ny - I.pesy[i];
                     dn[1] = fma(dd, dd, dn[1]);
                     I.pesy[i] = ny;
                 }
-                block_sum<2>(dn, sh.dred);
+                block_sum<2, kBW>(dn, sh.dred);
                 if (t == 0 && s_have_pe) {
                     const double dxn = dn[0], dyn = dn[1];
                     if (dxn > 1e-24 && dyn > 1e-24) {
@@ -631,11 +644,11 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
                 }
                 if (t == 0) s_have_pe = 1;
                 // the new anchor is the restart point (held in pes)
-                for (int j = t; j < n; j += kThreads) {
+                for (int j = t; j < n; j += kBT) {
                     I.xh[j] = I.pesx[j];
                     I.x[pc][j] = I.xa[pc][j] = 0.f;
                 }
-                for (int i = t; i < m; i += kThreads) {
+                for (int i = t; i < m; i += kBT) {
                     I.yh[i] = I.pesy[i];
                     I.y[pc][i] = I.ya[pc][i] = I.axc[pc][i] = 0.f;
                 }
@@ -651,13 +664,13 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
     double* xo = a.x_out ? a.x_out + d.col_off : nullptr;
     double* yo = a.y_out ? a.y_out + d.row_off : nullptr;
     if (xo)
-        for (int j = t; j < n; j += kThreads) {
+        for (int j = t; j < n; j += kBT) {
             const float xv = xs[j];
             xo[j] = xv == I.scl[j] ? I.cl[j]
                                    : (xv == I.scu[j] ? I.cu[j] : (I.xh[j] + (double)xv) * (double)I.dc[j]);
         }
     if (yo)
-        for (int i = t; i < m; i += kThreads) yo[i] = (I.yh[i] + (double)ys[i]) / (double)I.dr[i];
+        for (int i = t; i < m; i += kBT) yo[i] = (I.yh[i] + (double)ys[i]) / (double)I.dr[i];
     if (t == 0) {
         BatchOut o;
         o.status = s_status;
@@ -670,12 +683,13 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
         o.iterations = s_k - 1;
         o.attempts = s_attempts;
         o.restarts = s_restarts;
+        o.ns = global_ns() - t_begin;
         a.out[b] = o;
     }
     __syncthreads();
 }
 
-__global__ void __launch_bounds__(kThreads) k_batch(BatchArgs a) {
+__global__ void __launch_bounds__(kBT) k_batch(BatchArgs a) {
     __shared__ BatchShared sh;
     for (;;) {
         if (threadIdx.x == 0) sh.inst = (int)atomicAdd(a.queue, 1u);
@@ -829,13 +843,13 @@ extern "C" int igaos_pdhg_solve_batch(int count, const int* m, const int* n, con
         int sms = 0, dev = 0, per_sm = 0;
         CU(cudaGetDevice(&dev));
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kThreads, 0));
+        CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_batch, kBT, 0));
         const int grid = std::max(1, std::min(count, sms * std::max(1, per_sm)));
         cudaEvent_t e0, e1;
         CU(cudaEventCreate(&e0));
         CU(cudaEventCreate(&e1));
         CU(cudaEventRecord(e0, st));
-        k_batch<<<grid, kThreads, 0, st>>>(A);
+        k_batch<<<grid, kBT, 0, st>>>(A);
         CU(cudaGetLastError());
         CU(cudaEventRecord(e1, st));
         std::vector<BatchOut> out(count);
@@ -864,6 +878,7 @@ extern "C" int igaos_pdhg_solve_batch(int count, const int* m, const int* n, con
             r.restarts = q.restarts;
             r.kernel_time_ms = kms;
             r.total_time_ms = wall;
+            r.instance_time_ms = 1e-6 * (double)q.ns;
         }
     } catch (const CudaError& e) {
         return igx_set_error(e.code, e.what());

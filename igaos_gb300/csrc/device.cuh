@@ -161,9 +161,9 @@ __device__ __forceinline__ double warp_max(double v) {
     return v;
 }
 
-// Block-wide sum of NV values; result valid in thread 0. `sh` needs
-// kWarps * NV doubles. Fixed reduction tree -> deterministic.
-template <int NV>
+// Block-wide sum of NV values over NW warps (blockDim.x = 32 NW); result valid
+// in thread 0. `sh` needs NW * NV doubles. Fixed reduction tree -> deterministic.
+template <int NV, int NW = kWarps>
 __device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -177,7 +177,7 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
             double s = 0.0;
-            for (int k = 0; k < kWarps; ++k) s += sh[k * NV + q];
+            for (int k = 0; k < NW; ++k) s += sh[k * NV + q];
             v[q] = s;
         }
     }
@@ -208,7 +208,7 @@ __device__ __forceinline__ void block_sum_t(T (&v)[NV], T* sh) {
     __syncthreads();
 }
 
-template <int NV>
+template <int NV, int NW = kWarps>
 __device__ __forceinline__ void block_max(double (&v)[NV], double* sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -222,7 +222,7 @@ __device__ __forceinline__ void block_max(double (&v)[NV], double* sh) {
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
             double s = sh[q];
-            for (int k = 1; k < kWarps; ++k) s = smax(s, sh[k * NV + q]);
+            for (int k = 1; k < NW; ++k) s = smax(s, sh[k * NV + q]);
             v[q] = s;
         }
     }
@@ -231,7 +231,7 @@ __device__ __forceinline__ void block_max(double (&v)[NV], double* sh) {
 
 // Block-wide fixed-order merge of NV compensated accumulators; result in
 // thread 0. `sh` needs kWarps * NV entries.
-template <typename T, int NV>
+template <typename T, int NV, int NW = kWarps>
 __device__ __forceinline__ void block_merge(Acc<T> (&v)[NV], Acc<T>* sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -246,7 +246,7 @@ __device__ __forceinline__ void block_merge(Acc<T> (&v)[NV], Acc<T>* sh) {
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
             Acc<T> s = sh[q];
-            for (int k = 1; k < kWarps; ++k) s.merge(sh[k * NV + q]);
+            for (int k = 1; k < NW; ++k) s.merge(sh[k * NV + q]);
             v[q] = s;
         }
     }

@@ -209,6 +209,7 @@ typedef struct igaos_pdhg_batch_result {
     int64_t iterations, attempts, restarts;
     double kernel_time_ms;   /* the whole batch's persistent kernel (same for all) */
     double total_time_ms;    /* the whole call: upload, kernel, download */
+    double instance_time_ms; /* this instance, from its CTA taking it to its answer */
 } igaos_pdhg_batch_result;
 
 /* Solves `count` independent LPs of uneven sizes in one persistent kernel
