@@ -9,6 +9,7 @@
 #include <cstdio>
 #include <cstring>
 #include <limits>
+#include <thread>
 #include <type_traits>
 
 namespace igx {
@@ -83,24 +84,47 @@ static Sched upload_sched(Arena& ar, const int* ptr, int rows, int resident_ctas
 
 // CSR of the row-permuted matrix with renumbered indices; each row keeps its
 // entries in their original order (the same summation order).
+// The entries are gathered by the host's threads over row ranges of equal
+// size (the output does not depend on the split).
 static void permute_csr(int rows, const int* ptr, const int* idx, const double* val,
                         const std::vector<int>& rnew2old, const std::vector<int>& iold2new,
-                        std::vector<int>& P, std::vector<int>& I, std::vector<double>& V) {
+                        std::vector<int>& P, std::unique_ptr<int[]>& I,
+                        std::unique_ptr<double[]>& V) {
     P.assign(rows + 1, 0);
     for (int r = 0; r < rows; ++r) {
         const int o = rnew2old[r];
         P[r + 1] = P[r] + (ptr[o + 1] - ptr[o]);
     }
-    I.resize(P[rows]);
-    V.resize(P[rows]);
-    for (int r = 0; r < rows; ++r) {
-        const int o = rnew2old[r];
-        int q = P[r];
-        for (int p = ptr[o]; p < ptr[o + 1]; ++p, ++q) {
-            I[q] = iold2new[idx[p]];
-            V[q] = val[p];
+    const long long nnz = P[rows];
+    I.reset(new int[std::max<long long>(1, nnz)]);
+    V.reset(new double[std::max<long long>(1, nnz)]);
+    auto fill = [&](int r0, int r1) {
+        for (int r = r0; r < r1; ++r) {
+            const int o = rnew2old[r];
+            int q = P[r];
+            for (int p = ptr[o]; p < ptr[o + 1]; ++p, ++q) {
+                I[q] = iold2new[idx[p]];
+                V[q] = val[p];
+            }
         }
+    };
+    const int nt = nnz < (1 << 20) ? 1
+                                   : (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+    if (nt == 1) {
+        fill(0, rows);
+        return;
     }
+    std::vector<std::thread> pool;
+    int r0 = 0;
+    for (int t = 1; t <= nt; ++t) {
+        const long long target = nnz * t / nt;
+        const int r1 = t == nt ? rows
+                               : (int)(std::lower_bound(P.begin(), P.end(), (int)target) - P.begin());
+        const int hi = std::max(r0, std::min(rows, r1));
+        pool.emplace_back(fill, r0, hi);
+        r0 = hi;
+    }
+    for (auto& th : pool) th.join();
 }
 
 static std::vector<int> inverse(const std::vector<int>& p) {
@@ -135,8 +159,9 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     ipr_ = inverse(pr_);
     ipc_ = inverse(pc_);
     {
-        std::vector<int> P, I;
-        std::vector<double> V;
+        std::vector<int> P;
+        std::unique_ptr<int[]> I;
+        std::unique_ptr<double[]> V;
         ap_ = ar_.alloc<int>(m + 1);
         ai_ = ar_.alloc<int>(nnz);
         ax_ = ar_.alloc<double>(nnz);
@@ -147,16 +172,16 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         acx32_ = ar_.alloc<float>(nnz);
         permute_csr(m, ap, ai, ax, pr_, ipc_, P, I, V);
         CU(cudaMemcpy(ap_, P.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(ai_, I.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(ax_, V.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(ai_, I.get(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(ax_, V.get(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
         int sms = 0;
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
         const int resident = std::max(1, sms) * kHotCtasPerSm;
         sA_ = upload_sched(ar_, P.data(), m, resident);
         permute_csr(n, cp, ci, acx, pc_, ipr_, P, I, V);
         CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(ci_, I.data(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
-        CU(cudaMemcpy(acx_, V.data(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(ci_, I.get(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
+        CU(cudaMemcpy(acx_, V.get(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
         sAT_ = upload_sched(ar_, P.data(), n, resident);
     }
     // vectors
@@ -272,8 +297,8 @@ void Engine::setup_scaling() {
     k_fill<<<grid_for(m), kThreads, 0, st_>>>(m, 1.0, dr_);
     k_fill<<<grid_for(n), kThreads, 0, st_>>>(n, 1.0, dc_);
     for (int sweep = 0; sweep < 10; ++sweep) {
-        k_ruiz_rows<<<gr_full, kThreads, 0, st_>>>(m, ap_, ai_, ax_, dc_, dr_);
-        k_ruiz_cols<<<gc_full, kThreads, 0, st_>>>(n, cp_, ci_, acx_, dr_, dc_);
+        k_ruiz_rows<<<sA_.ctas, kThreads, 0, st_>>>(sA_.view(), ap_, ai_, ax_, dc_, dr_);
+        k_ruiz_cols<<<sAT_.ctas, kThreads, 0, st_>>>(sAT_.view(), cp_, ci_, acx_, dr_, dc_);
     }
     k_fix_scale<<<grid_for(m), kThreads, 0, st_>>>(m, dr_);
     k_fix_scale<<<grid_for(n), kThreads, 0, st_>>>(n, dc_);

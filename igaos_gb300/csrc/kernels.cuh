@@ -254,36 +254,51 @@ __global__ void __launch_bounds__(kThreads, kHotCtasPerSm)
 }
 
 // -------------------------------------------------------- Ruiz equilibration
-// src/pdhg/pdhg.cu:474-481: dr_i *= sqrt(max_j |a_ij| dc_j / dr_i). A warp per
-// row; max is order-free, the division and sqrt are IEEE, so the result is
-// bit-identical to the sequential host loop.
-__global__ void k_ruiz_rows(int m, const int* __restrict__ ap, const int* __restrict__ ai,
-                            const double* __restrict__ ax, const double* __restrict__ dc,
-                            double* __restrict__ dr) {
+// src/pdhg/pdhg.cu:474-481: dr_i *= sqrt(max_j |a_ij| dc_j / dr_i), and
+// :482-490: dc_j /= sqrt(max_i |a_ij| / dr_i * dc_j), over the warp schedule
+// of the length-sorted matrix (G lanes per row). The max is order-free and
+// the division and sqrt are IEEE, so the factors are bit-identical to the
+// sequential host loops.
+__global__ void __launch_bounds__(kThreads) k_ruiz_rows(WarpSched ws, const int* __restrict__ ap,
+                                                          const int* __restrict__ ai,
+                                                          const double* __restrict__ ax,
+                                                          const double* __restrict__ dc,
+                                                          double* __restrict__ dr) {
     const int lane = threadIdx.x & 31;
-    const int i = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (i >= m) return;
-    const double dri = dr[i];
-    double mx = 0.0;
-    for (int p = ap[i] + lane; p < ap[i + 1]; p += 32)
-        mx = smax(mx, __ddiv_rn(__dmul_rn(fabs(ax[p]), dc[ai[p]]), dri));
-    mx = warp_max(mx);
-    if (lane == 0 && (mx > 0) && isfinite(mx)) dr[i] = __dmul_rn(dri, __dsqrt_rn(mx));
+    for (int w = blockIdx.x * kWarps + (threadIdx.x >> 5); w < ws.nwarps; w += gridDim.x * kWarps) {
+        const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
+        const int lg = __ldg(ws.lg + w), G = 1 << lg, gl = lane & (G - 1);
+        const int i = r0 + (lane >> lg);
+        double mx = 0.0, dri = 1.0;
+        if (i < r1) {
+            dri = dr[i];
+            for (int p = ap[i] + gl; p < ap[i + 1]; p += G)
+                mx = smax(mx, __ddiv_rn(__dmul_rn(fabs(ax[p]), dc[ai[p]]), dri));
+        }
+        for (int o = G >> 1; o > 0; o >>= 1) mx = smax(mx, __shfl_xor_sync(0xffffffffu, mx, o, G));
+        if (i < r1 && gl == 0 && (mx > 0) && isfinite(mx)) dr[i] = __dmul_rn(dri, __dsqrt_rn(mx));
+    }
 }
 
-// src/pdhg/pdhg.cu:482-490: dc_j /= sqrt(max_i |a_ij| / dr_i * dc_j).
-__global__ void k_ruiz_cols(int n, const int* __restrict__ cp, const int* __restrict__ ci,
-                            const double* __restrict__ acx, const double* __restrict__ dr,
-                            double* __restrict__ dc) {
+__global__ void __launch_bounds__(kThreads) k_ruiz_cols(WarpSched ws, const int* __restrict__ cp,
+                                                          const int* __restrict__ ci,
+                                                          const double* __restrict__ acx,
+                                                          const double* __restrict__ dr,
+                                                          double* __restrict__ dc) {
     const int lane = threadIdx.x & 31;
-    const int j = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    if (j >= n) return;
-    const double dcj = dc[j];
-    double mx = 0.0;
-    for (int p = cp[j] + lane; p < cp[j + 1]; p += 32)
-        mx = smax(mx, __dmul_rn(__ddiv_rn(fabs(acx[p]), dr[ci[p]]), dcj));
-    mx = warp_max(mx);
-    if (lane == 0 && (mx > 0) && isfinite(mx)) dc[j] = __ddiv_rn(dcj, __dsqrt_rn(mx));
+    for (int w = blockIdx.x * kWarps + (threadIdx.x >> 5); w < ws.nwarps; w += gridDim.x * kWarps) {
+        const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
+        const int lg = __ldg(ws.lg + w), G = 1 << lg, gl = lane & (G - 1);
+        const int j = r0 + (lane >> lg);
+        double mx = 0.0, dcj = 1.0;
+        if (j < r1) {
+            dcj = dc[j];
+            for (int p = cp[j] + gl; p < cp[j + 1]; p += G)
+                mx = smax(mx, __dmul_rn(__ddiv_rn(fabs(acx[p]), dr[ci[p]]), dcj));
+        }
+        for (int o = G >> 1; o > 0; o >>= 1) mx = smax(mx, __shfl_xor_sync(0xffffffffu, mx, o, G));
+        if (j < r1 && gl == 0 && (mx > 0) && isfinite(mx)) dc[j] = __ddiv_rn(dcj, __dsqrt_rn(mx));
+    }
 }
 
 __global__ void k_fill(int n, double v, double* __restrict__ out) {
