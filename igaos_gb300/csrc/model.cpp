@@ -1,13 +1,17 @@
 // MPS reader and CSR/CSC builder (see model.hpp).
 #include "model.hpp"
 
+#include <cctype>
+#include <charconv>
 #include <cmath>
+#include <cstdint>
+#include <cstdio>
 #include <cstdlib>
-#include <fstream>
+#include <cstring>
 #include <limits>
 #include <stdexcept>
 #include <string_view>
-#include <unordered_map>
+#include <system_error>
 
 namespace igaos::io {
 
@@ -54,39 +58,156 @@ void split(std::string_view s, std::vector<std::string_view>& tok) {
     }
 }
 
+// std::stod semantics (leading number; std::invalid_argument if none,
+// std::out_of_range if it does not fit), on the fast path of std::from_chars
+// (correctly rounded, as strtod): plain decimal tokens, an optional leading
+// '+'; anything from_chars does not take whole goes to std::stod itself.
 double num(std::string_view v) {
-    // std::stod semantics (leading number, throws if none)
-    std::string s(v);
-    return std::stod(s);
+    const char* b = v.data();
+    const char* e = b + v.size();
+    if (e - b > 1 && *b == '+' && (std::isdigit((unsigned char)b[1]) || b[1] == '.')) ++b;
+    double out = 0.0;
+    const auto r = std::from_chars(b, e, out, std::chars_format::general);
+    // normal finite values taken whole; zeros only when spelled with zero
+    // digits (underflow and subnormals are std::stod's range errors)
+    const bool whole = r.ec == std::errc() && r.ptr == e;
+    if (whole && std::isfinite(out) &&
+        (out == 0.0 ? v.find_first_of("123456789") == std::string_view::npos
+                    : std::fabs(out) >= std::numeric_limits<double>::min()))
+        return out;
+    return std::stod(std::string(v));
 }
+
+// Names -> indices over views into the file buffer: open addressing,
+// FNV-1a hashing, power-of-two capacity kept under half full.
+class NameTable {
+   public:
+    explicit NameTable(size_t expect = 1024) { rehash(expect * 2); }
+    // index of `key`, or -2 if absent
+    int find(std::string_view key) const {
+        size_t h = hash(key) & mask_;
+        while (slots_[h].used) {
+            if (slots_[h].key == key) return slots_[h].val;
+            h = (h + 1) & mask_;
+        }
+        return -2;
+    }
+    void assign(std::string_view key, int val) { *slot(key) = val; }
+    // existing index of `key`, or `fresh` after inserting it (inserted = true)
+    int find_or_insert(std::string_view key, int fresh, bool& inserted) {
+        int* v = slot(key, &inserted);
+        if (inserted) *v = fresh;
+        return *v;
+    }
+    size_t size() const { return count_; }
+
+   private:
+    struct Slot {
+        std::string_view key;
+        int val = 0;
+        bool used = false;
+    };
+    std::vector<Slot> slots_;
+    size_t mask_ = 0, count_ = 0;
+    static size_t hash(std::string_view k) {
+        uint64_t h = 1469598103934665603ull;
+        for (unsigned char ch : k) h = (h ^ ch) * 1099511628211ull;
+        return (size_t)(h ^ (h >> 29));
+    }
+    void rehash(size_t want) {
+        size_t cap = 16;
+        while (cap < want) cap <<= 1;
+        std::vector<Slot> old;
+        old.swap(slots_);
+        slots_.assign(cap, Slot{});
+        mask_ = cap - 1;
+        for (const Slot& s : old)
+            if (s.used) {
+                size_t h = hash(s.key) & mask_;
+                while (slots_[h].used) h = (h + 1) & mask_;
+                slots_[h] = s;
+            }
+    }
+    int* slot(std::string_view key, bool* inserted = nullptr) {
+        if (2 * (count_ + 1) > slots_.size()) rehash(slots_.size() * 4);
+        size_t h = hash(key) & mask_;
+        while (slots_[h].used) {
+            if (slots_[h].key == key) {
+                if (inserted) *inserted = false;
+                return &slots_[h].val;
+            }
+            h = (h + 1) & mask_;
+        }
+        slots_[h].used = true;
+        slots_[h].key = key;
+        ++count_;
+        if (inserted) *inserted = true;
+        return &slots_[h].val;
+    }
+};
 
 struct Reader {
     static constexpr double INF = std::numeric_limits<double>::infinity();
-    std::unordered_map<std::string, int> rows;  // -1: objective / free row
-    std::unordered_map<std::string, int> cols;
-    std::string obj;
+    NameTable rows;  // -1: objective / free row
+    NameTable cols;
+    std::string_view obj;
+    bool have_obj = false;
     std::vector<char> sense;
     std::vector<double> rhs;
     std::vector<int> ti, tj;
     std::vector<double> tv;
     std::vector<std::pair<int, double>> ranges;
     bool in_int = false;
+    std::string_view last_col;  // COLUMNS lines come grouped by column
+    int last_j = -1;
 
     int row_of(std::string_view name) const {
-        auto it = rows.find(std::string(name));
-        return it == rows.end() ? -1 : it->second;
+        const int r = rows.find(name);
+        return r == -2 ? -1 : r;
     }
 };
 
 }  // namespace
 
 void parse_mps(const std::string& path, Model& M) {
-    std::ifstream in(path);
-    if (!in) throw std::runtime_error("cannot open " + path);
+    // the whole file in memory; names stay views into it while parsing
+    std::FILE* f = std::fopen(path.c_str(), "rb");
+    if (!f) throw std::runtime_error("cannot open " + path);
+    std::string buf;
+    {
+        std::fseek(f, 0, SEEK_END);
+        const long size = std::ftell(f);
+        std::fseek(f, 0, SEEK_SET);
+        if (size > 0) {
+            buf.resize((size_t)size);
+            buf.resize(std::fread(&buf[0], 1, (size_t)size, f));
+        }
+        char chunk[1 << 16];  // anything beyond the size seen (growing files)
+        size_t got;
+        while ((got = std::fread(chunk, 1, sizeof(chunk), f)) > 0) buf.append(chunk, got);
+        std::fclose(f);
+    }
     Reader R;
-    std::string line, section;
+    {
+        // one entry per line at most: reserve the triplets once
+        size_t lines = 0;
+        for (const char* q = buf.data(); (q = static_cast<const char*>(std::memchr(
+                                              q, '\n', (size_t)(buf.data() + buf.size() - q))));
+             ++q)
+            ++lines;
+        R.ti.reserve(lines);
+        R.tj.reserve(lines);
+        R.tv.reserve(lines);
+    }
+    std::string section;
     std::vector<std::string_view> t;
-    while (std::getline(in, line)) {
+    const char* p = buf.data();
+    const char* const end = p + buf.size();
+    while (p < end) {
+        const char* eol = static_cast<const char*>(std::memchr(p, '\n', (size_t)(end - p)));
+        if (!eol) eol = end;
+        const std::string_view line(p, (size_t)(eol - p));
+        p = eol + 1;
         if (line.empty() || line[0] == '*') continue;
         const bool header = line[0] != ' ' && line[0] != '\t';
         split(line, t);
@@ -97,36 +218,41 @@ void parse_mps(const std::string& path, Model& M) {
         }
         if (section == "ROWS") {
             if (t.size() < 2) continue;
-            const std::string name(t[1]);
+            const std::string_view name = t[1];
             if (t[0][0] == 'N') {
-                if (R.obj.empty()) R.obj = name;
-                R.rows[name] = -1;
+                if (!R.have_obj) {
+                    R.obj = name;
+                    R.have_obj = true;
+                }
+                R.rows.assign(name, -1);
             } else {
-                R.rows[name] = (int)R.sense.size();
+                R.rows.assign(name, (int)R.sense.size());
                 R.sense.push_back(t[0][0]);
                 R.rhs.push_back(0.0);
             }
         } else if (section == "COLUMNS") {
-            if (line.find("'MARKER'") != std::string::npos) {
-                R.in_int = line.find("INTORG") != std::string::npos;
+            if (line.find("'MARKER'") != std::string_view::npos) {
+                R.in_int = line.find("INTORG") != std::string_view::npos;
                 continue;
             }
-            const std::string cname(t[0]);
-            auto it = R.cols.find(cname);
             int j;
-            if (it == R.cols.end()) {
-                j = (int)R.cols.size();
-                R.cols.emplace(cname, j);
-                M.c.push_back(0.0);
-                M.cl.push_back(0.0);
-                M.cu.push_back(Reader::INF);
-                M.integ.push_back(R.in_int ? 1 : 0);
+            if (R.last_j >= 0 && t[0] == R.last_col) {
+                j = R.last_j;
             } else {
-                j = it->second;
+                bool inserted = false;
+                j = R.cols.find_or_insert(t[0], (int)R.cols.size(), inserted);
+                if (inserted) {
+                    M.c.push_back(0.0);
+                    M.cl.push_back(0.0);
+                    M.cu.push_back(Reader::INF);
+                    M.integ.push_back(R.in_int ? 1 : 0);
+                }
+                R.last_col = t[0];
+                R.last_j = j;
             }
             for (size_t k = 1; k + 1 < t.size(); k += 2) {
                 const double v = num(t[k + 1]);
-                if (t[k] == R.obj) {
+                if (R.have_obj && t[k] == R.obj) {
                     M.c[j] += v;
                     continue;
                 }
@@ -138,7 +264,7 @@ void parse_mps(const std::string& path, Model& M) {
             }
         } else if (section == "RHS") {
             for (size_t k = 1; k + 1 < t.size(); k += 2) {
-                if (t[k] == R.obj) {
+                if (R.have_obj && t[k] == R.obj) {
                     M.obj_const -= num(t[k + 1]);
                     continue;
                 }
@@ -155,18 +281,16 @@ void parse_mps(const std::string& path, Model& M) {
             }
         } else if (section == "QUADOBJ" || section == "QSECTION" || section == "QMATRIX") {
             for (size_t k = 0; k + 2 < t.size(); k += 3) {
-                auto a = R.cols.find(std::string(t[k]));
-                auto b = R.cols.find(std::string(t[k + 1]));
-                if (a == R.cols.end() || b == R.cols.end()) continue;
-                M.q_i.push_back(a->second);
-                M.q_j.push_back(b->second);
+                const int a = R.cols.find(t[k]), b = R.cols.find(t[k + 1]);
+                if (a == -2 || b == -2) continue;
+                M.q_i.push_back(a);
+                M.q_j.push_back(b);
                 M.q_v.push_back(num(t[k + 2]));
             }
         } else if (section == "BOUNDS") {
             if (t.size() < 3) continue;
-            auto it = R.cols.find(std::string(t[2]));
-            if (it == R.cols.end()) throw std::out_of_range("BOUNDS names an unknown column");
-            const int j = it->second;
+            const int j = R.cols.find(t[2]);
+            if (j == -2) throw std::out_of_range("BOUNDS names an unknown column");
             const double v = t.size() > 3 ? num(t[3]) : 0.0;
             const std::string_view ty = t[0];
             if (ty == "UP") {
