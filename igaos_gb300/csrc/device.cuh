@@ -31,6 +31,14 @@ constexpr int kWarps = kThreads / 32;
 #define IGX_HOT_CTAS 6
 #endif
 constexpr int kHotCtasPerSm = IGX_HOT_CTAS;
+// FP64 attempt kernels: their own residency. At 6 CTAs/SM they spill under
+// 40 registers; measured on the 200k x 500k LP: 6 CTAs 173 us per FP64
+// attempt, 4 CTAs (64 registers) 165 us, 3 CTAs (<= 85 registers) 160 us.
+#ifndef IGX_HOT_CTAS_F64
+#define IGX_HOT_CTAS_F64 3
+#endif
+template <typename T> struct HotCtas { static constexpr int value = kHotCtasPerSm; };
+template <> struct HotCtas<double> { static constexpr int value = IGX_HOT_CTAS_F64; };
 
 template <typename T>
 struct Csr {

@@ -75,6 +75,7 @@ static Sched upload_sched(Arena& ar, const int* ptr, int rows, int resident_ctas
     Sched s;
     s.nwarps = (int)wl.size();
     s.ctas = std::max(1, std::min(resident_ctas, (s.nwarps + kWarps - 1) / kWarps));
+    s.ctas64 = std::max(1, std::min(s.ctas, resident_ctas / kHotCtasPerSm * HotCtas<double>::value));
     s.row = ar.alloc<int>(wr.size());
     s.lg = ar.alloc<unsigned char>(wl.size());
     CU(cudaMemcpy(s.row, wr.data(), sizeof(int) * wr.size(), cudaMemcpyHostToDevice));
@@ -438,7 +439,9 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     }
     da.part = reinterpret_cast<Acc<T>*>(w.part_d);
     da.part_primal = reinterpret_cast<const Acc<T>*>(w.part_p);
-    da.n_primal = sAT_.ctas;
+    const bool f64 = std::is_same<T, double>::value;
+    const int gp = f64 ? sAT_.ctas64 : sAT_.ctas, gd = f64 ? sA_.ctas64 : sA_.ctas;
+    da.n_primal = gp;
     da.yhat = VecSel<T>::yh(v);
     da.fac = fac_;
     da.n_fac = kFac;
@@ -446,8 +449,8 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     launches_ += 2LL * count;
     auto enqueue = [&](int cnt) {
         for (int a = 0; a < cnt; ++a) {
-            k_primal<T><<<sAT_.ctas, kThreads, 0, st_>>>(pa);
-            k_dual<T><<<sA_.ctas, kThreads, 0, st_>>>(da);
+            k_primal<T><<<gp, kThreads, 0, st_>>>(pa);
+            k_dual<T><<<gd, kThreads, 0, st_>>>(da);
         }
     };
     if (!graphs) {

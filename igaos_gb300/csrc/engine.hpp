@@ -47,6 +47,7 @@ struct Sched {
     unsigned char* lg = nullptr;
     int nwarps = 0;
     int ctas = 0;  // kWarps warps per CTA
+    int ctas64 = 0;  // launch width of the FP64 attempt kernels
     WarpSched view() const { return WarpSched{row, lg, nwarps}; }
 };
 

@@ -93,7 +93,7 @@ struct PrimalEpi {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_primal(PrimalArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_primal(PrimalArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
@@ -213,7 +213,7 @@ __device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cro
 // reduction of all partials (kern_dotfin, :99-125) and the step decision that
 // the reference made on the host after a blocking copy (:768-794).
 template <typename T>
-__global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_dual(DualArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_dual(DualArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
