@@ -1,6 +1,7 @@
 // MPS reader and CSR/CSC builder (see model.hpp).
 #include "model.hpp"
 
+#include <algorithm>
 #include <cctype>
 #include <charconv>
 #include <cmath>
@@ -8,10 +9,12 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <exception>
 #include <limits>
 #include <stdexcept>
 #include <string_view>
 #include <system_error>
+#include <thread>
 
 namespace igaos::io {
 
@@ -79,41 +82,56 @@ double num(std::string_view v) {
 }
 
 // Names -> indices over views into the file buffer: open addressing,
-// FNV-1a hashing, power-of-two capacity kept under half full.
+// FNV-1a hashing, power-of-two capacity kept under half full. Each slot keeps
+// 32 bits of the hash, so probes and rehashes touch the names only on a match.
 class NameTable {
    public:
     explicit NameTable(size_t expect = 1024) { rehash(expect * 2); }
     // index of `key`, or -2 if absent
     int find(std::string_view key) const {
-        size_t h = hash(key) & mask_;
-        while (slots_[h].used) {
-            if (slots_[h].key == key) return slots_[h].val;
-            h = (h + 1) & mask_;
-        }
+        const uint64_t h = hash(key);
+        const uint32_t tg = tag(h);
+        for (size_t i = h & mask_; slots_[i].tag; i = (i + 1) & mask_)
+            if (slots_[i].tag == tg && slots_[i].len == key.size() &&
+                std::memcmp(slots_[i].ptr, key.data(), key.size()) == 0)
+                return slots_[i].val;
         return -2;
     }
-    void assign(std::string_view key, int val) { *slot(key) = val; }
+    // maps `key` to `val`; returns the index it replaced, or -2 if it was new
+    int assign(std::string_view key, int val) {
+        bool inserted = false;
+        int* v = slot(key, &inserted);
+        const int prev = inserted ? -2 : *v;
+        *v = val;
+        return prev;
+    }
     // existing index of `key`, or `fresh` after inserting it (inserted = true)
     int find_or_insert(std::string_view key, int fresh, bool& inserted) {
         int* v = slot(key, &inserted);
         if (inserted) *v = fresh;
         return *v;
     }
+    // room for `n` names without growing
+    void reserve(size_t n) {
+        if (2 * n > slots_.size()) rehash(2 * n);
+    }
     size_t size() const { return count_; }
 
    private:
     struct Slot {
-        std::string_view key;
+        const char* ptr = nullptr;
+        uint32_t len = 0;
+        uint32_t tag = 0;  // 0: empty
         int val = 0;
-        bool used = false;
     };
     std::vector<Slot> slots_;
     size_t mask_ = 0, count_ = 0;
-    static size_t hash(std::string_view k) {
+    static uint64_t hash(std::string_view k) {
         uint64_t h = 1469598103934665603ull;
         for (unsigned char ch : k) h = (h ^ ch) * 1099511628211ull;
-        return (size_t)(h ^ (h >> 29));
+        return h ^ (h >> 29);
     }
+    static uint32_t tag(uint64_t h) { return (uint32_t)(h >> 32) | 1u; }
     void rehash(size_t want) {
         size_t cap = 16;
         while (cap < want) cap <<= 1;
@@ -122,27 +140,29 @@ class NameTable {
         slots_.assign(cap, Slot{});
         mask_ = cap - 1;
         for (const Slot& s : old)
-            if (s.used) {
-                size_t h = hash(s.key) & mask_;
-                while (slots_[h].used) h = (h + 1) & mask_;
-                slots_[h] = s;
+            if (s.tag) {
+                size_t i = hash(std::string_view(s.ptr, s.len)) & mask_;
+                while (slots_[i].tag) i = (i + 1) & mask_;
+                slots_[i] = s;
             }
     }
     int* slot(std::string_view key, bool* inserted = nullptr) {
         if (2 * (count_ + 1) > slots_.size()) rehash(slots_.size() * 4);
-        size_t h = hash(key) & mask_;
-        while (slots_[h].used) {
-            if (slots_[h].key == key) {
+        const uint64_t h = hash(key);
+        const uint32_t tg = tag(h);
+        size_t i = h & mask_;
+        for (; slots_[i].tag; i = (i + 1) & mask_)
+            if (slots_[i].tag == tg && slots_[i].len == key.size() &&
+                std::memcmp(slots_[i].ptr, key.data(), key.size()) == 0) {
                 if (inserted) *inserted = false;
-                return &slots_[h].val;
+                return &slots_[i].val;
             }
-            h = (h + 1) & mask_;
-        }
-        slots_[h].used = true;
-        slots_[h].key = key;
+        slots_[i].ptr = key.data();
+        slots_[i].len = (uint32_t)key.size();
+        slots_[i].tag = tg;
         ++count_;
         if (inserted) *inserted = true;
-        return &slots_[h].val;
+        return &slots_[i].val;
     }
 };
 
@@ -150,6 +170,9 @@ struct Reader {
     static constexpr double INF = std::numeric_limits<double>::infinity();
     NameTable rows;  // -1: objective / free row
     NameTable cols;
+    // name of each row / column index (empty once a later ROWS line takes the
+    // name away): lookups try the index after the previous one first
+    std::vector<std::string_view> row_names, col_names;
     std::string_view obj;
     bool have_obj = false;
     std::vector<char> sense;
@@ -158,14 +181,201 @@ struct Reader {
     std::vector<double> tv;
     std::vector<std::pair<int, double>> ranges;
     bool in_int = false;
-    std::string_view last_col;  // COLUMNS lines come grouped by column
-    int last_j = -1;
 
     int row_of(std::string_view name) const {
         const int r = rows.find(name);
         return r == -2 ? -1 : r;
     }
+    // row_of / column index (-2 if absent) of a name, trying `hint` + 1 and
+    // `hint` before the table: RHS and BOUNDS entries mostly follow the order
+    // of ROWS and COLUMNS
+    int row_near(std::string_view name, int hint) const {
+        for (int c = hint + 1; c >= hint && c >= 0; --c)
+            if ((size_t)c < row_names.size() && row_names[c] == name) return c;
+        return row_of(name);
+    }
+    int col_near(std::string_view name, int hint) const {
+        for (int c = hint + 1; c >= hint && c >= 0; --c)
+            if ((size_t)c < col_names.size() && col_names[c] == name) return c;
+        return cols.find(name);
+    }
 };
+
+// Next line of [p, end): the view without its '\n', and p moved past it.
+std::string_view next_line(const char*& p, const char* end) {
+    const char* eol = static_cast<const char*>(std::memchr(p, '\n', (size_t)(end - p)));
+    if (!eol) eol = end;
+    const std::string_view line(p, (size_t)(eol - p));
+    p = eol + 1;
+    return line;
+}
+
+// A section header: a non-blank, non-comment line starting in column 1.
+bool is_header(std::string_view line) {
+    if (line.empty() || line[0] == '*' || line[0] == ' ' || line[0] == '\t') return false;
+    for (char ch : line)
+        if (ch != ' ' && ch != '\t' && ch != '\r') return true;
+    return false;
+}
+
+// End of the section whose body starts at p (the next header line, or end),
+// and its line count.
+const char* section_end(const char* p, const char* end, size_t* lines = nullptr) {
+    size_t k = 0;
+    while (p < end) {
+        const char* at = p;
+        if (is_header(next_line(p, end))) return at;
+        ++k;
+        if (lines) *lines = k;
+    }
+    return end;
+}
+
+// One slice of a COLUMNS section parsed on its own: columns numbered locally
+// in order of first appearance, with the integer-marker state at that point
+// (-1: no marker yet in this slice, the state entering it applies).
+struct ColumnSlice {
+    NameTable local{64};
+    std::vector<std::string_view> names;
+    std::vector<signed char> integ;
+    signed char end_state = -1;
+    std::vector<int> ti, tj;
+    std::vector<double> tv;
+    std::vector<std::pair<int, double>> obj;  // (local column, value), file order
+    std::exception_ptr err;
+
+    void parse(const Reader& R, const char* p, const char* end) {
+        std::vector<std::string_view> t;
+        std::string_view last;
+        int last_j = -1;
+        signed char state = -1;
+        try {
+            while (p < end) {
+                const std::string_view line = next_line(p, end);
+                if (line.empty() || line[0] == '*') continue;
+                split(line, t);
+                if (t.empty()) continue;
+                if (line.find("'MARKER'") != std::string_view::npos) {
+                    state = line.find("INTORG") != std::string_view::npos ? 1 : 0;
+                    continue;
+                }
+                int j;
+                if (last_j >= 0 && t[0] == last) {
+                    j = last_j;
+                } else {
+                    bool inserted = false;
+                    j = local.find_or_insert(t[0], (int)names.size(), inserted);
+                    if (inserted) {
+                        names.push_back(t[0]);
+                        integ.push_back(state);
+                    }
+                    last = t[0];
+                    last_j = j;
+                }
+                for (size_t k = 1; k + 1 < t.size(); k += 2) {
+                    const double v = num(t[k + 1]);
+                    if (R.have_obj && t[k] == R.obj) {
+                        obj.emplace_back(j, v);
+                        continue;
+                    }
+                    const int r = R.row_of(t[k]);
+                    if (r < 0) continue;
+                    ti.push_back(r);
+                    tj.push_back(j);
+                    tv.push_back(v);
+                }
+            }
+        } catch (...) {
+            err = std::current_exception();
+        }
+        end_state = state;
+    }
+};
+
+// The COLUMNS section starting at p, on the host's threads: slices at line
+// boundaries parsed independently (row names are only read), then merged in
+// file order, so column numbering, integer flags, objective sums and the
+// triplet order are those of a sequential pass; the first error in file
+// order is the one raised. Returns the start of the next section.
+const char* parse_columns_parallel(Reader& R, Model& M, const char* p, const char* end) {
+    const char* sec_end = section_end(p, end);
+    const size_t bytes = (size_t)(sec_end - p);
+    const int nt = bytes < (8u << 20)
+                       ? 1
+                       : (int)std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+    std::vector<const char*> cut(nt + 1, p);
+    cut[nt] = sec_end;
+    for (int s = 1; s < nt; ++s) {
+        const char* c = p + bytes * s / nt;
+        c = std::max(c, cut[s - 1]);
+        const char* nl = static_cast<const char*>(std::memchr(c, '\n', (size_t)(sec_end - c)));
+        cut[s] = nl ? nl + 1 : sec_end;
+    }
+    std::vector<ColumnSlice> sl(nt);
+    if (nt == 1) {
+        sl[0].parse(R, cut[0], cut[1]);
+    } else {
+        std::vector<std::thread> pool;
+        for (int s = 0; s < nt; ++s) pool.emplace_back([&, s] { sl[s].parse(R, cut[s], cut[s + 1]); });
+        for (auto& th : pool) th.join();
+    }
+    size_t names = R.cols.size(), trip = R.tv.size();
+    std::vector<size_t> at(nt + 1, trip);
+    for (int k = 0; k < nt; ++k) {
+        if (sl[k].err) std::rethrow_exception(sl[k].err);
+        names += sl[k].names.size();
+        at[k + 1] = at[k] + sl[k].tv.size();
+    }
+    R.cols.reserve(names);
+    R.col_names.reserve(names);
+    M.c.reserve(names);
+    M.cl.reserve(names);
+    M.cu.reserve(names);
+    M.integ.reserve(names);
+    // global numbering in file order
+    std::vector<std::vector<int>> gj(nt);
+    bool in_int = R.in_int;
+    for (int k = 0; k < nt; ++k) {
+        ColumnSlice& s = sl[k];
+        gj[k].resize(s.names.size());
+        for (size_t q = 0; q < s.names.size(); ++q) {
+            bool inserted = false;
+            gj[k][q] = R.cols.find_or_insert(s.names[q], (int)R.cols.size(), inserted);
+            if (inserted) {
+                const bool flag = s.integ[q] < 0 ? in_int : s.integ[q] == 1;
+                R.col_names.push_back(s.names[q]);
+                M.c.push_back(0.0);
+                M.cl.push_back(0.0);
+                M.cu.push_back(Reader::INF);
+                M.integ.push_back(flag ? 1 : 0);
+            }
+        }
+        for (const auto& [lj, v] : s.obj) M.c[gj[k][lj]] += v;
+        if (s.end_state >= 0) in_int = s.end_state == 1;
+    }
+    R.in_int = in_int;
+    // triplets at their file-order offsets
+    R.ti.resize(at[nt]);
+    R.tj.resize(at[nt]);
+    R.tv.resize(at[nt]);
+    auto place = [&](int k) {
+        const ColumnSlice& s = sl[k];
+        const std::vector<int>& g = gj[k];
+        for (size_t e = 0; e < s.tv.size(); ++e) {
+            R.ti[at[k] + e] = s.ti[e];
+            R.tj[at[k] + e] = g[s.tj[e]];
+            R.tv[at[k] + e] = s.tv[e];
+        }
+    };
+    if (nt == 1) {
+        place(0);
+    } else {
+        std::vector<std::thread> pool;
+        for (int k = 0; k < nt; ++k) pool.emplace_back(place, k);
+        for (auto& th : pool) th.join();
+    }
+    return sec_end;
+}
 
 }  // namespace
 
@@ -201,6 +411,7 @@ void parse_mps(const std::string& path, Model& M) {
     }
     std::string section;
     std::vector<std::string_view> t;
+    int hint_r = -1, hint_j = -1;  // last row of RHS, last column of BOUNDS
     const char* p = buf.data();
     const char* const end = p + buf.size();
     while (p < end) {
@@ -214,6 +425,14 @@ void parse_mps(const std::string& path, Model& M) {
         if (t.empty()) continue;
         if (header) {
             section.assign(t[0]);
+            if (section == "COLUMNS") {
+                p = parse_columns_parallel(R, M, p, end);
+            } else if (section == "ROWS") {
+                size_t lines = 0;
+                section_end(p, end, &lines);
+                R.rows.reserve(R.rows.size() + lines);
+                R.row_names.reserve(R.row_names.size() + lines);
+            }
             continue;
         }
         if (section == "ROWS") {
@@ -224,43 +443,14 @@ void parse_mps(const std::string& path, Model& M) {
                     R.obj = name;
                     R.have_obj = true;
                 }
-                R.rows.assign(name, -1);
+                const int prev = R.rows.assign(name, -1);
+                if (prev >= 0) R.row_names[prev] = {};
             } else {
-                R.rows.assign(name, (int)R.sense.size());
+                const int prev = R.rows.assign(name, (int)R.sense.size());
+                if (prev >= 0) R.row_names[prev] = {};
+                R.row_names.push_back(name);
                 R.sense.push_back(t[0][0]);
                 R.rhs.push_back(0.0);
-            }
-        } else if (section == "COLUMNS") {
-            if (line.find("'MARKER'") != std::string_view::npos) {
-                R.in_int = line.find("INTORG") != std::string_view::npos;
-                continue;
-            }
-            int j;
-            if (R.last_j >= 0 && t[0] == R.last_col) {
-                j = R.last_j;
-            } else {
-                bool inserted = false;
-                j = R.cols.find_or_insert(t[0], (int)R.cols.size(), inserted);
-                if (inserted) {
-                    M.c.push_back(0.0);
-                    M.cl.push_back(0.0);
-                    M.cu.push_back(Reader::INF);
-                    M.integ.push_back(R.in_int ? 1 : 0);
-                }
-                R.last_col = t[0];
-                R.last_j = j;
-            }
-            for (size_t k = 1; k + 1 < t.size(); k += 2) {
-                const double v = num(t[k + 1]);
-                if (R.have_obj && t[k] == R.obj) {
-                    M.c[j] += v;
-                    continue;
-                }
-                const int r = R.row_of(t[k]);
-                if (r < 0) continue;
-                R.ti.push_back(r);
-                R.tj.push_back(j);
-                R.tv.push_back(v);
             }
         } else if (section == "RHS") {
             for (size_t k = 1; k + 1 < t.size(); k += 2) {
@@ -268,8 +458,9 @@ void parse_mps(const std::string& path, Model& M) {
                     M.obj_const -= num(t[k + 1]);
                     continue;
                 }
-                const int r = R.row_of(t[k]);
+                const int r = R.row_near(t[k], hint_r);
                 if (r < 0) continue;
+                hint_r = r;
                 R.rhs[r] = num(t[k + 1]);
             }
         } else if (section == "RANGES") {
@@ -289,8 +480,9 @@ void parse_mps(const std::string& path, Model& M) {
             }
         } else if (section == "BOUNDS") {
             if (t.size() < 3) continue;
-            const int j = R.cols.find(t[2]);
+            const int j = R.col_near(t[2], hint_j);
             if (j == -2) throw std::out_of_range("BOUNDS names an unknown column");
+            hint_j = j;
             const double v = t.size() > 3 ? num(t[3]) : 0.0;
             const std::string_view ty = t[0];
             if (ty == "UP") {

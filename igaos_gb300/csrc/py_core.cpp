@@ -114,6 +114,7 @@ PYBIND11_MODULE(_core, m) {
         .def_readonly("cu", &Model::cu)
         .def_readonly("rmin", &Model::rmin)
         .def_readonly("rmax", &Model::rmax)
+        .def_readonly("integ", &Model::integ)
         .def("nnz", &Model::nnz)
         .def_property_readonly("stats", &model_stats)
         .def("__repr__", [](const Model& mm) {

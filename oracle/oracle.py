@@ -331,6 +331,13 @@ def ref_parse_mps(path: str) -> LP:
     return LP(m=m, n=n, obj_const=oc.value, **a)
 
 
+def ref_last_integ(n: int) -> np.ndarray:
+    """Integer flags (uint8 per column) of the model ref_parse_mps parsed last."""
+    out = np.zeros(n, np.uint8)
+    _ref_eval().ref_fetch_integ(out.ctypes.data_as(C.POINTER(C.c_ubyte)))
+    return out
+
+
 def ref_simplex_solve(lp: LP, time_limit=600.0):
     global _REF_SIMPLEX
     if _REF_SIMPLEX is None:

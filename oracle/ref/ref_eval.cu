@@ -65,6 +65,11 @@ int ref_parse_mps(const char* path, int* m, int* n, long* nnz,
     return 0;
 }
 
+// integer flag of each column of the last parsed model (1: integer)
+void ref_fetch_integ(unsigned char* out) {
+    for (size_t j = 0; j < g_model.integ.size(); ++j) out[j] = g_model.integ[j] ? 1 : 0;
+}
+
 void ref_fetch_model(int* ap, int* ai, double* ax, int* cp, int* ci,
                      double* acx, double* c, double* cl, double* cu,
                      double* rmin, double* rmax) {

@@ -112,3 +112,112 @@ def test_generators_are_feasible_at_x_star():
     g = G.config5(seed=0, side=10, commodities=3)
     assert g.n == 3 * 2 * 2 * 10 * 9 and g.nnz == 3 * g.n
     assert g.m == 3 * 100 + 2 * 2 * 10 * 9
+
+
+def _big_mps(seed=3, n=110_000, m=30_000):
+    """A COLUMNS section well above the reader's 8 MB split threshold, with
+    what a split must keep in file order: integer MARKER blocks crossing the
+    cut points, a column continued after other columns (and again in the
+    last slice), two pairs on one line, comment and free-row entries, and
+    several objective entries for one column. Returns (text, expected) where
+    expected holds the triplets, objective and integer flags by construction."""
+    rng = np.random.default_rng(seed)
+    rows = [" N  COST", " N  FREE"]
+    sense = rng.choice(np.array(list("LGE")), m)
+    rows += [f" {s}  R{i}" for i, s in enumerate(sense)]
+    cols, ti, tj, tv = [], [], [], []
+    c = np.zeros(n)
+    integ = np.zeros(n, np.uint8)
+    in_int = False
+    vals = np.round(rng.uniform(-9, 9, 4 * n), 3)
+    vi = 0
+
+    def val():
+        nonlocal vi
+        vi += 1
+        return float(vals[vi - 1])
+
+    def emit(j, pairs):
+        for r, v in pairs:
+            if r >= 0:
+                ti.append(r); tj.append(j); tv.append(v)
+            elif r == -1:
+                c[j] += v
+
+    def name(r):
+        return "COST" if r == -1 else ("FREE" if r == -2 else f"R{r}")
+
+    revisit = [17, 54_321]
+    for j in range(n):
+        if j % 9_973 == 0:
+            in_int = not in_int
+            cols.append("    MARKER  'MARKER'  " + ("'INTORG'" if in_int else "'INTEND'"))
+        integ[j] = in_int
+        k = int(rng.integers(1, 5))
+        rs = rng.choice(m, k, replace=False)
+        pairs = [(-1, val())] + [(int(r), val()) for r in rs]
+        if j % 7 == 0:
+            pairs.append((-2, 1.0))
+        if j % 1000 == 0:
+            cols.append("* comment line inside COLUMNS")
+        q = 0
+        while q < len(pairs):
+            if q + 1 < len(pairs) and j % 3 == 0:
+                (r1, v1), (r2, v2) = pairs[q], pairs[q + 1]
+                cols.append(f"    C{j}  {name(r1)}  {v1!r}  {name(r2)}  {v2!r}")
+                q += 2
+            else:
+                r1, v1 = pairs[q]
+                cols.append(f"    C{j}  {name(r1)}  {v1!r}")
+                q += 1
+        emit(j, pairs)
+        if j in (60_000, n - 1):  # continue earlier columns much later
+            for jj in revisit:
+                more = [(-1, 0.5), (int(rng.integers(m)), val())]
+                cols += [f"    C{jj}  {name(r)}  {v!r}" for r, v in more]
+                emit(jj, more)
+    rhs = [f"    RHS  R{i}  {float(np.round(rng.uniform(-5, 5), 2))!r}" for i in range(0, m, 3)]
+    rhs.append("    RHS  COST  2.5")
+    bounds = []
+    for j in range(0, n, 5):
+        t = ("UP", "LO", "FX", "FR", "MI", "PL", "BV", "LI", "UI")[(j // 5) % 9]
+        if t in ("BV", "LI", "UI"):
+            integ[j] = 1
+        bounds.append(f" {t} BND  C{j}" + ("" if t in ("FR", "MI", "PL", "BV") else
+                                          f"  {float((j % 13) - 4)!r}"))
+    text = "\n".join(["NAME BIG", "ROWS", *rows, "COLUMNS", *cols, "RHS", *rhs,
+                      "RANGES", "    RNG  R1  4.0", "    RNG  R2  -3.0",
+                      "BOUNDS", *bounds, "ENDATA"]) + "\n"
+    exp = dict(ti=np.array(ti), tj=np.array(tj), tv=np.array(tv), c=c, integ=integ, m=m, n=n)
+    return text, exp
+
+
+def test_mps_reader_split_columns_section(core, orc, tmp_path):
+    """The COLUMNS section parsed in slices on several threads gives the
+    arrays of a sequential reading: by construction, and against the
+    reference's parse_mps where the reference tree is present."""
+    text, e = _big_mps()
+    cols_bytes = text.index("\nRHS\n") - text.index("\nCOLUMNS\n")
+    assert cols_bytes > (8 << 20)
+    p = tmp_path / "big.mps"
+    p.write_text(text)
+    M = core.read_mps(str(p))
+    assert (M.m, M.n) == (e["m"], e["n"])
+    ro = np.argsort(e["ti"], kind="stable")
+    co = np.argsort(e["tj"], kind="stable")
+    assert np.array_equal(np.asarray(M.ap), np.r_[0, np.cumsum(np.bincount(e["ti"], minlength=e["m"]))])
+    assert np.array_equal(np.asarray(M.ai), e["tj"][ro])
+    assert np.array_equal(np.asarray(M.ax), e["tv"][ro])
+    assert np.array_equal(np.asarray(M.cp), np.r_[0, np.cumsum(np.bincount(e["tj"], minlength=e["n"]))])
+    assert np.array_equal(np.asarray(M.ci), e["ti"][co])
+    assert np.array_equal(np.asarray(M.acx), e["tv"][co])
+    assert np.array_equal(np.asarray(M.c), e["c"])
+    assert np.array_equal(np.asarray(M.integ, np.uint8), e["integ"])
+    assert M.obj_const == -2.5
+    if reference_dir() is None or not orc.ref_available():
+        return
+    want = orc.ref_parse_mps(str(p))
+    for k in KEYS:
+        assert _same(getattr(M, k), getattr(want, k)), k
+    assert M.obj_const == want.obj_const
+    assert np.array_equal(np.asarray(M.integ, np.uint8), orc.ref_last_integ(want.n))
