@@ -37,6 +37,19 @@ constexpr int kHotCtasPerSm = IGX_HOT_CTAS;
 #ifndef IGX_HOT_CTAS_F64
 #define IGX_HOT_CTAS_F64 3
 #endif
+// Entries per lane the warp schedule aims at (G = smallest power of two with
+// G * kLaneEntries >= row length), and the batch of entries a lane loads
+// before its gathers. Measured on the 200k x 500k LP (FP32 attempt, 6 CTAs
+// per SM): 4 entries per lane 60.2 us, 8 entries 55.8 us, 16 entries 59.2 us;
+// batches of 8 (5 CTAs per SM) 55.6 us.
+#ifndef IGX_LANE_ENTRIES
+#define IGX_LANE_ENTRIES 8
+#endif
+#ifndef IGX_LANE_BATCH
+#define IGX_LANE_BATCH 4
+#endif
+constexpr int kLaneEntries = IGX_LANE_ENTRIES;
+constexpr int kLaneBatch = IGX_LANE_BATCH;
 template <typename T> struct HotCtas { static constexpr int value = kHotCtasPerSm; };
 template <> struct HotCtas<double> { static constexpr int value = IGX_HOT_CTAS_F64; };
 
@@ -286,7 +299,7 @@ __device__ __forceinline__ bool last_cta(unsigned int* ticket) {
 // Rows are processed by warps. The host permutes the LP so that rows (and
 // columns) appear in decreasing nonzero count, then deals consecutive rows to
 // warps: a warp owns 32/G consecutive rows of similar length with G lanes per
-// row (G = 1..32, about four entries per lane). No shared memory and no
+// row (G = 1..32, about kLaneEntries entries per lane). No shared memory and no
 // block-wide barrier on the hot path.
 struct WarpSched {
     const int* row;           // nwarps + 1 row boundaries
@@ -308,8 +321,8 @@ struct PlainEpi {
 
 // One warp item: every row of item `w` of A times x. The epilogue's vector
 // entries for the lane's row are loaded first (epi.load), then the row's
-// entries in predicated batches of four per lane (eight independent loads,
-// then four gathers in flight), the G-lane shuffle reduction, and the row step
+// entries in predicated batches of kLaneBatch per lane (all value and index
+// loads of a batch, then its gathers in flight), the G-lane shuffle reduction, and the row step
 // (epi.apply) from lane i for the item's i-th row, so consecutive lanes touch
 // consecutive vector entries.
 template <typename T, class E>
@@ -328,21 +341,21 @@ __device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
     Acc<T> acc;
     if (r < r1) {
         const int b = __ldg(A.ptr + r), e = __ldg(A.ptr + r + 1);
-        for (int p = b + gl; p < e; p += 4 * G) {
-            T a[4];
-            int j[4];
+        for (int p = b + gl; p < e; p += kLaneBatch * G) {
+            T a[kLaneBatch];
+            int j[kLaneBatch];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) {
+            for (int u = 0; u < kLaneBatch; ++u) {
                 const int q = p + u * G;
                 const bool ok = q < e;
                 a[u] = ok ? __ldg(A.val + q) : T(0);
                 j[u] = ok ? __ldg(A.idx + q) : 0;
             }
-            T xv[4];
+            T xv[kLaneBatch];
 #pragma unroll
-            for (int u = 0; u < 4; ++u) xv[u] = __ldg(x + j[u]);
+            for (int u = 0; u < kLaneBatch; ++u) xv[u] = __ldg(x + j[u]);
 #pragma unroll
-            for (int u = 0; u < 4; ++u) acc.add(a[u], xv[u]);  // masked: 0 * x[0] adds 0
+            for (int u = 0; u < kLaneBatch; ++u) acc.add(a[u], xv[u]);  // masked: 0 * x[0] adds 0
         }
     }
     for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(0xffffffffu, o, G);

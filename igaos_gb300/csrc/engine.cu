@@ -58,7 +58,7 @@ void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<u
     while (r < rows) {
         const int len = ptr[r + 1] - ptr[r];
         int lg = 0;
-        while (lg < 5 && (1 << lg) * 4 < len) ++lg;  // about four entries per lane
+        while (lg < 5 && (1 << lg) * kLaneEntries < len) ++lg;
         r = std::min(rows, r + (32 >> lg));
         wrow.push_back(r);
         wlg.push_back((unsigned char)lg);
