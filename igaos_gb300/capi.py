@@ -107,6 +107,8 @@ def lib():
         L.igaos_pdhg_spmv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp]
         L.igaos_pdhg_dual_repair.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, _dp,
                                              C.POINTER(C.c_int)]
+        L.igaos_pdhg_dual_repair_device.argtypes = [C.c_void_p, _dp, _dp, C.c_double,
+                                                    C.c_double, _dp, C.POINTER(C.c_int), _dp]
         L.igaos_pdhg_solve_batch.argtypes = [
             C.c_int, _ip, _ip, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, C.POINTER(Options),
             C.POINTER(BatchResult), _dp, _dp]
@@ -264,6 +266,18 @@ class Problem:
         _check(lib().igaos_pdhg_dual_repair(self.h, *[_d(v) for v in a], C.c_double(col_tol),
                                             _d(y), C.byref(ok)))
         return bool(ok.value), y
+
+    def dual_repair_device(self, x, y_it, col_tol, tol):
+        """(certified, y, metrics): the engine's matrix-free dual repair on the
+        device at candidate x from the dual estimate y_it, original units (any
+        m); metrics = dict of pinf, dinf, gap, op, od, prow of (x, y)."""
+        a = [np.ascontiguousarray(v, np.float64) for v in (x, y_it)]
+        y = np.zeros(self.m)
+        m6 = np.zeros(6)
+        ok = C.c_int(0)
+        _check(lib().igaos_pdhg_dual_repair_device(self.h, _d(a[0]), _d(a[1]), C.c_double(col_tol),
+                                                   C.c_double(tol), _d(y), C.byref(ok), _d(m6)))
+        return bool(ok.value), y, dict(zip(("pinf", "dinf", "gap", "op", "od", "prow"), m6.tolist()))
 
     def spmv(self, x, transpose=False, precision="fp64"):
         x = np.ascontiguousarray(x, np.float64)

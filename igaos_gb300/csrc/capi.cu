@@ -274,6 +274,20 @@ int igaos_pdhg_dual_repair(igaos_pdhg_problem* p, const double* x, const double*
     return guarded([&] { *certified = p->eng->repair(x, Ax, y_it, col_tol, y) ? 1 : 0; });
 }
 
+int igaos_pdhg_dual_repair_device(igaos_pdhg_problem* p, const double* x, const double* y_it,
+                                  double col_tol, double tol, double* y, int* certified,
+                                  double* metrics6) {
+    if (!p || !p->eng || !x || !y_it || !y || !certified)
+        return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (!(col_tol >= 0.0)) return fail(IGAOS_PDHG_ERR_INVALID, "col_tol must be >= 0");
+    if (!(tol > 0.0)) return fail(IGAOS_PDHG_ERR_INVALID, "tol must be > 0");
+    return guarded([&] {
+        double m6[6];
+        *certified = p->eng->repair_device(x, y_it, col_tol, tol, y, m6) ? 1 : 0;
+        if (metrics6) std::memcpy(metrics6, m6, sizeof(m6));
+    });
+}
+
 int igaos_pdhg_spmv(igaos_pdhg_problem* p, int transpose, int precision, const double* x,
                     double* y) {
     if (!p || !p->eng || !x || !y) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");

@@ -3,10 +3,12 @@
 // work moved onto the device (kernels.cuh) and replayed from CUDA graphs.
 #include "engine.hpp"
 #include "kernels.cuh"
+#include "repair_dev.cuh"
 
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <thread>
@@ -200,6 +202,9 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     base_.rmax = vec(rmax, pr_);
     base_.cmax = 0.0;
     for (int j = 0; j < n; ++j) base_.cmax = std::max(base_.cmax, std::fabs(c[j]));
+    // IGAOS_PDHG_REPAIR=device: the matrix-free device repair for every m
+    // (by default it serves m > kRepairMaxRows only)
+    if (const char* e = std::getenv("IGAOS_PDHG_REPAIR")) force_dev_repair_ = std::strcmp(e, "device") == 0;
     if (m <= kRepairMaxRows) {  // host copy for dual repair (original units and order)
         hlp_.reset(new HostLP());
         HostLP& h = *hlp_;
@@ -580,6 +585,49 @@ bool Engine::try_repair(const Vecs& v, int p, bool anch, const DevMetrics& ma,
         if (verbosity > 1)
             std::fprintf(stderr, "[pdhg-gb300] dual repair @k=%lld candidate %d (pinf %.2e prow %.2e "
                                  "dinf %.2e)\n", k, cnd, t->pinf, t->prow, t->dinf);
+        if (!hlp_ || force_dev_repair_) {  // matrix-free repair on the device
+            ensure_rep();
+            const double *xs, *ys;
+            if (anch) {
+                xs = cnd == 1 ? anc_.xf[1] : anc_.xb;
+                ys = cnd == 1 ? anc_.yf[1] : anc_.yf[0];
+            } else if constexpr (std::is_same<T, double>::value) {
+                xs = cnd == 1 ? w.xavg[p] : w.xb;
+                ys = cnd == 1 ? w.yavg[p] : w.y[p];
+            } else {
+                k_convert<T, double><<<grid_for(n), kThreads, 0, st_>>>(n, cnd == 1 ? w.xavg[p] : w.xb,
+                                                                       rep_.xs);
+                k_convert<T, double><<<grid_for(m), kThreads, 0, st_>>>(m, cnd == 1 ? w.yavg[p] : w.y[p],
+                                                                       rep_.ys);
+                CU(cudaGetLastError());
+                xs = rep_.xs;
+                ys = rep_.ys;
+            }
+            for (const double col_tol : {1e-6, 1e-1}) {
+                DevMetrics mt{};
+                const bool ok = repair_dev(xs, ys, col_tol, tol, verbosity, mt);
+                if (verbosity > 1)
+                    std::fprintf(stderr, "[pdhg-gb300] device dual repair col_tol %.0e: gap %.3e\n",
+                                 col_tol, ok ? mt.gap : std::numeric_limits<double>::infinity());
+                if (!ok) continue;
+                std::vector<double> hx(n), hy(m);
+                CU(cudaMemcpyAsync(hx.data(), xs, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+                CU(cudaMemcpyAsync(hy.data(), rep_.ybest, sizeof(double) * m, cudaMemcpyDeviceToHost,
+                                   st_));
+                CU(cudaStreamSynchronize(st_));
+                out.rx.assign(n, 0.0);
+                out.ry.assign(m, 0.0);
+                for (int j = 0; j < n; ++j) out.rx[pc_[j]] = hx[j] * hp_dc_[j];
+                for (int i = 0; i < m; ++i) out.ry[pr_[i]] = hy[i] / hp_dr_[i];
+                out.last = mt;
+                out.last_is_avg = cnd == 1;
+                out.use_inc = false;
+                out.repaired = true;
+                out.status = IGAOS_STATUS_NEAR_OPTIMAL;
+                return true;
+            }
+            continue;
+        }
         // candidate in original units, device numbering
         std::vector<double> hx(n), hy(m);
         if (anch) {  // full FP64 iterates of this check (anchor + delta)
@@ -637,6 +685,159 @@ bool Engine::try_repair(const Vecs& v, int p, bool anch, const DevMetrics& ma,
         }
     }
     return false;
+}
+
+void Engine::ensure_rep() {
+    if (have_rep_) return;
+    rep_.d = ar_.alloc<double>(n);
+    rep_.r = ar_.alloc<double>(n);
+    rep_.q = ar_.alloc<double>(n);
+    rep_.step = ar_.alloc<double>(n);
+    rep_.nrm2 = ar_.alloc<double>(n);
+    rep_.xs = ar_.alloc<double>(n);
+    rep_.sgn = ar_.alloc<signed char>(n);
+    rep_.inj = ar_.alloc<unsigned char>(n);
+    rep_.rm = ar_.alloc<unsigned char>(m);
+    rep_.y = ar_.alloc<double>(m);
+    rep_.z = ar_.alloc<double>(m);
+    rep_.t = ar_.alloc<double>(m);
+    rep_.p = ar_.alloc<double>(m);
+    rep_.ybest = ar_.alloc<double>(m);
+    rep_.ys = ar_.alloc<double>(m);
+    rep_.s = ar_.alloc<double>(16);
+    CU(cudaMallocHost(&rep_.h, 16 * sizeof(double)));
+    have_rep_ = true;
+}
+
+void Engine::rep_sum(const double* v, const double* w, const unsigned char* mask, int len,
+                     double* out) {
+    ++launches_;
+    k_rep_sum<<<red_blocks_, kThreads, 0, st_>>>(
+        RepSum{v, w, mask, len, red_part_, out, ticket_ + 1});
+    CU(cudaGetLastError());
+}
+
+// CGLS for min ||(A~^T z)_J + d_J||^2 + ridge ||z||^2 from z = 0 over the
+// rows k_rep_rowmask frees at the current dual, with r = -d_J already in
+// rep_.r and the ridge in s[6]; scalars stay on the device (a converged or
+// broken-down iteration turns the rest into no-ops).
+void Engine::rep_cgls(int iters, double rtol) {
+    RepBufs& b = rep_;
+    const int gm = grid_for(m), gn = grid_for(n), gmn = grid_for(std::max(m, n));
+    CU(cudaMemsetAsync(b.z, 0, sizeof(double) * m, st_));
+    k_rep_rowmask<<<gm, kThreads, 0, st_>>>(m, b.y, base_.rmin, base_.rmax, b.rm);
+    spmv_dev<double>(false, b.r, b.t);            // t = P A~ r (r is 0 off J)
+    k_rep_grad<<<gm, kThreads, 0, st_>>>(m, b.s, b.z, b.rm, b.t);
+    k_rep_dir<<<gm, kThreads, 0, st_>>>(m, b.s, b.t, b.p, 1);
+    rep_sum(b.t, b.t, nullptr, m, b.s + 0);        // gamma
+    k_rep_cg_init<<<1, 1, 0, st_>>>(b.s);
+    for (int k = 0; k < iters; ++k) {
+        spmv_dev<double>(true, b.p, b.q);         // q = (A~^T p)_J
+        k_rep_mask<<<gn, kThreads, 0, st_>>>(n, b.inj, b.q);
+        rep_sum(b.q, b.q, nullptr, n, b.s + 9);    // ||q||^2
+        rep_sum(b.p, b.p, nullptr, m, b.s + 11);   // ||p||^2
+        k_rep_cg_alpha<<<1, 1, 0, st_>>>(b.s, rtol * rtol);
+        k_rep_zr<<<gmn, kThreads, 0, st_>>>(m, n, b.s, b.p, b.z, b.q, b.r);
+        spmv_dev<double>(false, b.r, b.t);        // t = A~ r - ridge z
+        k_rep_grad<<<gm, kThreads, 0, st_>>>(m, b.s, b.z, b.rm, b.t);
+        rep_sum(b.t, b.t, nullptr, m, b.s + 13);   // gamma'
+        k_rep_cg_beta<<<1, 1, 0, st_>>>(b.s);
+        k_rep_dir<<<gm, kThreads, 0, st_>>>(m, b.s, b.t, b.p, 0);
+        launches_ += 7;
+    }
+    CU(cudaGetLastError());
+}
+
+// Matrix-free dual repair (see repair_dev.cuh) of the candidate (xs, ys_it),
+// scaled FP64 device vectors in device numbering. On success the certified
+// scaled dual is in rep_.ybest and mt holds its metrics.
+bool Engine::repair_dev(const double* xs, const double* ys_it, double col_tol, double tol,
+                        int verbosity, DevMetrics& mt) {
+    ensure_rep();
+    RepBufs& b = rep_;
+    const int gm = grid_for(m), gn = grid_for(n);
+    constexpr int kRounds = 150;  // per anchor
+    constexpr int kStall = 40;
+    constexpr int kCg = 40;
+    constexpr double kCgTol = 1e-10;
+    k_rep_cols<<<gn, kThreads, 0, st_>>>(n, cp_, acx_, xs, dc_, base_.cl, base_.cu, col_tol, b.sgn,
+                                         b.inj, b.nrm2);
+    rep_sum(b.nrm2, nullptr, b.inj, n, b.s + 9);  // trace of A~_J A~_J^T, |J|
+    CU(cudaMemcpyAsync(b.h, b.s, 16 * sizeof(double), cudaMemcpyDeviceToHost, st_));
+    CU(cudaStreamSynchronize(st_));
+    const double trace = b.h[9];
+    const long long nj = (long long)b.h[10];
+    b.h[6] = trace > 0 ? 1e-10 * trace / m : 1e-14;  // ridge (src/pdhg/pdhg.cu:335-337)
+    CU(cudaMemcpyAsync(b.s + 6, b.h + 6, sizeof(double), cudaMemcpyHostToDevice, st_));
+    double best_gap = std::numeric_limits<double>::infinity();
+    bool certified = false;
+    for (int anchor = 0; anchor < 2 && !certified; ++anchor) {
+        k_rep_start<<<gm, kThreads, 0, st_>>>(m, anchor == 0 ? ys_it : nullptr, base_.rmin,
+                                              base_.rmax, b.y);
+        bool finite_seen = false;
+        for (int it = 0; it < kRounds; ++it) {
+            // an anchor whose duals stay uncertifiable (infinite gap) for
+            // kStall rounds is abandoned
+            if (it == kStall && !finite_seen) break;
+            if (nj > 0) {  // onto d_J = 0
+                spmv_dev<double>(true, b.y, b.d);
+                k_rep_rinit<<<gn, kThreads, 0, st_>>>(n, base_.sc, b.d, b.inj, b.r);
+                rep_cgls(kCg, kCgTol);
+                k_rep_addz<<<gm, kThreads, 0, st_>>>(m, b.z, b.y);
+            }
+            // onto the violated sign half-spaces, then the row cone
+            spmv_dev<double>(true, b.y, b.d);
+            k_rep_sign<<<gn, kThreads, 0, st_>>>(n, base_.sc, b.d, b.sgn, b.nrm2, b.step);
+            k_rep_rows<<<gm, kThreads, 0, st_>>>(m, ap_, ai_, ax_, b.step, base_.rmin, base_.rmax,
+                                                 b.y);
+            launches_ += 5;
+            CU(cudaGetLastError());
+            kkt<double>(base_, xs, b.y, xs, b.y, 1);
+            const DevMetrics t = h_met_[0];
+            if (verbosity > 2 && it % 25 == 0)
+                std::fprintf(stderr, "[pdhg-gb300] device repair anchor %d round %d: gap %.3e "
+                                     "dinf %.3e\n", anchor, it, t.gap, t.dinf);
+            finite_seen = finite_seen || std::isfinite(t.gap);
+            if (std::isfinite(t.gap) && t.gap < best_gap) {
+                best_gap = t.gap;
+                mt = t;
+                CU(cudaMemcpyAsync(b.ybest, b.y, sizeof(double) * m, cudaMemcpyDeviceToDevice, st_));
+                if (t.pinf <= tol && t.prow <= tol && t.gap <= tol) {
+                    certified = true;
+                    break;
+                }
+            }
+        }
+    }
+    if (!std::isfinite(best_gap))
+        CU(cudaMemcpyAsync(b.ybest, b.y, sizeof(double) * m, cudaMemcpyDeviceToDevice, st_));
+    CU(cudaStreamSynchronize(st_));
+    return certified;
+}
+
+bool Engine::repair_device(const double* x, const double* y_it, double col_tol, double tol,
+                           double* y, double* out6) {
+    ensure_rep();
+    std::vector<double> xs(n), ys(m);
+    for (int j = 0; j < n; ++j) xs[j] = x[pc_[j]] / hp_dc_[j];
+    for (int i = 0; i < m; ++i) ys[i] = y_it[pr_[i]] * hp_dr_[i];
+    CU(cudaMemcpyAsync(rep_.xs, xs.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st_));
+    CU(cudaMemcpyAsync(rep_.ys, ys.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st_));
+    DevMetrics mt{};
+    mt.gap = std::numeric_limits<double>::infinity();
+    const bool ok = repair_dev(rep_.xs, rep_.ys, col_tol, tol, 0, mt);
+    CU(cudaMemcpyAsync(ys.data(), rep_.ybest, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
+    CU(cudaStreamSynchronize(st_));
+    for (int i = 0; i < m; ++i) y[pr_[i]] = ys[i] / hp_dr_[i];
+    kkt<double>(base_, rep_.xs, rep_.ybest, rep_.xs, rep_.ybest, 1);
+    const DevMetrics& t = h_met_[0];
+    out6[0] = t.pinf;
+    out6[1] = t.dinf;
+    out6[2] = t.gap;
+    out6[3] = t.op;
+    out6[4] = t.od;
+    out6[5] = t.prow;
+    return ok;
 }
 
 bool Engine::repair(const double* x, const double* Ax, const double* y_it, double col_tol,
@@ -723,7 +924,7 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
             if (passes(ma)) { out.last = ma; out.last_is_avg = true; out.status = IGAOS_STATUS_NEAR_OPTIMAL; break; }
             // dual repair of a converged candidate whose dual bound is not
             // certified (src/pdhg/pdhg.cu:854-931), on the reference's schedule
-            if (hlp_ && k_done >= 5000 && k_done >= next_repair) {
+            if (k_done >= 5000 && k_done >= next_repair) {
                 next_repair = k_done + repair_spacing;
                 repair_spacing = std::min(repair_spacing * 3, 30000LL);
                 if (try_repair<T>(v, p, anch, ma, have_inc ? &inc : nullptr, o.tol, o.verbosity,

@@ -143,6 +143,11 @@ class Engine {
     // units, caller's numbering
     bool repair(const double* x, const double* Ax, const double* y_it, double col_tol,
                 double* y);
+    // matrix-free dual repair on the device (any m): original units, caller's
+    // numbering; certified when pinf, prow and a finite gap are <= tol.
+    // out6 = pinf, dinf, gap, op, od, prow of (x, y).
+    bool repair_device(const double* x, const double* y_it, double col_tol, double tol, double* y,
+                       double* out6);
 
    private:
     int device_ = 0;
@@ -208,6 +213,23 @@ class Engine {
     template <typename T>
     bool try_repair(const Vecs& v, int p, bool anch, const DevMetrics& ma, const DevMetrics* inc,
                     double tol, int verbosity, long long k, LoopOut& out);
+    // matrix-free dual repair (device path; csrc/repair_dev.cuh)
+    struct RepBufs {
+        double *d, *r, *q, *step, *nrm2, *xs;  // n
+        signed char* sgn;
+        unsigned char *inj, *rm;  // inner columns (n), movable rows (m)
+        double *y, *z, *t, *p, *ybest, *ys;    // m
+        double* s;                             // CGLS scalars (16)
+        double* h;                             // pinned mirror of s
+    };
+    RepBufs rep_{};
+    bool have_rep_ = false;
+    bool force_dev_repair_ = false;
+    void ensure_rep();
+    void rep_sum(const double* v, const double* w, const unsigned char* mask, int len, double* out);
+    void rep_cgls(int iters, double rtol);
+    bool repair_dev(const double* xs, const double* ys_it, double col_tol, double tol,
+                    int verbosity, DevMetrics& mt);
     Anchor anc_{};
     Vecs av_{};
     bool have_anchor_ = false;

@@ -296,6 +296,81 @@ def mixed_bounds_lp(m: int, n: int, extra_nnz: int, seed: int) -> LPData:
     return lp
 
 
+def known_optimum_lp(m: int, n: int, extra_nnz: int, seed: int):
+    """LP with the sparsity, bound and row types of mixed_bounds_lp and a
+    known optimal pair (x*, y*): columns strictly inside their bounds (all
+    free ones) have zero reduced cost, columns at a bound a reduced cost of
+    the sign that bound allows; rows with y*_i != 0 are tight at the bound
+    matching its sign, the others slack. Returns (lp, x*, y*); in the
+    convention d = c + A^T y the gap of (x*, y*) is zero."""
+    rng = np.random.default_rng(seed)
+    r0 = rng.integers(0, m, n)
+    r1 = rng.integers(0, m, extra_nnz)
+    c1 = rng.integers(0, n, extra_nnz)
+    rows, cols = _dedupe(np.concatenate([r0, r1]), np.concatenate([np.arange(n), c1]))
+    vals = rng.standard_normal(rows.shape[0])
+    kind = rng.integers(0, 5, n)  # 0 free, 1 lower, 2 upper, 3 box, 4 fixed
+    base = rng.uniform(-2.0, 2.0, n)
+    cl = np.full(n, -INF)
+    cu = np.full(n, INF)
+    lo_set = (kind == 1) | (kind == 3)
+    up_set = (kind == 2) | (kind == 3)
+    cl[lo_set] = base[lo_set] - rng.uniform(0.5, 1.5, lo_set.sum())
+    cu[up_set] = base[up_set] + rng.uniform(0.5, 1.5, up_set.sum())
+    cl[kind == 4] = cu[kind == 4] = base[kind == 4]
+    # where x* sits: 0 inside, 1 at the lower bound, 2 at the upper bound
+    at = np.zeros(n, np.int64)
+    pick = rng.integers(0, 3, n)
+    at[(kind == 1) & (pick > 0)] = 1
+    at[(kind == 2) & (pick > 0)] = 2
+    at[kind == 3] = pick[kind == 3]
+    at[kind == 4] = 1
+    xs = base.copy()
+    xs[at == 1] = cl[at == 1]
+    xs[at == 2] = cu[at == 2]
+    lp = from_triplets(m, n, rows, cols, vals, np.zeros(n), cl, cu, np.zeros(m), np.zeros(m),
+                       name=f"known-{seed}", presorted=True)
+    ax = _csr_matvec(lp, xs)
+    rk = rng.integers(0, 4, m)  # 0 E, 1 L, 2 G, 3 ranged
+    tight = rng.integers(0, 2, m) == 1
+    ys = np.zeros(m)
+    rmin = np.full(m, -INF)
+    rmax = np.full(m, INF)
+    e = rk == 0
+    rmin[e] = rmax[e] = ax[e]
+    ys[e] = rng.standard_normal(e.sum())
+    for k, sgn in ((1, 1.0), (2, -1.0)):
+        sel = rk == k
+        t, f = sel & tight, sel & ~tight
+        ys[t] = sgn * rng.uniform(0.1, 2.0, t.sum())
+        if k == 1:
+            rmax[t] = ax[t]
+            rmax[f] = ax[f] + rng.uniform(0.1, 1.0, f.sum())
+        else:
+            rmin[t] = ax[t]
+            rmin[f] = ax[f] - rng.uniform(0.1, 1.0, f.sum())
+    r_ = rk == 3
+    side = rng.integers(0, 3, m)  # 0 slack, 1 tight at rmax, 2 tight at rmin
+    rmin[r_] = ax[r_] - rng.uniform(0.1, 1.0, r_.sum())
+    rmax[r_] = ax[r_] + rng.uniform(0.1, 1.0, r_.sum())
+    hi_t, lo_t = r_ & (side == 1), r_ & (side == 2)
+    rmax[hi_t] = ax[hi_t]
+    ys[hi_t] = rng.uniform(0.1, 2.0, hi_t.sum())
+    rmin[lo_t] = ax[lo_t]
+    ys[lo_t] = -rng.uniform(0.1, 2.0, lo_t.sum())
+    aty = np.zeros(n)
+    rr = np.repeat(np.arange(m), np.diff(lp.ap))
+    np.add.at(aty, lp.ai, lp.ax * ys[rr])
+    s = np.zeros(n)
+    s[at == 1] = rng.uniform(0.1, 2.0, (at == 1).sum())
+    s[at == 2] = -rng.uniform(0.1, 2.0, (at == 2).sum())
+    s[kind == 4] = rng.standard_normal((kind == 4).sum())
+    lp.c = s - aty
+    lp.rmin, lp.rmax = rmin, rmax
+    lp.meta = dict(seed=seed)
+    return lp, xs, ys
+
+
 def free_cost_lp(m: int, n: int, extra_nnz: int, seed: int) -> LPData:
     """The bound and row structure of mixed_bounds_lp, with costs that give
     free and one-sided columns nonzero reduced-cost pressure: c = -A^T y* + s

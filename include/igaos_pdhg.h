@@ -186,6 +186,23 @@ int igaos_pdhg_iterate(igaos_pdhg_problem* p, int precision, int64_t iters,
 int igaos_pdhg_dual_repair(igaos_pdhg_problem* p, const double* x, const double* Ax,
                            const double* y_it, double col_tol, double* y, int* certified);
 
+/* Matrix-free dual repair on the device, for any m (the solve loop uses it
+ * in place of igaos_pdhg_dual_repair when m > 4096, on the same schedule).
+ * Same three sets as the reference's dual_repair (src/pdhg/pdhg.cu:288-448)
+ * on the Ruiz-scaled LP: the regularised least-squares step onto
+ * {A_J^T y = -c_J} by CGLS instead of a dense Cholesky solve, all violated
+ * sign half-spaces at once (component-averaged) instead of one at a time,
+ * then the row cone; two anchors (y_it, 0), up to 150 rounds each, stopping
+ * at the first dual certified at `tol`. x and y_it in ORIGINAL units, the
+ * caller's numbering. *certified = 1 when pinf, prow and a finite gap of
+ * (x, y) are all <= tol; y = the dual with the smallest finite gap seen
+ * (else the last iterate). metrics6 (may be NULL) = pinf, dinf, gap, op, od,
+ * prow of (x, y). No reference counterpart: the reference's dense repair is
+ * limited by its m x m factor. */
+int igaos_pdhg_dual_repair_device(igaos_pdhg_problem* p, const double* x, const double* y_it,
+                                  double col_tol, double tol, double* y, int* certified,
+                                  double* metrics6);
+
 /* FP64 KKT metrics of (x, y) given in ORIGINAL units, evaluated on the
  * device (the fused pass replacing src/pdhg/pdhg.cu:173-254 + :698-733).
  * out6 = {pinf, dinf, gap, op, od, prow}. */
