@@ -206,8 +206,8 @@ __device__ __forceinline__ void block_sum(double (&v)[NV], double* sh) {
 }
 
 // Same tree in the working precision (FP32 partials of FP32 kernels; the
-// cross-CTA finish is FP64). `sh` needs kWarps * NV values of type T.
-template <typename T, int NV>
+// cross-CTA finish is FP64). `sh` needs NW * NV values of type T.
+template <typename T, int NV, int NW = kWarps>
 __device__ __forceinline__ void block_sum_t(T (&v)[NV], T* sh) {
     const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
 #pragma unroll
@@ -222,7 +222,7 @@ __device__ __forceinline__ void block_sum_t(T (&v)[NV], T* sh) {
 #pragma unroll
         for (int q = 0; q < NV; ++q) {
             T s = 0;
-            for (int k = 0; k < kWarps; ++k) s += sh[k * NV + q];
+            for (int k = 0; k < NW; ++k) s += sh[k * NV + q];
             v[q] = s;
         }
     }
@@ -325,7 +325,9 @@ struct PlainEpi {
 // loads of a batch, then its gathers in flight), the G-lane shuffle reduction, and the row step
 // (epi.apply) from lane i for the item's i-th row, so consecutive lanes touch
 // consecutive vector entries.
-template <typename T, class E>
+// kCoherent: gather x through L2 (ld.global.cg), for vectors that other CTAs
+// rewrite while this kernel runs (the read-only path may hold stale lines).
+template <typename T, class E, bool kCoherent = false>
 __device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
                                           const T* __restrict__ x, int w, E& epi) {
     const int lane = threadIdx.x & 31;
@@ -353,7 +355,7 @@ __device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
             }
             T xv[kLaneBatch];
 #pragma unroll
-            for (int u = 0; u < kLaneBatch; ++u) xv[u] = __ldg(x + j[u]);
+            for (int u = 0; u < kLaneBatch; ++u) xv[u] = kCoherent ? __ldcg(x + j[u]) : __ldg(x + j[u]);
 #pragma unroll
             for (int u = 0; u < kLaneBatch; ++u) acc.add(a[u], xv[u]);  // masked: 0 * x[0] adds 0
         }
@@ -371,6 +373,15 @@ __device__ __forceinline__ void warp_rows_all(const WarpSched& ws, const Csr<T>&
     const int stride = gridDim.x * kWarps;
     for (int w = blockIdx.x * kWarps + (threadIdx.x >> 5); w < ws.nwarps; w += stride)
         warp_item<T>(ws, A, x, w, epi);
+}
+
+// The items w0, w0 + stride, ... of the schedule (a warp's share when the
+// warps of several CTAs split one schedule), x gathered through L2.
+template <typename T, class E>
+__device__ __forceinline__ void warp_rows_coherent(const WarpSched& ws, const Csr<T>& A,
+                                                   const T* __restrict__ x, E& epi, int w0,
+                                                   int stride) {
+    for (int w = w0; w < ws.nwarps; w += stride) warp_item<T, E, true>(ws, A, x, w, epi);
 }
 
 }  // namespace igx

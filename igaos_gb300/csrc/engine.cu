@@ -4,6 +4,7 @@
 #include "engine.hpp"
 #include "kernels.cuh"
 #include "repair_dev.cuh"
+#include "cluster.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -65,6 +66,27 @@ void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<u
         wrow.push_back(r);
         wlg.push_back((unsigned char)lg);
     }
+}
+
+// Per-rank staged entries and row-pointer slots of a schedule for the cluster
+// attempt kernel (rank r's warps take items r * kSmallWarps + wi + k *
+// kSmallCluster * kSmallWarps); false when a warp would hold more than
+// kSmallItems items.
+static bool small_share(const int* ptr, int rows, std::vector<long long>& ent,
+                        std::vector<long long>& slots) {
+    std::vector<int> wr;
+    std::vector<unsigned char> wl;
+    build_warps(ptr, rows, wr, wl);
+    const int nw = (int)wl.size(), stride = kSmallCluster * kSmallWarps;
+    if (nw > stride * kSmallItems) return false;
+    ent.assign(kSmallCluster, 0);
+    slots.assign(kSmallCluster, 0);
+    for (int w = 0; w < nw; ++w) {
+        const int r = (w % stride) / kSmallWarps;
+        ent[r] += ptr[wr[w + 1]] - ptr[wr[w]];
+        slots[r] += wr[w + 1] - wr[w] + 1;
+    }
+    return true;
 }
 
 // Launch width: enough CTAs for every warp item, capped at what stays
@@ -181,11 +203,35 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
         const int resident = std::max(1, sms) * kHotCtasPerSm;
         sA_ = upload_sched(ar_, P.data(), m, resident);
+        std::vector<long long> ent_a, slot_a, ent_at, slot_at;
+        bool fit = small_share(P.data(), m, ent_a, slot_a);
         permute_csr(n, cp, ci, acx, pc_, ipr_, P, I, V);
         CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(ci_, I.get(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(acx_, V.get(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
         sAT_ = upload_sched(ar_, P.data(), n, resident);
+        fit = small_share(P.data(), n, ent_at, slot_at) && fit;
+        // small LPs: the attempts of a chunk in one thread-block cluster with
+        // the LP staged in its shared memory (cluster.cuh) when the largest
+        // rank's share fits. FP32 only by default: on the 2,000 x 5,000 LP an
+        // FP32 attempt takes 7.9 us there against 12.1 us on the grid-wide
+        // kernels, an FP64 attempt 17.9 us against 17.3 us (FP64 arithmetic
+        // on 8 SMs). IGAOS_PDHG_CLUSTER=0: never; =all: FP64 too.
+        const char* e = std::getenv("IGAOS_PDHG_CLUSTER");
+        const bool allow = !(e && std::strcmp(e, "0") == 0);
+        const bool with64 = e && std::strcmp(e, "all") == 0;
+        if (allow && fit) {
+            for (int k = 0; k < (with64 ? 2 : 1); ++k) {
+                const int sz = k ? 8 : 4;
+                size_t worst = 0;
+                for (int r = 0; r < kSmallCluster; ++r)
+                    worst = std::max(worst, small_smem_bytes(m, n,
+                                                             SmallLayout{ent_at[r], slot_at[r], ent_a[r],
+                                                                         slot_a[r]},
+                                                             sz));
+                if (worst <= kSmallSmemMax) small_bytes_[k] = (int)worst;
+            }
+        }
     }
     // vectors
     auto vec = [&](const double* h, const std::vector<int>& perm) {
@@ -234,6 +280,8 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     base_.frmax = ar_.alloc<float>(m);
     dr_ = ar_.alloc<double>(m);
     dc_ = ar_.alloc<double>(n);
+    idr_ = ar_.alloc<double>(m);
+    idc_ = ar_.alloc<double>(n);
     // control + scratch
     ctl_ = ar_.alloc<DevCtl>(1);
     met_ = ar_.alloc<DevMetrics>(2);
@@ -315,6 +363,8 @@ void Engine::setup_scaling() {
     k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.c, dc_, 1, base_.sc, base_.fc);
     k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cl, dc_, 0, base_.scl, base_.fcl);
     k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cu, dc_, 0, base_.scu, base_.fcu);
+    k_recip<<<grid_for(m), kThreads, 0, st_>>>(m, dr_, idr_);
+    k_recip<<<grid_for(n), kThreads, 0, st_>>>(n, dc_, idc_);
     CU(cudaGetLastError());
     hp_dr_.resize(m);
     hp_dc_.resize(n);
@@ -388,8 +438,8 @@ void Engine::ensure_work() {
     w.pesx = ar_.alloc<T>(n);
     w.yb = ar_.alloc<T>(m);
     w.pesy = ar_.alloc<T>(m);
-    w.part_p = ar_.alloc<double>(sAT_.ctas);
-    w.part_d = ar_.alloc<double>(2 * (size_t)sA_.ctas);
+    w.part_p = ar_.alloc<double>(std::max(sAT_.ctas, kSmallCluster));
+    w.part_d = ar_.alloc<double>(2 * (size_t)std::max(sA_.ctas, kSmallCluster));
     have = true;
 }
 
@@ -451,6 +501,14 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     da.fac = fac_;
     da.n_fac = kFac;
     da.ctl = ctl_;
+    if (const int sb = small_bytes_[std::is_same<T, double>::value ? 1 : 0]) {
+        // one cluster runs the whole chunk with the LP in shared memory
+        ++launches_;
+        CU(cudaFuncSetAttribute(k_attempts_cluster<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, sb));
+        k_attempts_cluster<T><<<kSmallCluster, kSmallThreads, sb, st_>>>(pa, da, m, n, count);
+        CU(cudaGetLastError());
+        return;
+    }
     launches_ += 2LL * count;
     auto enqueue = [&](int cnt) {
         for (int a = 0; a < cnt; ++a) {
@@ -545,6 +603,8 @@ void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* 
     ka.y[1] = y1;
     ka.dr = dr_;
     ka.dc = dc_;
+    ka.idr = idr_;
+    ka.idc = idc_;
     ka.c = v.c;
     ka.cl = v.cl;
     ka.cu = v.cu;

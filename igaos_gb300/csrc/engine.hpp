@@ -159,6 +159,7 @@ class Engine {
     float *ax32_, *acx32_;
     Sched sA_, sAT_;
     double *dr_, *dc_;
+    double *idr_, *idc_;  // reciprocals of the scaling, for the KKT kernels
     Vecs base_{};
     // device numbering: new index -> original (pr_, pc_) and inverses
     std::vector<int> pr_, pc_, ipr_, ipc_;
@@ -225,6 +226,9 @@ class Engine {
     RepBufs rep_{};
     bool have_rep_ = false;
     bool force_dev_repair_ = false;
+    // dynamic shared memory of the cluster attempt kernel for FP32 / FP64
+    // (0: that precision uses the grid-wide kernels)
+    int small_bytes_[2] = {0, 0};
     void ensure_rep();
     void rep_sum(const double* v, const double* w, const unsigned char* mask, int len, double* out);
     void rep_cgls(int iters, double rtol);

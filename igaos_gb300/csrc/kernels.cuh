@@ -70,11 +70,19 @@ struct PrimalArgs {
 // xavg' = xavg + w (x' - xavg), w = 2/(hn+2) (kern_mix2, :129-141, :795-799),
 // written to the other parity slot so that a rejected attempt leaves the
 // accepted state untouched.
-template <typename T>
+// Hook called with each row's new gathered-vector entry (xbar_j, y'_i):
+// nothing for the grid-wide kernels.
+struct NoBcast {
+    template <typename U>
+    __device__ __forceinline__ void operator()(int, U) const {}
+};
+
+template <typename T, class B = NoBcast>
 struct PrimalEpi {
     const T *c, *lo, *hi, *xc, *xa;
     T *xn_out, *xa_out, *xbar;
     T tau, w, dx2;
+    B bc{};
     struct Pre {
         T c, lo, hi, x, xa;
     };
@@ -85,7 +93,9 @@ struct PrimalEpi {
         const T g = v.c + acc.result();
         const T xn = fmin(fmax(fma(-tau, g, v.x), v.lo), v.hi);
         xn_out[j] = xn;
-        xbar[j] = fma((T)2, xn, -v.x);
+        const T xb = fma((T)2, xn, -v.x);
+        xbar[j] = xb;
+        bc(j, xb);
         const T dx = xn - v.x;
         dx2 = fma(dx, dx, dx2);
         xa_out[j] = fma(w, xn - v.xa, v.xa);
@@ -134,11 +144,12 @@ struct DualArgs {
 // FP64 anchor yhat; the dual projection must act on the full value, so the
 // clamp argument is (t + yhat)/sigma with t = dy + sigma A dxbar and the row
 // bounds shifted by the anchor's activity. yhat == nullptr: plain iterates.
-template <typename T>
+template <typename T, class B = NoBcast>
 struct DualEpi {
     const T *rmin, *rmax, *yc, *axc, *ya, *yhat;
     T *yn_out, *axc_out, *ya_out;
     T sigma, w, dy2, cross;
+    B bc{};
     struct Pre {
         T lo, hi, y, ax, ya, yh;
     };
@@ -152,6 +163,7 @@ struct DualEpi {
         const T arg = yhat ? (t + v.yh) / sigma : t / sigma;
         const T yn = fma(-sigma, fmin(fmax(arg, v.lo), v.hi), t);
         yn_out[i] = yn;
+        bc(i, yn);
         const T dy = yn - v.y;
         const T adx = (T)0.5 * (ab - v.ax);
         axc_out[i] = v.ax + adx;
@@ -332,6 +344,12 @@ __global__ void k_scale_matrix(int rows, const int* __restrict__ ptr, const int*
 }
 
 // s = v / d (bounds) or v * d (cost), elementwise, FP64 and FP32 copies.
+// out = 1 / d (IEEE quotient, as the inline 1.0 / d it replaces)
+__global__ void k_recip(int n, const double* __restrict__ d, double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = __ddiv_rn(1.0, d[i]);
+}
+
 __global__ void k_scale_vec(int n, const double* __restrict__ v, const double* __restrict__ d,
                             int mul, double* __restrict__ out, float* __restrict__ out32) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
@@ -430,6 +448,11 @@ __global__ void k_convert(int n, const TI* __restrict__ in, TO* __restrict__ out
 //   rowdual: row part of the Lagrangian bound (needs max |y| for its noise
 //            threshold) and the final metrics.
 
+// IGX_KKT_RECIP_DC: reduced costs d = c + (A~^T y~) * (1/dc) instead of the
+// quotient (within an ulp of it); FP64 division is slow on this part.
+#ifndef IGX_KKT_RECIP_DC
+#define IGX_KKT_RECIP_DC 0
+#endif
 template <typename T>
 struct KktArgs {
     WarpSched wsA, wsAT;
@@ -437,6 +460,7 @@ struct KktArgs {
     const T* x[2];
     const T* y[2];
     const double *dr, *dc;
+    const double *idr, *idc;                  // 1 / dr, 1 / dc (IEEE quotients)
     const double *c, *cl, *cu, *rmin, *rmax;  // original units
     const T *slo, *shi;                       // scaled column bounds, iterate precision
     double cmax;
@@ -458,11 +482,13 @@ __global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_rows(KktArgs<T>
         pv = smax(pv, vi);
         pa = smax(pa, fabs(smin(smax(Ax, lo), hi)));
         const double viol = smax(0.0, vi);
-        double sc = fabs(Ax);
-        if (isfinite(lo)) sc = smax(sc, fabs(lo));
-        if (isfinite(hi)) sc = smax(sc, fabs(hi));
-        prow = smax(prow, viol / (1.0 + sc));
-        ymax = smax(ymax, fabs((double)yv[i] * (1.0 / a.dr[i])));
+        if (viol > 0.0) {  // viol / (1 + sc) is 0 otherwise: skip the FP64 division
+            double sc = fabs(Ax);
+            if (isfinite(lo)) sc = smax(sc, fabs(lo));
+            if (isfinite(hi)) sc = smax(sc, fabs(hi));
+            prow = smax(prow, viol / (1.0 + sc));
+        }
+        ymax = smax(ymax, fabs((double)yv[i] * a.idr[i]));
     };
     PlainEpi<decltype(f)> epi{f};
     warp_rows_all<T>(a.wsA, a.A, a.x[v], epi);
@@ -496,7 +522,11 @@ __global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_cols(KktArgs<T>
     const double dz = 1e-8 * (1.0 + a.cmax);
     double dv = 0.0, op = 0.0, od = 0.0, unb = 0.0;
     auto f = [&](int j, const Acc<T>& acc) {
+#if IGX_KKT_RECIP_DC
+        const double d = a.c[j] + acc.result_d() * a.idc[j];
+#else
         const double d = a.c[j] + 1.0 * acc.result_d() / a.dc[j];
+#endif
         const double x = unscale_x(xv[j], a.slo[j], a.shi[j], a.dc[j], a.cl[j], a.cu[j]);
         const double cl = a.cl[j], cu = a.cu[j];
         const double bnd = fabs(isfinite(cu) ? cu : cl);
@@ -560,7 +590,7 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rowdual(KktArgs<T> a, int m) {
     const double yz = 1e-8 * (1.0 + a.out[v].ymax);
     double od = 0.0, unb = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-        const double y = (double)yv[i] * (1.0 / a.dr[i]);
+        const double y = (double)yv[i] * a.idr[i];
         if (y > yz) {
             if (isfinite(a.rmax[i])) od -= y * a.rmax[i];
             else unb = 1.0;
