@@ -405,6 +405,24 @@ def main():
     # m-vector read of the rounded anchor y)
     prec_key = "fp64" if args.precision == "fp64" else "fp32"
     traffic = traffic_from_profile(f"fused_attempt_{prec_key}_{'c2' if s == 1.0 else 'scaled'}")
+    # The attempt's gathers are served by L2 (its working set nearly fits the
+    # 126 MB L2), so its second roofline is the random-sector rate of L2:
+    # L1-miss sectors per attempt (ncu, committed summary) against the
+    # device's measured rate for random 4-byte reads of a 2 MB vector.
+    l2 = None
+    sectors = traffic_from_profile(f"fused_attempt_{prec_key}_c2_l1_miss_sectors") if s == 1.0 else None
+    try:
+        ceiling = capi.gather_rate(19)
+    except Exception as ex:  # calibration is a report, not a gate
+        ceiling = None
+        print(f"gather-rate calibration failed: {ex}", file=sys.stderr)
+    if ceiling:
+        l2 = {"bound": "l2 random sectors", "ceiling_sectors_per_s": ceiling,
+              "ceiling_probe": "random 4-byte reads of a 2 MB resident vector (igaos_pdhg_gather_rate)"}
+        if sectors:
+            rate = sectors / (1e-3 * att_ms / att)
+            l2.update({"sectors_per_launch": sectors, "achieved_sectors_per_s": rate,
+                       "frac": rate / ceiling})
     if args.no_cpu:
         cpu_v, cpu_r = None, {"loop_seconds": 0.0}
     else:
@@ -420,7 +438,7 @@ def main():
                      "bound": "hbm", "achieved": achieved, "peak": pk, "peak_kind": pk_kind,
                      "unit": "GB/s", "frac": achieved / pk,
                      "bytes_per_launch": bpa, "launch_us": 1e3 * att_ms / att,
-                     "traffic": traffic},
+                     "traffic": traffic, "l2": l2},
         "cpu_baseline": {"value": cpu_v, "unit": "GB/s", "cores": os.cpu_count(),
                          "kind": "port",
                          "sample": f"{args.cpu_iters} iterations of the reference FP64 PDHG "

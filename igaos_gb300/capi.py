@@ -107,6 +107,7 @@ def lib():
         L.igaos_pdhg_spmv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp]
         L.igaos_pdhg_dual_repair.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, _dp,
                                              C.POINTER(C.c_int)]
+        L.igaos_pdhg_gather_rate.argtypes = [C.c_int, C.c_int, _dp]
         L.igaos_pdhg_dual_repair_device.argtypes = [C.c_void_p, _dp, _dp, C.c_double,
                                                     C.c_double, _dp, C.POINTER(C.c_int), _dp]
         L.igaos_pdhg_solve_batch.argtypes = [
@@ -125,6 +126,14 @@ def lib():
         L.igaos_pdhg_unrolled_backward.argtypes = [_lp] + [C.c_void_p] * 21
         _LIB = L
     return _LIB
+
+
+def gather_rate(log2_words: int, device: int = -1) -> float:
+    """Random 4-byte gathers per second the GPU serves from a resident vector
+    of 2**log2_words floats (igaos_pdhg_gather_rate)."""
+    out = C.c_double(0.0)
+    _check(lib().igaos_pdhg_gather_rate(int(log2_words), int(device), C.byref(out)))
+    return out.value
 
 
 def last_error() -> str:

@@ -104,6 +104,13 @@ typedef struct igaos_pdhg_problem igaos_pdhg_problem;
 /* ABI version (IGAOS_PDHG_ABI_VERSION). No reference counterpart. */
 int igaos_pdhg_abi_version(void);
 
+/* Calibration of the gather-bound roofline (no reference counterpart): the
+ * rate, in 4-byte gathers per second for the whole GPU, at which the device
+ * serves random reads of a resident zero vector of 2^log2_words floats
+ * (10..28), with 8 independent gathers in flight per thread and 8 CTAs of
+ * 256 threads per SM; best of 3 launches after a warming one. */
+int igaos_pdhg_gather_rate(int log2_words, int device, double* gathers_per_s);
+
 /* Number of visible CUDA devices (0 when none). Replaces the handle-creation
  * probe of src/pdhg/pdhg.cu:459-465. */
 int igaos_pdhg_device_count(void);

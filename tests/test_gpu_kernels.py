@@ -162,3 +162,13 @@ def test_evaluate_matches_oracle(case, orc):
                 assert g == w, k
             else:
                 assert g == pytest.approx(w, rel=1e-9, abs=1e-9), (k, g, w)
+
+
+def test_gather_rate_calibration(native):
+    """The gather-bound roofline's ceiling: random reads of an L1-resident
+    vector are served faster than of an L2-resident one, and those faster
+    than of an HBM-resident one; all rates are positive and finite."""
+    from igaos_gb300 import capi
+    l1, l2, hbm = capi.gather_rate(14), capi.gather_rate(19), capi.gather_rate(28)
+    assert all(np.isfinite(v) and v > 1e9 for v in (l1, l2, hbm)), (l1, l2, hbm)
+    assert l1 > l2 > hbm, (l1, l2, hbm)
