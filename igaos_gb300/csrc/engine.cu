@@ -68,6 +68,26 @@ void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<u
     }
 }
 
+// Whether one cluster of the attempt kernel with `bytes` of dynamic shared
+// memory can be resident on this device (else the grid-wide kernels serve).
+static bool cluster_fits(bool f64, int bytes) {
+    const void* fn = f64 ? (const void*)k_attempts_cluster<double> : (const void*)k_attempts_cluster<float>;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(kSmallCluster);
+    cfg.blockDim = dim3(kSmallThreads);
+    cfg.dynamicSmemBytes = bytes;
+    int clusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&clusters, fn, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return clusters > 0;
+}
+
 // Per-rank staged entries and row-pointer slots of a schedule for the cluster
 // attempt kernel (rank r's warps take items r * kSmallWarps + wi + k *
 // kSmallCluster * kSmallWarps); false when a warp would hold more than
@@ -229,7 +249,8 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
                                                              SmallLayout{ent_at[r], slot_at[r], ent_a[r],
                                                                          slot_a[r]},
                                                              sz));
-                if (worst <= kSmallSmemMax) small_bytes_[k] = (int)worst;
+                if (worst <= kSmallSmemMax && cluster_fits(k == 1, (int)worst))
+                    small_bytes_[k] = (int)worst;
             }
         }
     }
