@@ -307,10 +307,19 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     ctl_ = ar_.alloc<DevCtl>(1);
     met_ = ar_.alloc<DevMetrics>(2);
     CU(cudaMemsetAsync(ctl_, 0, sizeof(DevCtl), st_));
-    CU(cudaMallocHost(&h_ctl_, sizeof(DevCtl)));
-    CU(cudaMallocHost(&h_met_, 2 * sizeof(DevMetrics)));
-    CU(cudaMallocHost(&h_scal_, 16 * sizeof(double)));
-    CU(cudaMallocHost(&h_fac_, 2 * kFac * sizeof(double)));
+    {  // one pinned block for every host mirror (a pinned allocation costs ~1 ms)
+        const size_t o_met = (sizeof(DevCtl) + 63) & ~(size_t)63;
+        const size_t o_scal = o_met + ((2 * sizeof(DevMetrics) + 63) & ~(size_t)63);
+        const size_t o_fac = o_scal + 16 * sizeof(double);
+        const size_t o_rep = o_fac + 2 * kFac * sizeof(double);
+        CU(cudaMallocHost(&h_pin_, o_rep + 16 * sizeof(double)));
+        char* b = static_cast<char*>(h_pin_);
+        h_ctl_ = reinterpret_cast<DevCtl*>(b);
+        h_met_ = reinterpret_cast<DevMetrics*>(b + o_met);
+        h_scal_ = reinterpret_cast<double*>(b + o_scal);
+        h_fac_ = reinterpret_cast<double*>(b + o_fac);
+        h_rep_ = reinterpret_cast<double*>(b + o_rep);
+    }
     fac_ = ar_.alloc<double>(2 * kFac);
     std::memset(h_ctl_, 0, sizeof(DevCtl));
     red_blocks_ = grid_for(std::max(m, n), kThreads, 152 * 4);
@@ -354,10 +363,7 @@ Engine::~Engine() {
     for (auto& kv : graphs_) cudaGraphExecDestroy(kv.second);
     for (auto& e : ev_)
         if (e) cudaEventDestroy(e);
-    if (h_ctl_) cudaFreeHost(h_ctl_);
-    if (h_met_) cudaFreeHost(h_met_);
-    if (h_scal_) cudaFreeHost(h_scal_);
-    if (h_fac_) cudaFreeHost(h_fac_);
+    if (h_pin_) cudaFreeHost(h_pin_);
     if (st_) cudaStreamDestroy(st_);
 }
 
@@ -786,7 +792,7 @@ void Engine::ensure_rep() {
     rep_.ybest = ar_.alloc<double>(m);
     rep_.ys = ar_.alloc<double>(m);
     rep_.s = ar_.alloc<double>(16);
-    CU(cudaMallocHost(&rep_.h, 16 * sizeof(double)));
+    rep_.h = h_rep_;
     have_rep_ = true;
 }
 

@@ -192,6 +192,8 @@ class Engine {
     static constexpr int kFac = 512;  // step-factor table entries
     double* fac_ = nullptr;   // device (1 - k^-0.3, 1 + k^-0.6) table
     double* h_fac_ = nullptr; // pinned staging
+    void* h_pin_ = nullptr;   // the pinned block holding every host mirror
+    double* h_rep_ = nullptr; // pinned mirror of the dual repair's scalars
     long long fac_base_ = 0;  // iteration index of table entry 0 (0: empty)
     long long launches_ = 0;  // kernel launches of the current solve
 
