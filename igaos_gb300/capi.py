@@ -32,6 +32,7 @@ class Options(C.Structure):
         ("restarts", C.c_int), ("verbosity", C.c_int), ("precision", C.c_int),
         ("check_period", C.c_int), ("inner_tolerance", C.c_double),
         ("max_refinements", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
+        ("detect_infeasibility", C.c_int),
     ]
 
 

@@ -939,6 +939,118 @@ bool Engine::repair(const double* x, const double* Ax, const double* y_it, doubl
     return ok;
 }
 
+// Infeasibility certificates (no counterpart in the reference engine): the
+// change between consecutive restart points of an LP without a solution
+// tends to a ray (the iterates diverge along it), as in PDLP's test on
+// iterate differences. Tested in original units, device numbering, after
+// normalising the ray to max-norm 1:
+//   dual ray y, d = A^T y (no cost): d_j > 0 needs a finite lower bound and
+//     d_j < 0 a finite upper one, y_i > 0 a finite rmax and y_i < 0 a finite
+//     rmin; the dual objective along it, sum_j d_j (l_j or u_j) - sum_i y_i
+//     (rmax_i or rmin_i), positive => the dual is unbounded => infeasible;
+//   primal ray x, A x: x_j < 0 needs l_j = -inf, x_j > 0 needs u_j = +inf,
+//     (A x)_i < 0 needs rmin_i = -inf, > 0 needs rmax_i = +inf, and c^T x < 0
+//     => the dual is infeasible (a feasible LP is unbounded).
+// A certificate needs its sign violations below 1e-9 of the ray's scale and
+// its objective beyond 1e-6 of the objective's term magnitudes.
+template <typename T>
+int Engine::ray_check(bool anch, int p, LoopOut& out) {
+    Work<T>& w = work<T>();
+    const int gn = grid_for(n), gm = grid_for(m);
+    if (anch) {
+        k_ray_diff<double><<<gn, kThreads, 0, st_>>>(n, anc_.xh, anc_.pesx, tmp_n_);
+        k_ray_diff<double><<<gm, kThreads, 0, st_>>>(m, anc_.yh, anc_.pesy, tmp_m_);
+    } else {
+        k_ray_diff<T><<<gn, kThreads, 0, st_>>>(n, w.x[p], w.pesx, tmp_n_);
+        k_ray_diff<T><<<gm, kThreads, 0, st_>>>(m, w.y[p], w.pesy, tmp_m_);
+    }
+    launches_ += 2;
+    CU(cudaGetLastError());
+    spmv_dev<double>(true, tmp_m_, tmp_n2_);   // A~^T dy~
+    spmv_dev<double>(false, tmp_n_, tmp_m2_);  // A~ dx~
+    out.spmvs += 2;
+    std::vector<double> dx(n), dy(m), aty(n), ax(m);
+    CU(cudaMemcpyAsync(dx.data(), tmp_n_, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(dy.data(), tmp_m_, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(aty.data(), tmp_n2_, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+    CU(cudaMemcpyAsync(ax.data(), tmp_m2_, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
+    if (h_c_.empty()) {
+        auto get = [&](const double* d, int len, std::vector<double>& h) {
+            h.resize(len);
+            CU(cudaMemcpyAsync(h.data(), d, sizeof(double) * len, cudaMemcpyDeviceToHost, st_));
+        };
+        get(base_.c, n, h_c_);
+        get(base_.cl, n, h_cl_);
+        get(base_.cu, n, h_cu_);
+        get(base_.rmin, m, h_rmin_);
+        get(base_.rmax, m, h_rmax_);
+    }
+    CU(cudaStreamSynchronize(st_));
+    // original units: x = dc x~, y = y~ / dr, A^T y = (A~^T y~) / dc, A x = dr (A~ x~)
+    double ymax = 0.0, xmax = 0.0;
+    for (int i = 0; i < m; ++i) {
+        dy[i] /= hp_dr_[i];
+        ax[i] *= hp_dr_[i];
+        ymax = std::max(ymax, std::fabs(dy[i]));
+    }
+    for (int j = 0; j < n; ++j) {
+        dx[j] *= hp_dc_[j];
+        aty[j] /= hp_dc_[j];
+        xmax = std::max(xmax, std::fabs(dx[j]));
+    }
+    if (ymax > 0.0 && std::isfinite(ymax)) {  // dual ray
+        double obj = 0.0, mag = 0.0, viol = 0.0, dmax = 0.0;
+        for (int j = 0; j < n; ++j) {
+            const double d = aty[j] / ymax;
+            dmax = std::max(dmax, std::fabs(d));
+            if (d > 0.0) {
+                if (std::isfinite(h_cl_[j])) { obj += d * h_cl_[j]; mag += std::fabs(d * h_cl_[j]); }
+                else viol = std::max(viol, d);
+            } else if (d < 0.0) {
+                if (std::isfinite(h_cu_[j])) { obj += d * h_cu_[j]; mag += std::fabs(d * h_cu_[j]); }
+                else viol = std::max(viol, -d);
+            }
+        }
+        for (int i = 0; i < m; ++i) {
+            const double y = dy[i] / ymax;
+            if (y > 0.0) {
+                if (std::isfinite(h_rmax_[i])) { obj -= y * h_rmax_[i]; mag += std::fabs(y * h_rmax_[i]); }
+                else viol = std::max(viol, y);
+            } else if (y < 0.0) {
+                if (std::isfinite(h_rmin_[i])) { obj -= y * h_rmin_[i]; mag += std::fabs(y * h_rmin_[i]); }
+                else viol = std::max(viol, -y);
+            }
+        }
+        if (obj > 0.0 && obj > 1e-6 * mag && viol <= 1e-9 * std::max(1.0, dmax)) {
+            out.ry.assign(m, 0.0);
+            for (int i = 0; i < m; ++i) out.ry[pr_[i]] = dy[i] / ymax;
+            return 1;
+        }
+    }
+    if (xmax > 0.0 && std::isfinite(xmax)) {  // primal ray
+        double cx = 0.0, mag = 0.0, viol = 0.0, amax = 0.0;
+        for (int j = 0; j < n; ++j) {
+            const double x = dx[j] / xmax;
+            cx += h_c_[j] * x;
+            mag += std::fabs(h_c_[j] * x);
+            if (x < 0.0 && std::isfinite(h_cl_[j])) viol = std::max(viol, -x);
+            if (x > 0.0 && std::isfinite(h_cu_[j])) viol = std::max(viol, x);
+        }
+        for (int i = 0; i < m; ++i) {
+            const double a = ax[i] / xmax;
+            amax = std::max(amax, std::fabs(a));
+            if (a < 0.0 && std::isfinite(h_rmin_[i])) viol = std::max(viol, -a);
+            if (a > 0.0 && std::isfinite(h_rmax_[i])) viol = std::max(viol, a);
+        }
+        if (cx < 0.0 && -cx > 1e-6 * mag && viol <= 1e-9 * std::max(1.0, amax)) {
+            out.rx.assign(n, 0.0);
+            for (int j = 0; j < n; ++j) out.rx[pc_[j]] = dx[j] / xmax;
+            return 2;
+        }
+    }
+    return 0;
+}
+
 // incumbent, rollback, restart and primal weight (src/pdhg/pdhg.cu:665-1085).
 template <typename T>
 LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
@@ -972,6 +1084,7 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
     long long epoch_start = 0, last_rollback = 0;
     long long next_repair = 5000, repair_spacing = 2000;  // src/pdhg/pdhg.cu:741-743
     bool have_pe = false, have_last = false, have_inc = false;
+    int ray_prev = 0;  // certificate kind found at the previous restart
     double inc_op = 0.0;
     DevMetrics inc{};
     out.status = IGAOS_STATUS_ITERATION_LIMIT;
@@ -1111,6 +1224,20 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
                         if (std::isfinite(om) && om > 0.0)
                             h_ctl_->omega = std::clamp(om, 1e-6, 1e6);
                     }
+                    if (o.detect_inf) {
+                        // the same kind of certificate at two consecutive restarts
+                        const int kind = ray_check<T>(anch, p, out);
+                        if (kind != 0 && kind == ray_prev) {
+                            out.ray = kind;
+                            out.status = kind == 1 ? IGAOS_STATUS_INFEASIBLE : IGAOS_STATUS_UNBOUNDED;
+                            if (o.verbosity > 0)
+                                std::fprintf(stderr, "[pdhg-gb300] %s certificate @k=%lld\n",
+                                             kind == 1 ? "dual-ray (infeasible)" : "primal-ray (unbounded)",
+                                             k_done);
+                            break;
+                        }
+                        ray_prev = kind;
+                    }
                 }
                 have_pe = true;
                 if (anch) {
@@ -1216,6 +1343,7 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     lo.check = o.check_period > 0 ? o.check_period : 64;
     lo.verbosity = o.verbosity;
     lo.graphs = o.use_graphs != 0;
+    lo.detect_inf = o.detect_infeasibility != 0;
     lo.eta_init = eta0;
     lo.eta0 = eta0;
     lo.omega_init = omega0;
@@ -1281,8 +1409,21 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     emit_repaired(out, r, x, y);
 }
 
-// A pair certified by dual repair is the answer as the repair produced it.
+// A pair certified by dual repair is the answer as the repair produced it;
+// an infeasibility certificate replaces y (dual ray) or x (primal ray).
 void Engine::emit_repaired(const LoopOut& out, igaos_pdhg_result& r, double* x, double* y) {
+    if (out.ray == 1) {
+        fill_message(r, "primal infeasible: a dual ray (change between restart points) certifies it; "
+                        "y holds the ray");
+        if (y) std::memcpy(y, out.ry.data(), sizeof(double) * m);
+        return;
+    }
+    if (out.ray == 2) {
+        fill_message(r, "dual infeasible (unbounded if feasible): a primal ray certifies it; x holds "
+                        "the ray");
+        if (x) std::memcpy(x, out.rx.data(), sizeof(double) * n);
+        return;
+    }
     if (!out.repaired) return;
     fill_message(r, "converged: residuals @tol, duality gap certified by dual repair");
     if (x) std::memcpy(x, out.rx.data(), sizeof(double) * n);
@@ -1526,6 +1667,7 @@ void Engine::solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, dou
     lo.check = o.check_period > 0 ? o.check_period : 64;
     lo.verbosity = o.verbosity;
     lo.graphs = o.use_graphs != 0;
+    lo.detect_inf = o.detect_infeasibility != 0;
     lo.eta_init = eta0;
     lo.eta0 = eta0;
     lo.omega_init = omega0;

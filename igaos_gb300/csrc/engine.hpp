@@ -102,6 +102,7 @@ struct LoopOpts {
     int check = 64;
     int verbosity = 0;
     bool graphs = true;
+    bool detect_inf = false;  // infeasibility certificates at restarts
     double eta_init = 1, omega_init = 1, eta0 = 1;
 };
 
@@ -114,6 +115,7 @@ struct LoopOut {
     int parity = 0;
     bool numeric_failure = false;
     bool repaired = false;            // certified by dual repair: answer in rx, ry
+    int ray = 0;                      // 1: dual ray in ry (infeasible); 2: primal ray in rx
     std::vector<double> rx, ry;       // original units, caller's numbering
 };
 
@@ -213,6 +215,10 @@ class Engine {
     // host copy of the original LP for dual repair (small m only)
     std::unique_ptr<HostLP> hlp_;
     void emit_repaired(const LoopOut& out, igaos_pdhg_result& r, double* x, double* y);
+    // infeasibility certificates from the change between restart points
+    // (0: none, 1: dual ray, 2: primal ray; the ray in out.ry / out.rx)
+    template <typename T> int ray_check(bool anch, int p, LoopOut& out);
+    std::vector<double> h_c_, h_cl_, h_cu_, h_rmin_, h_rmax_;  // original units, device order
     template <typename T>
     bool try_repair(const Vecs& v, int p, bool anch, const DevMetrics& ma, const DevMetrics* inc,
                     double tol, int verbosity, long long k, LoopOut& out);

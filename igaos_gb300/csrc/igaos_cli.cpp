@@ -32,13 +32,15 @@ void usage() {
         "  --out <file.json>       write solution JSON here (else stdout)\n"
         "  --engine <name>         auto|simplex|pdhg|milp|qp (this build: pdhg)\n"
         "  --precision <p>         fp64|fp32-refine|fp32 (default fp64)\n"
-        "  --verbose               engine progress to stderr (repeat for more)\n");
+        "  --verbose               engine progress to stderr (repeat for more)\n"
+        "  --detect-infeasibility  stop with infeasible/unbounded on a ray certificate\n");
 }
 
 struct Args {
     std::string cmd, path, out, engine = "auto";
     igaos::Options opts;
     int precision = IGAOS_PDHG_FP64;
+    bool detect = false;
     bool ok = true;
 };
 
@@ -60,6 +62,7 @@ Args parse(int argc, char** argv) {
         else if (f == "--seed" && has) a.opts.seed = std::atoi(argv[++i]);
         else if (f == "--presolve" && has) a.opts.presolve = std::string(argv[++i]) == "on";
         else if (f == "--verbose") ++a.opts.verbosity;
+        else if (f == "--detect-infeasibility") a.detect = true;
         else if (f == "--out" && has) a.out = argv[++i];
         else if (f == "--engine" && has) {
             a.engine = argv[++i];
@@ -184,10 +187,11 @@ int main(int argc, char** argv) {
     }
     if (a.cmd == "info") return info(M);
     igaos::Solution s;
-    if (a.engine == "pdhg" && a.precision != IGAOS_PDHG_FP64) {
+    if (a.engine == "pdhg" && (a.precision != IGAOS_PDHG_FP64 || a.detect)) {
         igaos_pdhg_options o;
         igaos_pdhg_default_options(&o);
         o.precision = a.precision;
+        o.detect_infeasibility = a.detect ? 1 : 0;
         s = igaos::pdhg::solve_ex(M, a.opts, &o);
     } else {
         s = igaos::solve_with_engine(M, a.opts, a.engine);

@@ -344,6 +344,14 @@ __global__ void k_scale_matrix(int rows, const int* __restrict__ ptr, const int*
 }
 
 // s = v / d (bounds) or v * d (cost), elementwise, FP64 and FP32 copies.
+// out = a - b in FP64 (change between two restart points)
+template <typename T>
+__global__ void k_ray_diff(int n, const T* __restrict__ a, const T* __restrict__ b,
+                           double* __restrict__ out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        out[i] = (double)a[i] - (double)b[i];
+}
+
 // out = 1 / d (IEEE quotient, as the inline 1.0 / d it replaces)
 __global__ void k_recip(int n, const double* __restrict__ d, double* __restrict__ out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)

@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define IGAOS_PDHG_ABI_VERSION 1
+#define IGAOS_PDHG_ABI_VERSION 2
 
 /* Return codes of every entry point. */
 enum {
@@ -78,6 +78,14 @@ typedef struct igaos_pdhg_options {
     int max_refinements;      /* FP32_REFINE: outer rounds (12) */
     int use_graphs;           /* 1: replay captured CUDA graphs of attempts */
     int device;               /* CUDA device ordinal (-1: current) */
+    /* 1: at every restart, test the change between consecutive restart
+     * points as an infeasibility certificate (a dual ray: the LP is
+     * infeasible; a primal ray: its dual is, so a feasible LP is unbounded),
+     * in original units, and stop with IGAOS_STATUS_INFEASIBLE /
+     * IGAOS_STATUS_UNBOUNDED when the same kind holds at two consecutive
+     * restarts; the ray is returned in y / x (max-norm 1). 0 (default): off,
+     * as the reference engine, which has no such test. Added in ABI 2. */
+    int detect_infeasibility;
 } igaos_pdhg_options;
 
 typedef struct igaos_pdhg_result {

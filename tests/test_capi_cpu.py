@@ -29,12 +29,13 @@ def test_exports_every_declared_symbol(native):
 
 def test_abi_version_and_defaults(native):
     from igaos_gb300 import capi
-    assert native.igaos_pdhg_abi_version() == 1
+    assert native.igaos_pdhg_abi_version() == 2
     o = capi.default_options()
     # igaos::Options defaults (reference include/igaos/options.h:5-13)
     assert o.time_limit_s == 120.0 and o.tolerance == 1e-4 and o.max_iterations == 500000
     assert o.presolve == 1 and o.restarts == 0 and o.verbosity == 0 and o.seed == 0
     assert o.precision == capi.FP64 and o.check_period == 64 and o.use_graphs == 1
+    assert o.detect_infeasibility == 0  # off, as the reference engine
 
 
 def _tiny():
