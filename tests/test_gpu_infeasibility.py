@@ -128,10 +128,10 @@ def test_cli_flag_reports_infeasible(native, tmp_path):
     write_mps(lp, p)
     cli = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "igaos_gb300",
                        "igaos")
-    base = [cli, "solve", str(p), "--engine", "pdhg", "--tol", "1e-6", "--max-iter", "100000",
-            "--time-limit", "1e9"]
-    rec = json.loads(subprocess.run(base + ["--detect-infeasibility"], capture_output=True,
-                                    text=True, check=True).stdout)
+    base = [cli, "solve", str(p), "--engine", "pdhg", "--tol", "1e-6", "--time-limit", "1e9"]
+    rec = json.loads(subprocess.run(base + ["--max-iter", "400000", "--detect-infeasibility"],
+                                    capture_output=True, text=True, check=True).stdout)
     assert rec["status"] == "infeasible", rec["message"]
-    rec = json.loads(subprocess.run(base, capture_output=True, text=True, check=True).stdout)
+    rec = json.loads(subprocess.run(base + ["--max-iter", "20000"], capture_output=True, text=True,
+                                    check=True).stdout)
     assert rec["status"] == "iteration-limit", rec["message"]
