@@ -8,6 +8,7 @@ Only engine="pdhg" is carried by this build; it runs hand-written sm_103a
 kernels through the C ABI in include/igaos_pdhg.h.
 
 GB300 extensions:
+    solve(..., precision="fp64"|"fp32-refine"|"fp32", detect_infeasibility=False)
     capi.Problem / capi.solve_lp  -- LPs given as CSR arrays (C ABI via ctypes)
     generators                    -- seeded synthetic LPs of the benchmark shapes
 """

@@ -135,3 +135,16 @@ def test_cli_flag_reports_infeasible(native, tmp_path):
     rec = json.loads(subprocess.run(base + ["--max-iter", "20000"], capture_output=True, text=True,
                                     check=True).stdout)
     assert rec["status"] == "iteration-limit", rec["message"]
+
+
+def test_pybind_solve_reports_infeasible(native, tmp_path):
+    """igaos_gb300.solve(path, engine="pdhg", detect_infeasibility=True)."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from test_gpu_surfaces import write_mps
+    import igaos_gb300 as ig
+    p = tmp_path / "inf.mps"
+    write_mps(two_rows_infeasible(), p)
+    s = ig.solve(str(p), time_limit=60.0, tolerance=1e-6, engine="pdhg", detect_infeasibility=True)
+    assert s.status == "infeasible", s.message
