@@ -26,6 +26,13 @@ FP32, 8 for FP64; int32 indices):
 nine m- and nine n-vectors read or written once each: x, xavg, c, l, u, xbar
 and y, A x, yavg, rmin, rmax gathered/read; x', xavg', xbar, y', A x', yavg'
 written).
+roofline: the fused attempt's algorithmic bytes over its CUDA-event time
+against the measured HBM copy bandwidth; `roofline.l2` adds the bound that
+limits it on this LP, whose working set nearly fits L2: L1-miss sectors per
+attempt (committed ncu summary) per second against the device's random
+4-byte read rate of a 2 MB vector (igaos_pdhg_gather_rate, measured in the
+same run). The multicommodity extra reports `attempt_us` and
+`attempt_hbm_frac` for an LP that streams from HBM.
 e2e: the same metric through the C ABI with HOST buffers: igaos_pdhg_solve_csr
 (upload, device setup, solve, download, free) timed on the host.
 L2: flushed (512 MiB write) between steps. Reference arm and cpu_baseline:
