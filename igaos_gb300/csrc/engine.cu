@@ -94,6 +94,9 @@ static bool cluster_fits(bool f64, int bytes) {
 // kSmallItems items.
 static bool small_share(const int* ptr, int rows, std::vector<long long>& ent,
                         std::vector<long long>& slots) {
+    // a warp item holds at most 32 rows: more rows than that many items hold
+    // cannot fit (no need to build the schedule to know)
+    if ((long long)rows > 32LL * kSmallCluster * kSmallWarps * kSmallItems) return false;
     std::vector<int> wr;
     std::vector<unsigned char> wl;
     build_warps(ptr, rows, wr, wl);
