@@ -114,6 +114,28 @@ def test_generators_are_feasible_at_x_star():
     assert g.m == 3 * 100 + 2 * 2 * 10 * 9
 
 
+@pytest.mark.parametrize("seed", [0, 1, 2, 3])
+def test_known_optimum_lp_is_optimal_at_its_pair(orc, seed):
+    """known_optimum_lp's (x*, y*): primal and dual feasible with zero gap
+    under the oracle's restatement of the reference evaluate(), every bound
+    type present, and a perturbed dual with an infinite dual bound (the case
+    the dual repair certifies)."""
+    from igaos_gb300 import generators as G
+    import scipy.sparse as sp
+    lp, xs, ys = G.known_optimum_lp(300, 750, 600, seed)
+    A = sp.csr_matrix((lp.ax, lp.ai, lp.ap), shape=(lp.m, lp.n))
+    ev = lambda y: orc.evaluate_arrays(lp.rmin, lp.rmax, lp.cl, lp.cu, lp.c, xs, y, A @ xs,
+                                       lp.c + A.T @ y)
+    mt = ev(ys)
+    assert mt["pinf"] <= 1e-14 and mt["prow"] <= 1e-14 and mt["dinf"] <= 1e-12
+    assert np.isfinite(mt["gap"]) and mt["gap"] <= 1e-12
+    fin_l, fin_u = np.isfinite(lp.cl), np.isfinite(lp.cu)
+    assert (~fin_l & ~fin_u).any() and (fin_l & ~fin_u).any() and (~fin_l & fin_u).any()
+    assert (lp.cl == lp.cu).any() and (fin_l & fin_u & (lp.cl < lp.cu)).any()
+    rng = np.random.default_rng(seed)
+    assert not np.isfinite(ev(ys + 1e-6 * rng.standard_normal(lp.m))["gap"])
+
+
 def _big_mps(seed=3, n=110_000, m=30_000):
     """A COLUMNS section well above the reader's 8 MB split threshold, with
     what a split must keep in file order: integer MARKER blocks crossing the
