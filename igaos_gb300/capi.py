@@ -109,6 +109,7 @@ def lib():
         L.igaos_pdhg_dual_repair.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, _dp,
                                              C.POINTER(C.c_int)]
         L.igaos_pdhg_gather_rate.argtypes = [C.c_int, C.c_int, _dp]
+        L.igaos_pdhg_ray_certificate.argtypes = [C.c_int, C.c_int] + [_dp] * 11 + [C.POINTER(C.c_int)]
         L.igaos_pdhg_dual_repair_device.argtypes = [C.c_void_p, _dp, _dp, C.c_double,
                                                     C.c_double, _dp, C.POINTER(C.c_int), _dp]
         L.igaos_pdhg_solve_batch.argtypes = [
@@ -135,6 +136,25 @@ def gather_rate(log2_words: int, device: int = -1) -> float:
     out = C.c_double(0.0)
     _check(lib().igaos_pdhg_gather_rate(int(log2_words), int(device), C.byref(out)))
     return out.value
+
+
+def ray_certificate(lp, x, y):
+    """(kind, xray, yray): the infeasibility-certificate test of
+    detect_infeasibility on host arrays (original units): 1 = y is a dual ray
+    (the LP is infeasible), 2 = x is a primal ray (its dual is infeasible),
+    0 = neither. Needs no GPU."""
+    import scipy.sparse as sp
+    A = sp.csr_matrix((lp.ax, lp.ai, lp.ap), shape=(lp.m, lp.n))
+    f = lambda a: np.ascontiguousarray(a, np.float64)
+    x, y = f(x), f(y)
+    ax, aty = f(A @ x), f(A.T @ y)
+    xr, yr = np.zeros(lp.n), np.zeros(lp.m)
+    kind = C.c_int(-1)
+    _check(lib().igaos_pdhg_ray_certificate(
+        int(lp.m), int(lp.n), *[_d(v) for v in (x, ax, y, aty, f(lp.c), f(lp.cl), f(lp.cu),
+                                                  f(lp.rmin), f(lp.rmax), xr, yr)],
+        C.byref(kind)))
+    return kind.value, xr, yr
 
 
 def last_error() -> str:

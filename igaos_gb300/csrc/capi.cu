@@ -8,6 +8,7 @@
 #include <vector>
 
 #include "engine.hpp"
+#include "certificate.hpp"
 
 struct igaos_pdhg_problem {
     igx::Engine* eng;
@@ -285,6 +286,19 @@ int igaos_pdhg_dual_repair_device(igaos_pdhg_problem* p, const double* x, const 
         double m6[6];
         *certified = p->eng->repair_device(x, y_it, col_tol, tol, y, m6) ? 1 : 0;
         if (metrics6) std::memcpy(metrics6, m6, sizeof(m6));
+    });
+}
+
+int igaos_pdhg_ray_certificate(int m, int n, const double* x, const double* ax, const double* y,
+                               const double* aty, const double* c, const double* cl,
+                               const double* cu, const double* rmin, const double* rmax,
+                               double* xray, double* yray, int* kind) {
+    if (m < 0 || n < 0) return fail(IGAOS_PDHG_ERR_INVALID, "negative size");
+    if (!kind || (m > 0 && (!ax || !y || !rmin || !rmax)) ||
+        (n > 0 && (!x || !aty || !c || !cl || !cu)))
+        return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    return guarded([&] {
+        *kind = igx::ray_certificate(m, n, x, ax, y, aty, c, cl, cu, rmin, rmax, xray, yray);
     });
 }
 

@@ -5,6 +5,7 @@
 #include "kernels.cuh"
 #include "repair_dev.cuh"
 #include "cluster.cuh"
+#include "certificate.hpp"
 
 #include <algorithm>
 #include <cmath>
@@ -945,17 +946,9 @@ bool Engine::repair(const double* x, const double* Ax, const double* y_it, doubl
 // Infeasibility certificates (no counterpart in the reference engine): the
 // change between consecutive restart points of an LP without a solution
 // tends to a ray (the iterates diverge along it), as in PDLP's test on
-// iterate differences. Tested in original units, device numbering, after
-// normalising the ray to max-norm 1:
-//   dual ray y, d = A^T y (no cost): d_j > 0 needs a finite lower bound and
-//     d_j < 0 a finite upper one, y_i > 0 a finite rmax and y_i < 0 a finite
-//     rmin; the dual objective along it, sum_j d_j (l_j or u_j) - sum_i y_i
-//     (rmax_i or rmin_i), positive => the dual is unbounded => infeasible;
-//   primal ray x, A x: x_j < 0 needs l_j = -inf, x_j > 0 needs u_j = +inf,
-//     (A x)_i < 0 needs rmin_i = -inf, > 0 needs rmax_i = +inf, and c^T x < 0
-//     => the dual is infeasible (a feasible LP is unbounded).
-// A certificate needs its sign violations below 1e-9 of the ray's scale and
-// its objective beyond 1e-6 of the objective's term magnitudes.
+// iterate differences. The difference and its products are formed on the
+// device in FP64; the test itself (certificate.hpp) runs on the host in
+// original units.
 template <typename T>
 int Engine::ray_check(bool anch, int p, LoopOut& out) {
     Work<T>& w = work<T>();
@@ -990,68 +983,26 @@ int Engine::ray_check(bool anch, int p, LoopOut& out) {
     }
     CU(cudaStreamSynchronize(st_));
     // original units: x = dc x~, y = y~ / dr, A^T y = (A~^T y~) / dc, A x = dr (A~ x~)
-    double ymax = 0.0, xmax = 0.0;
     for (int i = 0; i < m; ++i) {
         dy[i] /= hp_dr_[i];
         ax[i] *= hp_dr_[i];
-        ymax = std::max(ymax, std::fabs(dy[i]));
     }
     for (int j = 0; j < n; ++j) {
         dx[j] *= hp_dc_[j];
         aty[j] /= hp_dc_[j];
-        xmax = std::max(xmax, std::fabs(dx[j]));
     }
-    if (ymax > 0.0 && std::isfinite(ymax)) {  // dual ray
-        double obj = 0.0, mag = 0.0, viol = 0.0, dmax = 0.0;
-        for (int j = 0; j < n; ++j) {
-            const double d = aty[j] / ymax;
-            dmax = std::max(dmax, std::fabs(d));
-            if (d > 0.0) {
-                if (std::isfinite(h_cl_[j])) { obj += d * h_cl_[j]; mag += std::fabs(d * h_cl_[j]); }
-                else viol = std::max(viol, d);
-            } else if (d < 0.0) {
-                if (std::isfinite(h_cu_[j])) { obj += d * h_cu_[j]; mag += std::fabs(d * h_cu_[j]); }
-                else viol = std::max(viol, -d);
-            }
-        }
-        for (int i = 0; i < m; ++i) {
-            const double y = dy[i] / ymax;
-            if (y > 0.0) {
-                if (std::isfinite(h_rmax_[i])) { obj -= y * h_rmax_[i]; mag += std::fabs(y * h_rmax_[i]); }
-                else viol = std::max(viol, y);
-            } else if (y < 0.0) {
-                if (std::isfinite(h_rmin_[i])) { obj -= y * h_rmin_[i]; mag += std::fabs(y * h_rmin_[i]); }
-                else viol = std::max(viol, -y);
-            }
-        }
-        if (obj > 0.0 && obj > 1e-6 * mag && viol <= 1e-9 * std::max(1.0, dmax)) {
-            out.ry.assign(m, 0.0);
-            for (int i = 0; i < m; ++i) out.ry[pr_[i]] = dy[i] / ymax;
-            return 1;
-        }
+    std::vector<double> xr(n), yr(m);
+    const int kind = ray_certificate(m, n, dx.data(), ax.data(), dy.data(), aty.data(), h_c_.data(),
+                                     h_cl_.data(), h_cu_.data(), h_rmin_.data(), h_rmax_.data(),
+                                     xr.data(), yr.data());
+    if (kind == 1) {
+        out.ry.assign(m, 0.0);
+        for (int i = 0; i < m; ++i) out.ry[pr_[i]] = yr[i];
+    } else if (kind == 2) {
+        out.rx.assign(n, 0.0);
+        for (int j = 0; j < n; ++j) out.rx[pc_[j]] = xr[j];
     }
-    if (xmax > 0.0 && std::isfinite(xmax)) {  // primal ray
-        double cx = 0.0, mag = 0.0, viol = 0.0, amax = 0.0;
-        for (int j = 0; j < n; ++j) {
-            const double x = dx[j] / xmax;
-            cx += h_c_[j] * x;
-            mag += std::fabs(h_c_[j] * x);
-            if (x < 0.0 && std::isfinite(h_cl_[j])) viol = std::max(viol, -x);
-            if (x > 0.0 && std::isfinite(h_cu_[j])) viol = std::max(viol, x);
-        }
-        for (int i = 0; i < m; ++i) {
-            const double a = ax[i] / xmax;
-            amax = std::max(amax, std::fabs(a));
-            if (a < 0.0 && std::isfinite(h_rmin_[i])) viol = std::max(viol, -a);
-            if (a > 0.0 && std::isfinite(h_rmax_[i])) viol = std::max(viol, a);
-        }
-        if (cx < 0.0 && -cx > 1e-6 * mag && viol <= 1e-9 * std::max(1.0, amax)) {
-            out.rx.assign(n, 0.0);
-            for (int j = 0; j < n; ++j) out.rx[pc_[j]] = dx[j] / xmax;
-            return 2;
-        }
-    }
-    return 0;
+    return kind;
 }
 
 // incumbent, rollback, restart and primal weight (src/pdhg/pdhg.cu:665-1085).

@@ -119,6 +119,22 @@ int igaos_pdhg_abi_version(void);
  * 256 threads per SM; best of 3 launches after a warming one. */
 int igaos_pdhg_gather_rate(int log2_words, int device, double* gathers_per_s);
 
+/* The infeasibility-certificate test of detect_infeasibility, on host arrays
+ * (no device needed; no reference counterpart). A candidate (x, y) with
+ * ax = A x and aty = A^T y, ORIGINAL units, is normalised to max-norm 1 and
+ * tested as a dual ray y (*kind = 1: with d = A^T y, every d_j and y_i has a
+ * sign its finite bound allows and sum_j d_j (l_j or u_j) - sum_i y_i (rmax_i
+ * or rmin_i) > 0: the LP is infeasible) or a primal ray x (*kind = 2: x and
+ * A x in the recession cones of the column and row bounds and c^T x < 0: the
+ * dual is infeasible). Sign violations up to 1e-9 of the ray's scale are
+ * tolerated; the objective must exceed 1e-6 of its terms' magnitude.
+ * *kind = 0: neither. The normalised ray goes to yray (m) / xray (n) when
+ * non-NULL. */
+int igaos_pdhg_ray_certificate(int m, int n, const double* x, const double* ax, const double* y,
+                               const double* aty, const double* c, const double* cl,
+                               const double* cu, const double* rmin, const double* rmax,
+                               double* xray, double* yray, int* kind);
+
 /* Number of visible CUDA devices (0 when none). Replaces the handle-creation
  * probe of src/pdhg/pdhg.cu:459-465. */
 int igaos_pdhg_device_count(void);
