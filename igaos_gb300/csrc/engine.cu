@@ -306,7 +306,6 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     dr_ = ar_.alloc<double>(m);
     dc_ = ar_.alloc<double>(n);
     idr_ = ar_.alloc<double>(m);
-    idc_ = ar_.alloc<double>(n);
     // control + scratch
     ctl_ = ar_.alloc<DevCtl>(1);
     met_ = ar_.alloc<DevMetrics>(2);
@@ -395,7 +394,6 @@ void Engine::setup_scaling() {
     k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cl, dc_, 0, base_.scl, base_.fcl);
     k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cu, dc_, 0, base_.scu, base_.fcu);
     k_recip<<<grid_for(m), kThreads, 0, st_>>>(m, dr_, idr_);
-    k_recip<<<grid_for(n), kThreads, 0, st_>>>(n, dc_, idc_);
     CU(cudaGetLastError());
     hp_dr_.resize(m);
     hp_dc_.resize(n);
@@ -635,7 +633,6 @@ void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* 
     ka.dr = dr_;
     ka.dc = dc_;
     ka.idr = idr_;
-    ka.idc = idc_;
     ka.c = v.c;
     ka.cl = v.cl;
     ka.cu = v.cu;

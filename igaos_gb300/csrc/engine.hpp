@@ -161,7 +161,7 @@ class Engine {
     float *ax32_, *acx32_;
     Sched sA_, sAT_;
     double *dr_, *dc_;
-    double *idr_, *idc_;  // reciprocals of the scaling, for the KKT kernels
+    double* idr_;  // 1 / dr, for the KKT kernels
     Vecs base_{};
     // device numbering: new index -> original (pr_, pc_) and inverses
     std::vector<int> pr_, pc_, ipr_, ipc_;

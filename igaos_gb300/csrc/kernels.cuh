@@ -456,11 +456,6 @@ __global__ void k_convert(int n, const TI* __restrict__ in, TO* __restrict__ out
 //   rowdual: row part of the Lagrangian bound (needs max |y| for its noise
 //            threshold) and the final metrics.
 
-// IGX_KKT_RECIP_DC: reduced costs d = c + (A~^T y~) * (1/dc) instead of the
-// quotient (within an ulp of it); FP64 division is slow on this part.
-#ifndef IGX_KKT_RECIP_DC
-#define IGX_KKT_RECIP_DC 0
-#endif
 template <typename T>
 struct KktArgs {
     WarpSched wsA, wsAT;
@@ -468,7 +463,7 @@ struct KktArgs {
     const T* x[2];
     const T* y[2];
     const double *dr, *dc;
-    const double *idr, *idc;                  // 1 / dr, 1 / dc (IEEE quotients)
+    const double* idr;                        // 1 / dr (IEEE quotients)
     const double *c, *cl, *cu, *rmin, *rmax;  // original units
     const T *slo, *shi;                       // scaled column bounds, iterate precision
     double cmax;
@@ -530,11 +525,7 @@ __global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_cols(KktArgs<T>
     const double dz = 1e-8 * (1.0 + a.cmax);
     double dv = 0.0, op = 0.0, od = 0.0, unb = 0.0;
     auto f = [&](int j, const Acc<T>& acc) {
-#if IGX_KKT_RECIP_DC
-        const double d = a.c[j] + acc.result_d() * a.idc[j];
-#else
         const double d = a.c[j] + 1.0 * acc.result_d() / a.dc[j];
-#endif
         const double x = unscale_x(xv[j], a.slo[j], a.shi[j], a.dc[j], a.cl[j], a.cu[j]);
         const double cl = a.cl[j], cu = a.cu[j];
         const double bnd = fabs(isfinite(cu) ? cu : cl);
