@@ -96,3 +96,29 @@ def test_solve_with_infinite_bounds(native, precision, tol):
     assert max(r["pinf"], r["prow"], r["rel_gap"]) <= tol
     if tol == 1e-2 and precision == "fp32-refine":
         assert "dual repair" in r["message"] and r["iterations"] < 20000, r
+
+
+def test_matrix_free_restatement_certifies_golden_cases(orc):
+    """The numpy restatement of the device repair (oracle/repair_mf.py)
+    certifies every golden candidate the reference's dense repair certifies,
+    at the reference's own gap (or 1e-6), and none of the others."""
+    from oracle import repair_mf
+    for k, lp, g in cases():
+        base = orc.evaluate_arrays(lp.rmin, lp.rmax, lp.cl, lp.cu, lp.c, g["x"], g["y_it"],
+                                   lp.dense() @ g["x"], lp.c + lp.dense().T @ g["y_it"])
+        if bool(g["ok"]):
+            ref = orc.evaluate_arrays(lp.rmin, lp.rmax, lp.cl, lp.cu, lp.c, g["x"], g["y"],
+                                      lp.dense() @ g["x"], lp.c + lp.dense().T @ g["y"])
+            tol = max(1e-6, ref["gap"], base["pinf"], base["prow"]) * (1.0 + 1e-9)
+        else:
+            tol = max(1e-6, base["pinf"], base["prow"]) * (1.0 + 1e-9)
+        ok, y, mt = repair_mf.repair(lp, g["x"], g["y_it"], float(g["tol"]), tol)
+        assert ok == bool(g["ok"]), (k, mt)
+
+
+def test_matrix_free_restatement_on_a_perturbed_optimum(orc):
+    from oracle import repair_mf
+    lp, xs, ys = G.known_optimum_lp(600, 1500, 1200, 1)
+    yn = ys + 1e-6 * np.random.default_rng(1).standard_normal(lp.m) * (1 + np.abs(ys))
+    ok, y, mt = repair_mf.repair(lp, xs, yn, 1e-6, 1e-6)
+    assert ok and np.isfinite(mt["gap"]) and mt["gap"] <= 1e-6
