@@ -85,3 +85,18 @@ def test_null_handles(native):
     from igaos_gb300 import capi
     assert native.igaos_pdhg_solve(None, None, None, None, None) == capi.ERR_INVALID
     native.igaos_pdhg_destroy(None)  # no-op
+
+
+def test_helper_entries_reject_bad_arguments(native):
+    """The certificate test and the gather-rate calibration refuse bad
+    arguments with IGAOS_PDHG_ERR_INVALID and a message, before any device
+    work."""
+    import ctypes as C
+    from igaos_gb300 import capi
+    kind = C.c_int(-1)
+    assert native.igaos_pdhg_ray_certificate(2, 2, *([None] * 11), C.byref(kind)) == capi.ERR_INVALID
+    assert "NULL" in capi.last_error()
+    assert native.igaos_pdhg_ray_certificate(-1, 2, *([None] * 11), C.byref(kind)) == capi.ERR_INVALID
+    out = C.c_double(0.0)
+    assert native.igaos_pdhg_gather_rate(4, -1, C.byref(out)) == capi.ERR_INVALID
+    assert "log2_words" in capi.last_error()
