@@ -8,8 +8,10 @@ Only engine="pdhg" is carried by this build; it runs hand-written sm_103a
 kernels through the C ABI in include/igaos_pdhg.h.
 
 GB300 extensions:
-    solve(..., precision="fp64"|"fp32-refine"|"fp32", detect_infeasibility=False)
+    solve(..., precision="fp64"|"fp32-refine"|"fp32", detect_infeasibility=False,
+          pdhg_presolve=False)
     capi.Problem / capi.solve_lp  -- LPs given as CSR arrays (C ABI via ctypes)
+    capi.Presolved                -- the engine's presolve / postsolve on the host
     generators                    -- seeded synthetic LPs of the benchmark shapes
 """
 from __future__ import annotations

@@ -32,7 +32,7 @@ class Options(C.Structure):
         ("restarts", C.c_int), ("verbosity", C.c_int), ("precision", C.c_int),
         ("check_period", C.c_int), ("inner_tolerance", C.c_double),
         ("max_refinements", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
-        ("detect_infeasibility", C.c_int),
+        ("detect_infeasibility", C.c_int), ("pdhg_presolve", C.c_int),
     ]
 
 
@@ -110,6 +110,15 @@ def lib():
                                              C.POINTER(C.c_int)]
         L.igaos_pdhg_gather_rate.argtypes = [C.c_int, C.c_int, _dp]
         L.igaos_pdhg_ray_certificate.argtypes = [C.c_int, C.c_int] + [_dp] * 11 + [C.POINTER(C.c_int)]
+        L.igaos_pdhg_presolve.argtypes = [
+            C.c_int, C.c_int, C.c_int64, _ip, _ip, _dp, _dp, _dp, _dp, _dp, _dp, C.c_double,
+            C.POINTER(C.c_void_p), C.POINTER(C.c_int)]
+        L.igaos_pdhg_presolved_info.argtypes = [C.c_void_p, _ip, _ip, C.POINTER(C.c_int64), _dp,
+                                                C.POINTER(C.c_int64)]
+        L.igaos_pdhg_presolved_lp.argtypes = [C.c_void_p, _ip, _ip] + [_dp] * 6
+        L.igaos_pdhg_postsolve.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        L.igaos_pdhg_presolved_destroy.argtypes = [C.c_void_p]
+        L.igaos_pdhg_presolved_destroy.restype = None
         L.igaos_pdhg_dual_repair_device.argtypes = [C.c_void_p, _dp, _dp, C.c_double,
                                                     C.c_double, _dp, C.POINTER(C.c_int), _dp]
         L.igaos_pdhg_solve_batch.argtypes = [
@@ -155,6 +164,63 @@ def ray_certificate(lp, x, y):
                                                   f(lp.rmin), f(lp.rmax), xr, yr)],
         C.byref(kind)))
     return kind.value, xr, yr
+
+
+PRESOLVE_COUNTS = ("empty_rows", "singleton_rows", "redundant_rows", "fixed_cols", "empty_cols",
+                   "free_singletons")
+
+
+class Presolved:
+    """The engine's presolve of an LP on the host (igaos_pdhg_presolve; no
+    GPU needed): `outcome` is "reduced", "infeasible" or "unbounded"; when
+    reduced, `lp` is the reduced LP (an LPData), `counts` the reductions made,
+    and postsolve(x_red, y_red) maps a pair of the reduced LP back."""
+
+    def __init__(self, lp):
+        from . import generators as G
+        a = _arrays(lp, with_transpose=False)
+        self.m0, self.n0 = int(lp.m), int(lp.n)
+        h = C.c_void_p()
+        oc = C.c_int(-1)
+        _check(lib().igaos_pdhg_presolve(
+            self.m0, self.n0, int(a["ap"][self.m0]), _i(a["ap"]), _i(a["ai"]), _d(a["ax"]),
+            _d(a["c"]), _d(a["cl"]), _d(a["cu"]), _d(a["rmin"]), _d(a["rmax"]),
+            float(getattr(lp, "obj_const", 0.0)), C.byref(h), C.byref(oc)))
+        self.outcome = {0: "reduced", 3: "infeasible", 4: "unbounded"}[oc.value]
+        self.h = h if oc.value == 0 else None
+        self.lp, self.counts = None, None
+        if self.h is None:
+            return
+        m, n, nnz = C.c_int(), C.c_int(), C.c_int64()
+        k = C.c_double()
+        cnt = (C.c_int64 * 6)()
+        _check(lib().igaos_pdhg_presolved_info(self.h, C.byref(m), C.byref(n), C.byref(nnz),
+                                               C.byref(k), cnt))
+        self.counts = dict(zip(PRESOLVE_COUNTS, list(cnt)))
+        m, n, nnz = m.value, n.value, nnz.value
+        ap, ai = np.zeros(m + 1, np.int32), np.zeros(max(nnz, 1), np.int32)
+        ax = np.zeros(max(nnz, 1))
+        v = {f: np.zeros(max(n, 1)) for f in ("c", "cl", "cu")}
+        v.update({f: np.zeros(max(m, 1)) for f in ("rmin", "rmax")})
+        _check(lib().igaos_pdhg_presolved_lp(self.h, _i(ap), _i(ai), _d(ax), *[
+            _d(v[f]) for f in ("c", "cl", "cu", "rmin", "rmax")]))
+        rows = np.repeat(np.arange(m), np.diff(ap))
+        self.lp = G.from_triplets(m, n, rows, ai[:nnz], ax[:nnz], v["c"][:n], v["cl"][:n],
+                                  v["cu"][:n], v["rmin"][:m], v["rmax"][:m], obj_const=k.value)
+
+    def postsolve(self, x_red, y_red):
+        f = lambda a: np.ascontiguousarray(a, np.float64)
+        xr, yr = f(x_red), f(y_red)
+        x, y = np.zeros(self.n0), np.zeros(self.m0)
+        _check(lib().igaos_pdhg_postsolve(self.h, _d(xr), _d(yr), _d(x), _d(y)))
+        return x, y
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().igaos_pdhg_presolved_destroy(self.h)
+            self.h = None
+
+    __del__ = close
 
 
 def last_error() -> str:

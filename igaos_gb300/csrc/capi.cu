@@ -1,17 +1,33 @@
 // C ABI of the GB300 PDHG engine (declared in include/igaos_pdhg.h).
 // No exception crosses this boundary: every failure becomes an
 // IGAOS_PDHG_ERR_* code plus a thread-local message.
+#include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <vector>
 
 #include "engine.hpp"
 #include "certificate.hpp"
+#include "presolve.hpp"
+#include "repair.hpp"
 
 struct igaos_pdhg_problem {
-    igx::Engine* eng;
+    igx::Engine* eng = nullptr;  // NULL when presolve removed the whole LP
+    // pdhg_presolve: the reductions and their outcome, the original LP's
+    // costs and bounds (metrics of the postsolved answer), the presolve time
+    igx::Presolved* pre = nullptr;
+    int pre_outcome = 0;
+    igx::HostLP orig;
+    double obj_const = 0.0;
+    double presolve_ms = 0.0;
+};
+
+struct igaos_pdhg_presolved {
+    igx::Presolved p;
 };
 
 namespace {
@@ -103,6 +119,120 @@ void transpose_host(int m, int n, const int* ap, const int* ai, const double* ax
             ++next[j];
         }
 }
+constexpr const char* kPresolvedInspect =
+    "inspection entry points see the engine's LP, which a presolved handle does not share "
+    "with its caller";
+
+// igaos_pdhg_solve of a handle made with pdhg_presolve: the engine solves the
+// reduced LP, postsolve maps the pair back, and the metrics are taken again
+// on the original LP (other norms than the reduced LP's). When the reduced
+// LP converged but the original misses the tolerance, the reduced LP is
+// solved again at a tenth of the tolerance, at most twice.
+int solve_presolved(igaos_pdhg_problem* p, const igaos_pdhg_options& o, igaos_pdhg_result* res,
+                    double* x, double* y) {
+    const igx::Presolved& R = *p->pre;
+    const int m0 = R.m0, n0 = R.n0;
+    std::memset(res, 0, sizeof(*res));
+    res->setup_time_ms = p->presolve_ms;
+    if (p->pre_outcome != igx::kPresolveReduced) {
+        res->status = p->pre_outcome;
+        res->objective = res->pinf = res->dinf = res->rel_gap = res->prow = std::nan("");
+        std::snprintf(res->message, sizeof(res->message), "%s",
+                      p->pre_outcome == igx::kPresolveInfeasible
+                          ? "presolve: the LP is infeasible"
+                          : "presolve: a column's cost runs to an infinite bound (unbounded if "
+                            "feasible)");
+        if (x) std::fill(x, x + n0, 0.0);
+        if (y) std::fill(y, y + m0, 0.0);
+        return ok();
+    }
+    std::vector<double> xr(R.n), yr(R.m), xo(n0), yo(m0), ax(m0), d(n0);
+    igaos_pdhg_options oo = o;
+    const bool timed = o.time_limit_s > 0.0 && o.time_limit_s < 1e6;
+    igaos_pdhg_result rr;
+    igx::HostMetrics mt{};
+    bool pass = false;
+    for (int round = 0;; ++round) {
+        if (p->eng) {
+            const int rc = guarded([&] { p->eng->solve(oo, rr, xr.data(), yr.data()); });
+            if (rc != IGAOS_PDHG_OK) {
+                std::memset(res, 0, sizeof(*res));
+                res->status = IGAOS_STATUS_ERROR;
+                res->error_code = rc;
+                std::snprintf(res->message, sizeof(res->message), "%.159s", g_msg);
+                return rc;
+            }
+            if (rr.error_code != IGAOS_PDHG_OK) {
+                *res = rr;
+                return fail(rr.error_code, rr.message);
+            }
+        } else {  // presolve removed every row and column
+            std::memset(&rr, 0, sizeof(rr));
+            rr.status = IGAOS_STATUS_NEAR_OPTIMAL;
+            std::snprintf(rr.message, sizeof(rr.message), "solved by presolve");
+        }
+        res->iterations += rr.iterations;
+        res->attempts += rr.attempts;
+        res->kkt_checks += rr.kkt_checks;
+        res->restarts += rr.restarts;
+        res->kkt_passes += rr.kkt_passes;
+        res->refinements += rr.refinements;
+        res->solve_time_ms += rr.solve_time_ms;
+        res->device_time_ms += rr.device_time_ms;
+        res->attempt_time_ms += rr.attempt_time_ms;
+        res->launches += rr.launches;
+        if (round == 0) res->setup_time_ms += rr.setup_time_ms;
+        if (rr.status == IGAOS_STATUS_INFEASIBLE || rr.status == IGAOS_STATUS_UNBOUNDED) {
+            // a ray of the reduced LP, on the surviving rows and columns
+            res->status = rr.status;
+            res->objective = rr.objective;
+            res->pinf = rr.pinf;
+            res->dinf = rr.dinf;
+            res->rel_gap = rr.rel_gap;
+            res->prow = rr.prow;
+            std::snprintf(res->message, sizeof(res->message), "%.120s (reduced LP)", rr.message);
+            for (int j = 0; j < n0 && x; ++j) x[j] = R.col_red[j] >= 0 ? xr[R.col_red[j]] : 0.0;
+            for (int i = 0; i < m0 && y; ++i) y[i] = R.row_red[i] >= 0 ? yr[R.row_red[i]] : 0.0;
+            return ok();
+        }
+        igx::postsolve(R, xr.data(), yr.data(), xo.data(), yo.data());
+        std::fill(ax.begin(), ax.end(), 0.0);
+        for (int j = 0; j < n0; ++j) {
+            double dj = R.c0[j];
+            for (int q = R.cp0[j]; q < R.cp0[j + 1]; ++q) {
+                ax[R.ci0[q]] += R.acx0[q] * xo[j];
+                dj += R.acx0[q] * yo[R.ci0[q]];
+            }
+            d[j] = dj;
+        }
+        mt = igx::host_evaluate(p->orig, xo.data(), yo.data(), ax.data(), d.data());
+        pass = mt.pinf <= o.tolerance && mt.dinf <= o.tolerance && mt.prow <= o.tolerance &&
+               std::isfinite(mt.gap) && mt.gap <= o.tolerance;
+        if (pass || rr.status != IGAOS_STATUS_NEAR_OPTIMAL || !p->eng || round == 2) break;
+        oo.tolerance *= 0.1;
+        if (timed) {
+            oo.time_limit_s = o.time_limit_s - res->solve_time_ms / 1000.0;
+            if (oo.time_limit_s <= 0.0) break;
+        }
+    }
+    if (pass) res->status = IGAOS_STATUS_NEAR_OPTIMAL;
+    else if (rr.status != IGAOS_STATUS_NEAR_OPTIMAL) res->status = rr.status;
+    else res->status = mt.pinf <= o.tolerance && mt.prow <= o.tolerance ? IGAOS_STATUS_FEASIBLE
+                                                                         : IGAOS_STATUS_ITERATION_LIMIT;
+    res->objective = mt.op + p->obj_const;
+    res->pinf = mt.pinf;
+    res->dinf = mt.dinf;
+    res->rel_gap = mt.gap;
+    res->prow = mt.prow;
+    std::snprintf(res->message, sizeof(res->message), "%.100s; presolve %d->%d rows, %d->%d cols",
+                  pass || rr.status != IGAOS_STATUS_NEAR_OPTIMAL
+                      ? rr.message
+                      : "converged on the reduced LP, original-LP metrics above tolerance",
+                  m0, R.m, n0, R.n);
+    if (x) std::memcpy(x, xo.data(), sizeof(double) * n0);
+    if (y) std::memcpy(y, yo.data(), sizeof(double) * m0);
+    return ok();
+}
 }  // namespace
 
 int igx::igx_set_error(int code, const char* msg) {
@@ -161,36 +291,60 @@ int igaos_pdhg_create(igaos_pdhg_problem** out, int m, int n, int64_t nnz, const
         if (igaos_pdhg_device_count() == 0)
             throw igx::CudaError(IGAOS_PDHG_ERR_NODEVICE,
                                  "no CUDA device: PDHG engine unavailable");
+        const int dev = opt ? opt->device : -1;
+        std::unique_ptr<igaos_pdhg_problem, void (*)(igaos_pdhg_problem*)> p(
+            new igaos_pdhg_problem, igaos_pdhg_destroy);
         std::vector<int> tcp, tci;
         std::vector<double> tacx;
-        if (!cp) {
-            transpose_host(m, n, ap, ai, ax, tcp, tci, tacx);
-            cp = tcp.data();
-            ci = tci.data();
-            acx = tacx.data();
-        }
-        const int dev = opt ? opt->device : -1;
-        auto* p = new igaos_pdhg_problem;
-        try {
+        if (opt && opt->pdhg_presolve) {
+            const auto t0 = std::chrono::steady_clock::now();
+            p->pre = new igx::Presolved;
+            p->pre_outcome = igx::presolve(m, n, ap, ai, ax, c, cl, cu, rmin, rmax, obj_const,
+                                           *p->pre);
+            igx::HostLP& o = p->orig;
+            o.m = m;
+            o.n = n;
+            o.c.assign(c, c + n);
+            o.cl.assign(cl, cl + n);
+            o.cu.assign(cu, cu + n);
+            o.rmin.assign(rmin, rmin + m);
+            o.rmax.assign(rmax, rmax + m);
+            p->obj_const = obj_const;
+            const igx::Presolved& R = *p->pre;
+            if (p->pre_outcome == igx::kPresolveReduced && R.m > 0)
+                transpose_host(R.m, R.n, R.ap.data(), R.ai.data(), R.ax.data(), tcp, tci, tacx);
+            p->presolve_ms =
+                std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0)
+                    .count();
+            if (p->pre_outcome == igx::kPresolveReduced && R.m > 0)
+                p->eng = new igx::Engine(R.m, R.n, (int64_t)R.ai.size(), R.ap.data(),
+                                         R.ai.data(), R.ax.data(), tcp.data(), tci.data(),
+                                         tacx.data(), R.c.data(), R.cl.data(), R.cu.data(),
+                                         R.rmin.data(), R.rmax.data(), R.obj_const, dev);
+        } else {
+            if (!cp) {
+                transpose_host(m, n, ap, ai, ax, tcp, tci, tacx);
+                cp = tcp.data();
+                ci = tci.data();
+                acx = tacx.data();
+            }
             p->eng = new igx::Engine(m, n, nnz, ap, ai, ax, cp, ci, acx, c, cl, cu, rmin, rmax,
                                      obj_const, dev);
-        } catch (...) {
-            delete p;
-            throw;
         }
-        *out = p;
+        *out = p.release();
     });
 }
 
 int igaos_pdhg_solve(igaos_pdhg_problem* p, const igaos_pdhg_options* opt,
                      igaos_pdhg_result* res, double* x, double* y) {
-    if (!p || !p->eng) return fail(IGAOS_PDHG_ERR_INVALID, "problem handle is NULL");
+    if (!p || (!p->eng && !p->pre)) return fail(IGAOS_PDHG_ERR_INVALID, "problem handle is NULL");
     if (!res) return fail(IGAOS_PDHG_ERR_INVALID, "result pointer is NULL");
     igaos_pdhg_options o;
     if (opt) o = *opt;
     else igaos_pdhg_default_options(&o);
     if (!(o.tolerance > 0)) return fail(IGAOS_PDHG_ERR_INVALID, "tolerance must be positive");
     if (o.precision < 0 || o.precision > 2) return fail(IGAOS_PDHG_ERR_INVALID, "unknown precision");
+    if (p->pre) return solve_presolved(p, o, res, x, y);
     int rc = guarded([&] { p->eng->solve(o, *res, x, y); });
     if (rc != IGAOS_PDHG_OK) {
         std::memset(res, 0, sizeof(*res));
@@ -206,6 +360,7 @@ int igaos_pdhg_solve(igaos_pdhg_problem* p, const igaos_pdhg_options* opt,
 void igaos_pdhg_destroy(igaos_pdhg_problem* p) {
     if (!p) return;
     delete p->eng;
+    delete p->pre;
     delete p;
 }
 
@@ -232,6 +387,7 @@ int igaos_pdhg_solve_csr(int m, int n, int64_t nnz, const int* ap, const int* ai
 }
 
 int igaos_pdhg_get_scaling(const igaos_pdhg_problem* p, double* dr, double* dc) {
+    if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng || !dr || !dc) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
     std::memcpy(dr, p->eng->h_dr.data(), sizeof(double) * p->eng->m);
     std::memcpy(dc, p->eng->h_dc.data(), sizeof(double) * p->eng->n);
@@ -240,6 +396,7 @@ int igaos_pdhg_get_scaling(const igaos_pdhg_problem* p, double* dr, double* dc) 
 
 int igaos_pdhg_get_step_init(const igaos_pdhg_problem* p, double* lambda, double* eta0,
                              double* omega0) {
+    if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
     if (lambda) *lambda = p->eng->lam2;
     if (eta0) *eta0 = p->eng->eta0;
@@ -248,12 +405,14 @@ int igaos_pdhg_get_step_init(const igaos_pdhg_problem* p, double* lambda, double
 }
 
 int igaos_pdhg_get_transpose(const igaos_pdhg_problem* p, int* cp, int* ci, double* acx) {
+    if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng || !cp || !ci || !acx) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
     return guarded([&] { p->eng->get_transpose(cp, ci, acx); });
 }
 
 int igaos_pdhg_iterate(igaos_pdhg_problem* p, int precision, int64_t iters, double* x, double* y,
                        double* xavg, double* yavg, double* axcur, double* state6) {
+    if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng || !x || !y || !xavg || !yavg || !axcur || !state6)
         return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
     if (iters < 0) return fail(IGAOS_PDHG_ERR_INVALID, "iters must be >= 0");
@@ -263,12 +422,14 @@ int igaos_pdhg_iterate(igaos_pdhg_problem* p, int precision, int64_t iters, doub
 }
 
 int igaos_pdhg_evaluate(igaos_pdhg_problem* p, const double* x, const double* y, double* out6) {
+    if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng || !x || !y || !out6) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
     return guarded([&] { p->eng->evaluate(x, y, out6); });
 }
 
 int igaos_pdhg_dual_repair(igaos_pdhg_problem* p, const double* x, const double* Ax,
                            const double* y_it, double col_tol, double* y, int* certified) {
+    if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng || !x || !Ax || !y_it || !y || !certified)
         return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
     if (!(col_tol >= 0.0)) return fail(IGAOS_PDHG_ERR_INVALID, "col_tol must be >= 0");
@@ -278,6 +439,7 @@ int igaos_pdhg_dual_repair(igaos_pdhg_problem* p, const double* x, const double*
 int igaos_pdhg_dual_repair_device(igaos_pdhg_problem* p, const double* x, const double* y_it,
                                   double col_tol, double tol, double* y, int* certified,
                                   double* metrics6) {
+    if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng || !x || !y_it || !y || !certified)
         return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
     if (!(col_tol >= 0.0)) return fail(IGAOS_PDHG_ERR_INVALID, "col_tol must be >= 0");
@@ -304,10 +466,70 @@ int igaos_pdhg_ray_certificate(int m, int n, const double* x, const double* ax, 
 
 int igaos_pdhg_spmv(igaos_pdhg_problem* p, int transpose, int precision, const double* x,
                     double* y) {
+    if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng || !x || !y) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
     if (precision != IGAOS_PDHG_FP64 && precision != IGAOS_PDHG_FP32)
         return fail(IGAOS_PDHG_ERR_INVALID, "precision must be FP64 or FP32");
     return guarded([&] { p->eng->spmv(transpose, precision, x, y); });
 }
+
+int igaos_pdhg_presolve(int m, int n, int64_t nnz, const int* ap, const int* ai,
+                        const double* ax, const double* c, const double* cl, const double* cu,
+                        const double* rmin, const double* rmax, double obj_const,
+                        igaos_pdhg_presolved** out, int* outcome) {
+    if (!out || !outcome) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    *outcome = 0;
+    return guarded([&] {
+        validate(m, n, nnz, ap, ai, ax, nullptr, nullptr, nullptr, c, cl, cu, rmin, rmax);
+        std::unique_ptr<igaos_pdhg_presolved> h(new igaos_pdhg_presolved);
+        *outcome = igx::presolve(m, n, ap, ai, ax, c, cl, cu, rmin, rmax, obj_const, h->p);
+        if (*outcome == igx::kPresolveReduced) *out = h.release();
+    });
+}
+
+int igaos_pdhg_presolved_info(const igaos_pdhg_presolved* p, int* m, int* n, int64_t* nnz,
+                              double* obj_const, int64_t* counts6) {
+    if (!p) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    const igx::Presolved& R = p->p;
+    if (m) *m = R.m;
+    if (n) *n = R.n;
+    if (nnz) *nnz = (int64_t)R.ai.size();
+    if (obj_const) *obj_const = R.obj_const;
+    if (counts6) {
+        const igx::PresolveCounts& k = R.counts;
+        const int64_t v[6] = {k.empty_rows, k.singleton_rows, k.redundant_rows,
+                              k.fixed_cols, k.empty_cols,     k.free_singletons};
+        std::memcpy(counts6, v, sizeof(v));
+    }
+    return ok();
+}
+
+int igaos_pdhg_presolved_lp(const igaos_pdhg_presolved* p, int* ap, int* ai, double* ax,
+                            double* c, double* cl, double* cu, double* rmin, double* rmax) {
+    if (!p || !ap || !c || !cl || !cu || !rmin || !rmax ||
+        (!p->p.ai.empty() && (!ai || !ax)))
+        return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    const igx::Presolved& R = p->p;
+    std::copy(R.ap.begin(), R.ap.end(), ap);
+    std::copy(R.ai.begin(), R.ai.end(), ai);
+    std::copy(R.ax.begin(), R.ax.end(), ax);
+    std::copy(R.c.begin(), R.c.end(), c);
+    std::copy(R.cl.begin(), R.cl.end(), cl);
+    std::copy(R.cu.begin(), R.cu.end(), cu);
+    std::copy(R.rmin.begin(), R.rmin.end(), rmin);
+    std::copy(R.rmax.begin(), R.rmax.end(), rmax);
+    return ok();
+}
+
+int igaos_pdhg_postsolve(const igaos_pdhg_presolved* p, const double* x_red,
+                         const double* y_red, double* x, double* y) {
+    if (!p || !x || !y || (p->p.n > 0 && !x_red) || (p->p.m > 0 && !y_red))
+        return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    igx::postsolve(p->p, x_red, y_red, x, y);
+    return ok();
+}
+
+void igaos_pdhg_presolved_destroy(igaos_pdhg_presolved* p) { delete p; }
 
 }  // extern "C"

@@ -33,7 +33,8 @@ void usage() {
         "  --engine <name>         auto|simplex|pdhg|milp|qp (this build: pdhg)\n"
         "  --precision <p>         fp64|fp32-refine|fp32 (default fp64)\n"
         "  --verbose               engine progress to stderr (repeat for more)\n"
-        "  --detect-infeasibility  stop with infeasible/unbounded on a ray certificate\n");
+        "  --detect-infeasibility  stop with infeasible/unbounded on a ray certificate\n"
+        "  --pdhg-presolve         reduce the LP on the host first (exact dual postsolve)\n");
 }
 
 struct Args {
@@ -41,6 +42,7 @@ struct Args {
     igaos::Options opts;
     int precision = IGAOS_PDHG_FP64;
     bool detect = false;
+    bool reduce = false;
     bool ok = true;
 };
 
@@ -63,6 +65,7 @@ Args parse(int argc, char** argv) {
         else if (f == "--presolve" && has) a.opts.presolve = std::string(argv[++i]) == "on";
         else if (f == "--verbose") ++a.opts.verbosity;
         else if (f == "--detect-infeasibility") a.detect = true;
+        else if (f == "--pdhg-presolve") a.reduce = true;
         else if (f == "--out" && has) a.out = argv[++i];
         else if (f == "--engine" && has) {
             a.engine = argv[++i];
@@ -187,11 +190,12 @@ int main(int argc, char** argv) {
     }
     if (a.cmd == "info") return info(M);
     igaos::Solution s;
-    if (a.engine == "pdhg" && (a.precision != IGAOS_PDHG_FP64 || a.detect)) {
+    if (a.engine == "pdhg" && (a.precision != IGAOS_PDHG_FP64 || a.detect || a.reduce)) {
         igaos_pdhg_options o;
         igaos_pdhg_default_options(&o);
         o.precision = a.precision;
         o.detect_infeasibility = a.detect ? 1 : 0;
+        o.pdhg_presolve = a.reduce ? 1 : 0;
         s = igaos::pdhg::solve_ex(M, a.opts, &o);
     } else {
         s = igaos::solve_with_engine(M, a.opts, a.engine);

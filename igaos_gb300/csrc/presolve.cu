@@ -1,0 +1,311 @@
+// Presolve for the PDHG engine (host code; see presolve.hpp).
+#include "presolve.hpp"
+
+#include <algorithm>
+#include <cmath>
+#include <limits>
+
+namespace igx {
+namespace {
+
+constexpr double kInf = std::numeric_limits<double>::infinity();
+constexpr int kMaxRounds = 64;
+constexpr double kFeasTol = 1e-9;
+
+inline double mag(double b) { return std::isfinite(b) ? std::fabs(b) : 0.0; }
+
+}  // namespace
+
+int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const double* c,
+             const double* cl, const double* cu, const double* rmin, const double* rmax,
+             double obj_const, Presolved& P) {
+    P = Presolved();
+    P.m0 = m;
+    P.n0 = n;
+    // row-wise copy without exact zeros, and its column-wise counterpart
+    std::vector<int> rp(m + 1, 0);
+    for (int i = 0; i < m; ++i) {
+        int k = 0;
+        for (int p = ap[i]; p < ap[i + 1]; ++p) k += ax[p] != 0.0;
+        rp[i + 1] = rp[i] + k;
+    }
+    const int64_t nz = rp[m];
+    std::vector<int> rj(nz);
+    std::vector<double> ra(nz);
+    for (int i = 0, w = 0; i < m; ++i)
+        for (int p = ap[i]; p < ap[i + 1]; ++p)
+            if (ax[p] != 0.0) {
+                rj[w] = ai[p];
+                ra[w] = ax[p];
+                ++w;
+            }
+    std::vector<int>& cp = P.cp0;
+    std::vector<int>& ci = P.ci0;
+    std::vector<double>& ca = P.acx0;
+    cp.assign(n + 1, 0);
+    ci.resize(nz);
+    ca.resize(nz);
+    for (int64_t p = 0; p < nz; ++p) cp[rj[p] + 1]++;
+    for (int j = 0; j < n; ++j) cp[j + 1] += cp[j];
+    {
+        std::vector<int> next(cp.begin(), cp.end() - 1);
+        for (int i = 0; i < m; ++i)
+            for (int p = rp[i]; p < rp[i + 1]; ++p) {
+                const int q = next[rj[p]]++;
+                ci[q] = i;
+                ca[q] = ra[p];
+            }
+    }
+    P.c0.assign(c, c + n);
+
+    std::vector<double> lo(cl, cl + n), hi(cu, cu + n), cost(c, c + n);
+    std::vector<double> rlo(rmin, rmin + m), rhi(rmax, rmax + m), rscale(m);
+    for (int j = 0; j < n; ++j)
+        if (lo[j] == kInf || hi[j] == -kInf) return kPresolveInfeasible;
+    for (int i = 0; i < m; ++i) {
+        if (rlo[i] == kInf || rhi[i] == -kInf) return kPresolveInfeasible;
+        rscale[i] = 1.0 + mag(rlo[i]) + mag(rhi[i]);
+    }
+    std::vector<char> ralive(m, 1), calive(n, 1);
+    std::vector<int> rcnt(m), ccnt(n);
+    for (int i = 0; i < m; ++i) rcnt[i] = rp[i + 1] - rp[i];
+    for (int j = 0; j < n; ++j) ccnt[j] = cp[j + 1] - cp[j];
+    double shift = 0.0;
+    PresolveCounts& K = P.counts;
+
+    auto kill_row = [&](int i) {
+        ralive[i] = 0;
+        for (int p = rp[i]; p < rp[i + 1]; ++p)
+            if (calive[rj[p]]) --ccnt[rj[p]];
+    };
+    auto kill_col = [&](int j) {
+        calive[j] = 0;
+        for (int p = cp[j]; p < cp[j + 1]; ++p)
+            if (ralive[ci[p]]) --rcnt[ci[p]];
+    };
+    auto fix_col = [&](int j, double v) {
+        for (int p = cp[j]; p < cp[j + 1]; ++p) {
+            const int i = ci[p];
+            if (!ralive[i]) continue;
+            const double t = ca[p] * v;
+            rlo[i] -= t;  // -inf and +inf stay as they are
+            rhi[i] -= t;
+            rscale[i] += std::fabs(t);
+        }
+        shift += cost[j] * v;
+        PresolveRec r;
+        r.kind = PresolveRec::FixVal;
+        r.j = j;
+        r.val = v;
+        P.recs.push_back(r);
+        kill_col(j);
+    };
+    auto empty_row = [&](int i) -> bool {  // false: 0 is outside the row's range
+        const double t = kFeasTol * rscale[i];
+        if (rlo[i] > t || rhi[i] < -t) return false;
+        kill_row(i);
+        ++K.empty_rows;
+        return true;
+    };
+    auto empty_col = [&](int j) -> bool {  // false: the cost runs to an infinite bound
+        double v;
+        if (cost[j] > 0.0) {
+            if (!std::isfinite(lo[j])) return false;
+            v = lo[j];
+        } else if (cost[j] < 0.0) {
+            if (!std::isfinite(hi[j])) return false;
+            v = hi[j];
+        } else {
+            v = std::isfinite(lo[j]) ? lo[j] : (std::isfinite(hi[j]) ? hi[j] : 0.0);
+        }
+        fix_col(j, v);
+        ++K.empty_cols;
+        return true;
+    };
+
+    bool changed = true;
+    while (changed && P.rounds < kMaxRounds) {
+        changed = false;
+        ++P.rounds;
+        for (int i = 0; i < m; ++i) {
+            if (!ralive[i]) continue;
+            if (rcnt[i] == 0) {
+                if (!empty_row(i)) return kPresolveInfeasible;
+                changed = true;
+                continue;
+            }
+            if (rcnt[i] == 1) {
+                int p = rp[i];
+                while (!calive[rj[p]]) ++p;
+                const int j = rj[p];
+                const double a = ra[p];
+                // a x_j in [rlo, rhi]  <=>  x_j in [blo, bhi]
+                const double blo = a > 0.0 ? rlo[i] / a : rhi[i] / a;
+                const double bhi = a > 0.0 ? rhi[i] / a : rlo[i] / a;
+                const bool tl = blo > lo[j], th = bhi < hi[j];
+                double nlo = tl ? blo : lo[j], nhi = th ? bhi : hi[j];
+                if (nlo > nhi) {
+                    if (nlo - nhi > kFeasTol * (1.0 + mag(nlo) + mag(nhi)))
+                        return kPresolveInfeasible;
+                    if (tl && !th) nlo = nhi;  // crossing by rounding only
+                    else nhi = nlo;
+                }
+                lo[j] = nlo;
+                hi[j] = nhi;
+                PresolveRec r;
+                r.kind = PresolveRec::SingletonRow;
+                r.i = i;
+                r.j = j;
+                r.a = a;
+                r.lo_from_row = tl;
+                r.hi_from_row = th;
+                P.recs.push_back(r);
+                kill_row(i);
+                ++K.singleton_rows;
+                changed = true;
+                continue;
+            }
+            // activity range over the current column bounds
+            double L = 0.0, U = 0.0;
+            for (int p = rp[i]; p < rp[i + 1]; ++p) {
+                const int j = rj[p];
+                if (!calive[j]) continue;
+                const double a = ra[p];
+                L += a > 0.0 ? a * lo[j] : a * hi[j];
+                U += a > 0.0 ? a * hi[j] : a * lo[j];
+            }
+            if (L >= rlo[i] && U <= rhi[i]) {
+                kill_row(i);
+                ++K.redundant_rows;
+                changed = true;
+            }
+        }
+        for (int j = 0; j < n; ++j) {
+            if (!calive[j]) continue;
+            if (lo[j] == hi[j]) {
+                fix_col(j, lo[j]);
+                ++K.fixed_cols;
+                changed = true;
+                continue;
+            }
+            if (ccnt[j] == 0) {
+                if (!empty_col(j)) return kPresolveUnbounded;
+                changed = true;
+                continue;
+            }
+            if (ccnt[j] != 1 || lo[j] != -kInf || hi[j] != kInf) continue;
+            int p = cp[j];
+            while (!ralive[ci[p]]) ++p;
+            const int i = ci[p];
+            const double a = ca[p];
+            const double q = cost[j] / a;
+            double t;
+            if (q > 0.0) {
+                if (!std::isfinite(rlo[i])) return kPresolveUnbounded;
+                t = rlo[i];
+            } else if (q < 0.0) {
+                if (!std::isfinite(rhi[i])) return kPresolveUnbounded;
+                t = rhi[i];
+            } else {
+                t = std::isfinite(rlo[i]) ? rlo[i] : (std::isfinite(rhi[i]) ? rhi[i] : 0.0);
+            }
+            PresolveRec r;
+            r.kind = PresolveRec::FreeSingleton;
+            r.i = i;
+            r.j = j;
+            r.a = a;
+            r.q = q;
+            r.val = t;
+            r.t0 = (int64_t)P.term_col.size();
+            for (int s = rp[i]; s < rp[i + 1]; ++s) {
+                const int k = rj[s];
+                if (k == j || !calive[k]) continue;
+                P.term_col.push_back(k);
+                P.term_a.push_back(ra[s]);
+                cost[k] -= q * ra[s];
+            }
+            r.t1 = (int64_t)P.term_col.size();
+            shift += q * t;
+            P.recs.push_back(r);
+            kill_col(j);
+            kill_row(i);
+            ++K.free_singletons;
+            changed = true;
+        }
+    }
+    // a round cap can leave empty rows and columns behind: clear them so that
+    // the reduced LP has rows exactly when it has columns
+    for (int i = 0; i < m; ++i)
+        if (ralive[i] && rcnt[i] == 0 && !empty_row(i)) return kPresolveInfeasible;
+    for (int j = 0; j < n; ++j)
+        if (calive[j] && ccnt[j] == 0 && !empty_col(j)) return kPresolveUnbounded;
+
+    // reduced LP
+    P.row_red.assign(m, -1);
+    P.col_red.assign(n, -1);
+    for (int i = 0; i < m; ++i)
+        if (ralive[i]) P.row_red[i] = P.m++;
+    for (int j = 0; j < n; ++j)
+        if (calive[j]) P.col_red[j] = P.n++;
+    P.ap.assign(P.m + 1, 0);
+    P.ai.reserve(nz);
+    P.ax.reserve(nz);
+    P.rmin.resize(P.m);
+    P.rmax.resize(P.m);
+    for (int i = 0; i < m; ++i) {
+        const int r = P.row_red[i];
+        if (r < 0) continue;
+        P.rmin[r] = rlo[i];
+        P.rmax[r] = rhi[i];
+        for (int p = rp[i]; p < rp[i + 1]; ++p)
+            if (calive[rj[p]]) {
+                P.ai.push_back(P.col_red[rj[p]]);
+                P.ax.push_back(ra[p]);
+            }
+        P.ap[r + 1] = (int)P.ai.size();
+    }
+    P.c.resize(P.n);
+    P.cl.resize(P.n);
+    P.cu.resize(P.n);
+    for (int j = 0; j < n; ++j) {
+        const int k = P.col_red[j];
+        if (k < 0) continue;
+        P.c[k] = cost[j];
+        P.cl[k] = lo[j];
+        P.cu[k] = hi[j];
+    }
+    P.obj_const = obj_const + shift;
+    return kPresolveReduced;
+}
+
+void postsolve(const Presolved& P, const double* x_red, const double* y_red, double* x, double* y) {
+    for (int j = 0; j < P.n0; ++j) x[j] = P.col_red[j] >= 0 ? x_red[P.col_red[j]] : 0.0;
+    for (int i = 0; i < P.m0; ++i) y[i] = P.row_red[i] >= 0 ? y_red[P.row_red[i]] : 0.0;
+    // the duals of substituted rows do not depend on the solution; every
+    // reduced cost below needs them
+    for (const PresolveRec& r : P.recs)
+        if (r.kind == PresolveRec::FreeSingleton) y[r.i] = -r.q;
+    for (auto it = P.recs.rbegin(); it != P.recs.rend(); ++it) {
+        const PresolveRec& r = *it;
+        switch (r.kind) {
+            case PresolveRec::FixVal:
+                x[r.j] = r.val;
+                break;
+            case PresolveRec::FreeSingleton: {
+                double s = 0.0;
+                for (int64_t t = r.t0; t < r.t1; ++t) s += P.term_a[t] * x[P.term_col[t]];
+                x[r.j] = (r.val - s) / r.a;
+                break;
+            }
+            case PresolveRec::SingletonRow: {
+                // rows removed before this one still hold y = 0 here
+                double d = P.c0[r.j];
+                for (int p = P.cp0[r.j]; p < P.cp0[r.j + 1]; ++p) d += P.acx0[p] * y[P.ci0[p]];
+                if ((r.lo_from_row && d > 0.0) || (r.hi_from_row && d < 0.0)) y[r.i] = -d / r.a;
+                break;
+            }
+        }
+    }
+}
+
+}  // namespace igx

@@ -1,0 +1,82 @@
+// Presolve for the PDHG engine (host code). No counterpart on the reference's
+// PDHG path, whose solve ignores Options.presolve; the reference's own
+// presolve (src/simplex/presolve.hpp:176-600, Andersen & Andersen 1995) is
+// simplex-only and maps back x alone, setting y = 0 on every removed row.
+//
+// The reductions here are the subset of Andersen & Andersen whose optimal
+// duals are recovered exactly, so that postsolve turns an optimal pair of the
+// reduced LP into an optimal pair of the original (the engine's termination
+// test is on both):
+//   empty row        -- 0 must lie in [rmin, rmax]; y_i = 0;
+//   singleton row    -- a x_j in [rmin, rmax] becomes a bound of x_j; the
+//                       side(s) it tightened are recorded, and postsolve
+//                       moves a reduced cost d_j pressing on such a side
+//                       into y_i = -d_j / a;
+//   redundant row    -- its activity range over the column bounds lies in
+//                       [rmin, rmax]; y_i = 0;
+//   fixed column     -- l_j = u_j: removed, row bounds shifted by a x_j;
+//   empty column     -- x_j at the bound its cost prefers (the LP is
+//                       unbounded or infeasible when that bound is infinite);
+//   free singleton   -- a free column j met by one row i: x_j takes up the
+//                       row (activity pinned at the row bound the sign of
+//                       q = c_j / a selects), the row's other columns pay
+//                       c_k -= q a_ik, and y_i = -q.
+// Exact zeros of A are dropped. Rounds repeat until nothing changes.
+#pragma once
+
+#include <cstdint>
+#include <vector>
+
+namespace igx {
+
+struct PresolveCounts {
+    int64_t empty_rows = 0, singleton_rows = 0, redundant_rows = 0;
+    int64_t fixed_cols = 0, empty_cols = 0, free_singletons = 0;
+};
+
+// Outcome codes share the values of IGAOS_STATUS_INFEASIBLE / _UNBOUNDED.
+constexpr int kPresolveReduced = 0;
+constexpr int kPresolveInfeasible = 3;
+constexpr int kPresolveUnbounded = 4;  // dual infeasible: unbounded if feasible
+
+struct PresolveRec {
+    enum Kind : unsigned char { FixVal = 0, SingletonRow = 1, FreeSingleton = 2 } kind;
+    bool lo_from_row = false, hi_from_row = false;  // SingletonRow
+    int i = -1, j = -1;
+    double a = 0.0;    // SingletonRow / FreeSingleton: the entry a_ij
+    double val = 0.0;  // FixVal: x_j; FreeSingleton: the row target t
+    double q = 0.0;    // FreeSingleton: c_j / a_ij (y_i = -q)
+    int64_t t0 = 0, t1 = 0;  // FreeSingleton: its row's other entries in terms
+};
+
+struct Presolved {
+    // original LP, column-wise (reduced costs in postsolve) and its costs
+    int m0 = 0, n0 = 0;
+    std::vector<int> cp0, ci0;
+    std::vector<double> acx0, c0;
+    // reduced LP (CSR), its constant, and the index maps original -> reduced
+    int m = 0, n = 0;
+    std::vector<int> ap, ai;
+    std::vector<double> ax, c, cl, cu, rmin, rmax;
+    double obj_const = 0.0;
+    std::vector<int> row_red, col_red;
+    // reductions in the order they were made
+    std::vector<PresolveRec> recs;
+    std::vector<int> term_col;
+    std::vector<double> term_a;
+    PresolveCounts counts;
+    int rounds = 0;
+};
+
+// Reduces the LP (CSR, original units). Returns kPresolveReduced (out holds
+// the reduced LP, possibly with no rows and no columns), kPresolveInfeasible
+// or kPresolveUnbounded. Bounds must satisfy cl <= cu and rmin <= rmax.
+int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const double* c,
+             const double* cl, const double* cu, const double* rmin, const double* rmax,
+             double obj_const, Presolved& out);
+
+// x (n0) and y (m0) of the original LP from x_red (n) and y_red (m) of the
+// reduced one: records undone in reverse order.
+void postsolve(const Presolved& p, const double* x_red, const double* y_red, double* x, double* y);
+
+}  // namespace igx

@@ -24,7 +24,8 @@ namespace {
 
 Solution py_solve(const std::string& path, double time_limit, double tolerance,
                   long max_iterations, bool presolve, long seed, const std::string& engine,
-                  const std::string& precision, bool detect_infeasibility) {
+                  const std::string& precision, bool detect_infeasibility,
+                  bool pdhg_presolve) {
     static const char* kEngines[] = {"auto", "simplex", "pdhg", "milp", "qp"};
     bool valid = false;
     for (const char* e : kEngines) valid |= engine == e;
@@ -45,11 +46,12 @@ Solution py_solve(const std::string& path, double time_limit, double tolerance,
     o.presolve = presolve;
     o.seed = static_cast<int>(seed);
     py::gil_scoped_release nogil;
-    if (engine == "pdhg" && (prec != IGAOS_PDHG_FP64 || detect_infeasibility)) {
+    if (engine == "pdhg" && (prec != IGAOS_PDHG_FP64 || detect_infeasibility || pdhg_presolve)) {
         igaos_pdhg_options eo;
         igaos_pdhg_default_options(&eo);
         eo.precision = prec;
         eo.detect_infeasibility = detect_infeasibility ? 1 : 0;
+        eo.pdhg_presolve = pdhg_presolve ? 1 : 0;
         return igaos::pdhg::solve_ex(mdl, o, &eo);
     }
     return igaos::solve_with_engine(mdl, o, engine);
@@ -157,7 +159,8 @@ PYBIND11_MODULE(_core, m) {
     m.def("solve", &py_solve, py::arg("path"), py::arg("time_limit") = 120.0,
           py::arg("tolerance") = 1e-4, py::arg("max_iterations") = 500000L,
           py::arg("presolve") = true, py::arg("seed") = 0L, py::arg("engine") = "auto",
-          py::arg("precision") = "fp64", py::arg("detect_infeasibility") = false);
+          py::arg("precision") = "fp64", py::arg("detect_infeasibility") = false,
+          py::arg("pdhg_presolve") = false);
 
     m.def(
         "read_mps",

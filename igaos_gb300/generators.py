@@ -398,3 +398,103 @@ def free_cost_lp(m: int, n: int, extra_nnz: int, seed: int) -> LPData:
     lp.c = -aty + s
     lp.name = f"freecost-{seed}"
     return lp
+
+
+def presolvable_lp(m: int, n: int, extra_nnz: int, seed: int) -> LPData:
+    """random_lp(m, n, extra_nnz, seed) with every reduction of the engine's
+    presolve planted, feasible and bounded by construction: fixed columns in
+    base rows (row bounds shifted by their contribution), empty columns (cost
+    sign matched to a finite bound, or zero cost), empty rows around 0, free
+    columns held by two singleton rows (x >= lo and x <= hi, so the implied
+    bounds decide the optimum), free columns fixed by an equality singleton
+    row, free singleton columns in base equality rows (some with zero cost)
+    and redundant rows over boxed base columns. Rows and columns are then
+    permuted so that the planted parts are spread through the LP."""
+    rng = np.random.default_rng(seed + 7919)
+    base = random_lp(m, n, extra_nnz, seed)
+    xs = base.meta["x_star"]
+    R = list(np.repeat(np.arange(m), np.diff(base.ap)))
+    Cc = list(base.ai)
+    V = list(base.ax)
+    c, cl, cu = list(base.c), list(base.cl), list(base.cu)
+    rmin, rmax = list(base.rmin), list(base.rmax)
+
+    def col(cost, lo, hi):
+        c.append(cost)
+        cl.append(lo)
+        cu.append(hi)
+        return len(c) - 1
+
+    def row(lo, hi):
+        rmin.append(lo)
+        rmax.append(hi)
+        return len(rmin) - 1
+
+    def put(i, j, a):
+        R.append(i)
+        Cc.append(j)
+        V.append(a)
+
+    def in_base_rows(j, value, count):
+        for i in rng.choice(m, count, replace=False):
+            a = rng.standard_normal()
+            put(i, j, a)
+            rmin[i] += a * value  # -inf stays -inf
+            rmax[i] += a * value
+
+    k = max(2, n // 20)
+    for _ in range(k):  # fixed columns
+        v = rng.uniform(-3.0, 3.0)
+        in_base_rows(col(rng.standard_normal(), v, v), v, 3)
+    for t in range(k):  # empty columns
+        g = abs(rng.standard_normal()) + 0.1
+        if t % 4 == 0:
+            col(g, rng.uniform(-2.0, 0.0), INF)
+        elif t % 4 == 1:
+            col(-g, -INF, rng.uniform(0.0, 2.0))
+        elif t % 4 == 2:
+            col(0.0, -INF, INF)
+        else:
+            col(rng.standard_normal(), -1.0, 1.0)
+    for t in range(k):  # empty rows
+        if t % 3 == 0:
+            row(0.0, 0.0)
+        elif t % 3 == 1:
+            row(-INF, rng.uniform(0.0, 1.0))
+        else:
+            row(-rng.uniform(0.0, 1.0), rng.uniform(0.0, 1.0))
+    for _ in range(k):  # free columns bounded by two singleton rows
+        lo = rng.uniform(-2.0, 0.0)
+        hi = lo + rng.uniform(0.5, 2.0)
+        j = col(2.0 * rng.standard_normal(), -INF, INF)
+        in_base_rows(j, 0.5 * (lo + hi), 2)
+        a1 = rng.uniform(0.5, 2.0)
+        put(row(a1 * lo, INF), j, a1)       # a1 x >= a1 lo
+        a2 = -rng.uniform(0.5, 2.0)
+        put(row(a2 * hi, INF), j, a2)       # a2 x >= a2 hi, i.e. x <= hi
+    for _ in range(k // 2 + 1):  # free columns fixed by an equality singleton row
+        v = rng.uniform(-1.0, 1.0)
+        j = col(rng.standard_normal(), -INF, INF)
+        in_base_rows(j, v, 2)
+        a = rng.uniform(1.0, 3.0) * rng.choice([-1.0, 1.0])
+        put(row(a * v, a * v), j, a)
+    eq = rng.permutation(m // 2)[:k]  # free singleton columns in equality rows
+    for t, i in enumerate(eq):
+        j = col(0.0 if t % 3 == 0 else rng.standard_normal(), -INF, INF)
+        put(i, j, rng.uniform(0.5, 2.0) * rng.choice([-1.0, 1.0]))
+    for t in range(k):  # redundant rows over boxed base columns [0, 10]
+        js = rng.choice(n, 4, replace=False)
+        a = rng.standard_normal(4)
+        L = float(np.minimum(0.0, 10.0 * a).sum())
+        U = float(np.maximum(0.0, 10.0 * a).sum())
+        i = row(L - 1.0, U + 1.0) if t % 2 == 0 else row(-INF, U + 0.5)
+        for jj, aa in zip(js, a):
+            put(i, int(jj), float(aa))
+    M, N = len(rmin), len(c)
+    pr, pc = rng.permutation(M), rng.permutation(N)  # new index of each old one
+    lp = from_triplets(M, N, pr[np.asarray(R)], pc[np.asarray(Cc)], V,
+                       np.asarray(c)[np.argsort(pc)], np.asarray(cl)[np.argsort(pc)],
+                       np.asarray(cu)[np.argsort(pc)], np.asarray(rmin)[np.argsort(pr)],
+                       np.asarray(rmax)[np.argsort(pr)], name=f"presolvable-{seed}")
+    lp.meta = dict(seed=seed, planted=k)
+    return lp

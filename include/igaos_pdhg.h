@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define IGAOS_PDHG_ABI_VERSION 2
+#define IGAOS_PDHG_ABI_VERSION 3
 
 /* Return codes of every entry point. */
 enum {
@@ -69,7 +69,7 @@ typedef struct igaos_pdhg_options {
     double tolerance;         /* 1e-4: relative KKT (pinf, prow, dinf, gap) */
     int64_t max_iterations;   /* 500000 */
     int seed;                 /* ignored, as in the reference engine */
-    int presolve;             /* ignored, as in the reference engine */
+    int presolve;             /* ignored, as in the reference engine (see pdhg_presolve) */
     int restarts;             /* ignored: the engine always restarts */
     int verbosity;            /* 0 quiet, 1 progress, 2 debug (stderr) */
     int precision;            /* IGAOS_PDHG_FP64 (default) / FP32_REFINE / FP32 */
@@ -86,6 +86,16 @@ typedef struct igaos_pdhg_options {
      * restarts; the ray is returned in y / x (max-norm 1). 0 (default): off,
      * as the reference engine, which has no such test. Added in ABI 2. */
     int detect_infeasibility;
+    /* 1: reduce the LP on the host before the upload (empty, singleton and
+     * redundant rows; fixed, empty and free-singleton columns; see
+     * igaos_pdhg_presolve) and map the answer back with exact duals; the
+     * result's metrics are then those of the ORIGINAL LP. The handle's
+     * inspection entry points (get_scaling ... spmv) see the reduced LP, and
+     * a ray of detect_infeasibility is the reduced LP's, on the surviving
+     * rows and columns (0 elsewhere). 0 (default): off, as the reference
+     * engine, which ignores `presolve`. Read by igaos_pdhg_create. Added in
+     * ABI 3. */
+    int pdhg_presolve;
 } igaos_pdhg_options;
 
 typedef struct igaos_pdhg_result {
@@ -134,6 +144,39 @@ int igaos_pdhg_ray_certificate(int m, int n, const double* x, const double* ax, 
                                const double* aty, const double* c, const double* cl,
                                const double* cu, const double* rmin, const double* rmax,
                                double* xray, double* yray, int* kind);
+
+/* ---- presolve (host only; no device needed) ----------------------------
+ * The reductions of the pdhg_presolve option, callable on their own. The
+ * reference's PDHG path has none (its solve ignores Options.presolve); its
+ * simplex presolve (src/simplex/presolve.hpp:176-600) maps back x only. Here
+ * every reduction has an exact dual postsolve: an optimal pair of the reduced
+ * LP maps to an optimal pair of the original.
+ * igaos_pdhg_presolve reduces the CSR LP; *outcome = 0 (reduced: *out holds
+ * it, possibly with no rows and no columns), IGAOS_STATUS_INFEASIBLE or
+ * IGAOS_STATUS_UNBOUNDED (a column whose cost runs to an infinite bound: the
+ * LP is unbounded if it is feasible), with *out = NULL. */
+typedef struct igaos_pdhg_presolved igaos_pdhg_presolved;
+
+int igaos_pdhg_presolve(int m, int n, int64_t nnz, const int* ap, const int* ai,
+                        const double* ax, const double* c, const double* cl,
+                        const double* cu, const double* rmin, const double* rmax,
+                        double obj_const, igaos_pdhg_presolved** out, int* outcome);
+
+/* Sizes and constant of the reduced LP; counts6 (may be NULL) = empty rows,
+ * singleton rows, redundant rows, fixed columns, empty columns and free
+ * singleton columns removed. */
+int igaos_pdhg_presolved_info(const igaos_pdhg_presolved* p, int* m, int* n, int64_t* nnz,
+                              double* obj_const, int64_t* counts6);
+
+/* The reduced LP: ap (m+1), ai, ax (nnz), c, cl, cu (n), rmin, rmax (m). */
+int igaos_pdhg_presolved_lp(const igaos_pdhg_presolved* p, int* ap, int* ai, double* ax,
+                            double* c, double* cl, double* cu, double* rmin, double* rmax);
+
+/* x (original n) and y (original m) from x_red, y_red of the reduced LP. */
+int igaos_pdhg_postsolve(const igaos_pdhg_presolved* p, const double* x_red,
+                         const double* y_red, double* x, double* y);
+
+void igaos_pdhg_presolved_destroy(igaos_pdhg_presolved* p);
 
 /* Number of visible CUDA devices (0 when none). Replaces the handle-creation
  * probe of src/pdhg/pdhg.cu:459-465. */

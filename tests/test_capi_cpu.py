@@ -28,14 +28,17 @@ def test_exports_every_declared_symbol(native):
 
 
 def test_abi_version_and_defaults(native):
+    import ctypes as C
     from igaos_gb300 import capi
-    assert native.igaos_pdhg_abi_version() == 2
+    assert native.igaos_pdhg_abi_version() == 3
     o = capi.default_options()
     # igaos::Options defaults (reference include/igaos/options.h:5-13)
     assert o.time_limit_s == 120.0 and o.tolerance == 1e-4 and o.max_iterations == 500000
     assert o.presolve == 1 and o.restarts == 0 and o.verbosity == 0 and o.seed == 0
     assert o.precision == capi.FP64 and o.check_period == 64 and o.use_graphs == 1
     assert o.detect_infeasibility == 0  # off, as the reference engine
+    assert o.pdhg_presolve == 0  # off: the reference engine ignores `presolve`
+    assert C.sizeof(o) == 80  # ABI 3 layout of igaos_pdhg_options
 
 
 def _tiny():
@@ -100,3 +103,17 @@ def test_helper_entries_reject_bad_arguments(native):
     out = C.c_double(0.0)
     assert native.igaos_pdhg_gather_rate(4, -1, C.byref(out)) == capi.ERR_INVALID
     assert "log2_words" in capi.last_error()
+
+
+def test_presolve_entries_reject_bad_arguments(native):
+    """The host presolve entries refuse NULL handles and outputs with
+    IGAOS_PDHG_ERR_INVALID; a presolved problem handle refuses the
+    inspection entry points (their sizes are the reduced LP's)."""
+    import ctypes as C
+    from igaos_gb300 import capi
+    oc = C.c_int(-1)
+    assert native.igaos_pdhg_presolve(2, 2, 0, *([None] * 8), 0.0, None, C.byref(oc)) == \
+        capi.ERR_INVALID
+    assert native.igaos_pdhg_presolved_info(None, None, None, None, None, None) == capi.ERR_INVALID
+    assert native.igaos_pdhg_postsolve(None, None, None, None, None) == capi.ERR_INVALID
+    native.igaos_pdhg_presolved_destroy(None)  # no-op

@@ -1,0 +1,212 @@
+"""The engine's presolve on host arrays (igaos_pdhg_presolve / _postsolve; no
+GPU needed).
+
+The bar is the one the solve needs: an optimal pair of the reduced LP maps
+back to an optimal pair of the original, duals included. The optimal pair of
+the reduced LP comes from HiGHS (scipy), and the postsolved pair is checked
+with the oracle's restatement of the reference evaluate() on the ORIGINAL LP
+(primal and row infeasibility, reduced-cost complementarity and the duality
+gap), and its objective against HiGHS on the original LP.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import reference_dir
+from igaos_gb300 import generators as G
+
+INF = float("inf")
+
+
+def highs(lp):
+    """(x, y, objective) of an optimal pair by HiGHS; y in the engine's sign
+    convention (reduced cost d = c + A^T y: y >= 0 pushes a row down to rmax,
+    y <= 0 up to rmin)."""
+    opt = pytest.importorskip("scipy.optimize")
+    import scipy.sparse as sp
+    A = sp.csr_matrix((lp.ax, lp.ai, lp.ap), shape=(lp.m, lp.n))
+    hi, lo = np.isfinite(lp.rmax), np.isfinite(lp.rmin)
+    eq = hi & lo & (lp.rmin == lp.rmax)
+    up, dn = hi & ~eq, lo & ~eq
+    bounds = [(l if np.isfinite(l) else None, u if np.isfinite(u) else None)
+              for l, u in zip(lp.cl, lp.cu)]
+    kw = {}
+    if up.any() or dn.any():
+        kw.update(A_ub=sp.vstack([A[up], -A[dn]]), b_ub=np.concatenate([lp.rmax[up], -lp.rmin[dn]]))
+    if eq.any():
+        kw.update(A_eq=A[eq], b_eq=lp.rmin[eq])
+    r = opt.linprog(lp.c, bounds=bounds, method="highs",
+                    options=dict(primal_feasibility_tolerance=1e-10,
+                                 dual_feasibility_tolerance=1e-10), **kw)
+    assert r.status == 0, r.message
+    y = np.zeros(lp.m)
+    if up.any() or dn.any():
+        mu = r.ineqlin.marginals
+        y[np.nonzero(up)[0]] -= mu[:up.sum()]
+        y[np.nonzero(dn)[0]] += mu[up.sum():]
+    if eq.any():
+        y[np.nonzero(eq)[0]] -= r.eqlin.marginals
+    return r.x, y, r.fun
+
+
+def metrics(orc, lp, x, y):
+    import scipy.sparse as sp
+    A = sp.csr_matrix((lp.ax, lp.ai, lp.ap), shape=(lp.m, lp.n))
+    return orc.evaluate(lp, x, y, A @ x, lp.c + A.T @ y)
+
+
+def assert_optimal(mt, tol):
+    assert max(mt["pinf"], mt["prow"], mt["dinf"]) <= tol, mt
+    assert np.isfinite(mt["gap"]) and mt["gap"] <= tol, mt
+
+
+def tiny(rows, cols, vals, c, cl, cu, rmin, rmax):
+    return G.from_triplets(len(rmin), len(c), rows, cols, vals, c, cl, cu, rmin, rmax)
+
+
+def test_highs_pair_is_optimal_under_evaluate(native, orc):
+    """Pins the checker: the HiGHS pair, converted to the engine's sign
+    convention, is optimal for the oracle's evaluate."""
+    for lp in (G.presolvable_lp(60, 150, 250, 0), G.mixed_bounds_lp(40, 90, 150, 1)):
+        x, y, _ = highs(lp)
+        assert_optimal(metrics(orc, lp, x, y), 1e-9)
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_postsolve_of_an_optimal_reduced_pair_is_optimal(native, orc, seed):
+    from igaos_gb300 import capi
+    lp = G.presolvable_lp(60, 150, 250, seed)
+    P = capi.Presolved(lp)
+    assert P.outcome == "reduced"
+    assert P.lp.m < lp.m and P.lp.n < lp.n
+    xr, yr, fr = highs(P.lp)
+    x, y = P.postsolve(xr, yr)
+    assert_optimal(metrics(orc, lp, x, y), 1e-9)
+    _, _, f = highs(lp)
+    assert abs((fr + P.lp.obj_const) - f) <= 1e-8 * (1.0 + abs(f))
+    assert abs(lp.c @ x - f) <= 1e-8 * (1.0 + abs(f))
+
+
+def test_every_reduction_is_made(native):
+    from igaos_gb300 import capi
+    tot = dict.fromkeys(capi.PRESOLVE_COUNTS, 0)
+    for seed in range(4):
+        for k, v in capi.Presolved(G.presolvable_lp(60, 150, 250, seed)).counts.items():
+            tot[k] += v
+    assert all(v > 0 for v in tot.values()), tot
+
+
+def test_implied_bound_moves_into_the_singleton_row_dual(native, orc):
+    """min x s.t. 2x >= 4, x free: the row becomes x >= 2, the column is then
+    empty and fixed at 2, and the whole LP is gone. Postsolve moves the
+    reduced cost 1 into the row: y = -1/2 (d = 1 + 2 y = 0)."""
+    from igaos_gb300 import capi
+    lp = tiny([0], [0], [2.0], [1.0], [-INF], [INF], [4.0], [INF])
+    P = capi.Presolved(lp)
+    assert (P.lp.m, P.lp.n) == (0, 0)
+    assert P.lp.obj_const == 2.0
+    x, y = P.postsolve(np.zeros(0), np.zeros(0))
+    assert np.array_equal(x, [2.0]) and np.array_equal(y, [-0.5])
+    assert_optimal(metrics(orc, lp, x, y), 0.0)
+
+
+def test_singleton_rows_on_both_sides(native, orc):
+    """x in [0, 10] with rows x >= 3 (a = 1) and -x >= -5 (x <= 5): the
+    implied side that binds carries the dual, for either cost sign."""
+    from igaos_gb300 import capi
+    for cost, xs, ys in ((1.0, 3.0, [-1.0, 0.0]), (-1.0, 5.0, [0.0, -1.0])):
+        lp = tiny([0, 1], [0, 0], [1.0, -1.0], [cost], [0.0], [10.0], [3.0, -5.0], [INF, INF])
+        P = capi.Presolved(lp)
+        assert P.counts["singleton_rows"] == 2 and (P.lp.m, P.lp.n) == (0, 0)
+        x, y = P.postsolve(np.zeros(0), np.zeros(0))
+        assert np.array_equal(x, [xs]) and np.array_equal(y, ys), (x, y)
+        assert_optimal(metrics(orc, lp, x, y), 0.0)
+
+
+def test_free_singleton_substitution(native, orc):
+    """min x1 + 2 x2 + 3 x3 s.t. x1 + x2 + x3 = 4, x1, x2 in [0, 10], x3
+    free: x3 takes up the row (y = -3), x1 and x2 then cost -2 and -1 and go
+    to 10, x3 = -16; objective -18."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 0, 0], [0, 1, 2], [1.0, 1.0, 1.0], [1.0, 2.0, 3.0], [0.0, 0.0, -INF],
+              [10.0, 10.0, INF], [4.0], [4.0])
+    P = capi.Presolved(lp)
+    assert P.counts["free_singletons"] == 1
+    x, y = P.postsolve(np.zeros(P.lp.n), np.zeros(P.lp.m))
+    assert np.allclose(x, [10.0, 10.0, -16.0]) and np.allclose(y, [-3.0])
+    assert_optimal(metrics(orc, lp, x, y), 1e-12)
+    assert lp.c @ x == -18.0
+
+
+@pytest.mark.parametrize("case, outcome", [
+    ("empty row excludes 0", "infeasible"),
+    ("singleton rows cross", "infeasible"),
+    ("cost runs to an infinite bound", "unbounded"),
+    ("free singleton against an open row", "unbounded"),
+])
+def test_outcomes(native, case, outcome):
+    from igaos_gb300 import capi
+    lps = {
+        "empty row excludes 0": tiny([0], [0], [1.0], [1.0], [0.0], [1.0], [0.0, 1.0], [1.0, 2.0]),
+        "singleton rows cross": tiny([0, 1], [0, 0], [1.0, 1.0], [1.0], [0.0], [10.0],
+                                     [-INF, 3.0], [1.0, INF]),
+        "cost runs to an infinite bound": tiny([0], [0], [1.0], [1.0, -1.0], [0.0, 0.0],
+                                               [1.0, INF], [0.0], [1.0]),
+        "free singleton against an open row": tiny([0, 0], [0, 1], [1.0, 1.0], [0.0, 1.0],
+                                                   [0.0, -INF], [1.0, INF], [-INF], [1.0]),
+    }
+    P = capi.Presolved(lps[case])
+    assert P.outcome == outcome and P.lp is None
+
+
+def test_invalid_input_is_refused(native):
+    from igaos_gb300 import capi
+    with pytest.raises(capi.EngineError, match="lower bound above upper"):
+        capi.Presolved(tiny([0], [0], [1.0], [1.0], [2.0], [1.0], [0.0], [1.0]))
+
+
+def test_no_reduction_leaves_the_lp_unchanged(native):
+    """A dense LP with boxed columns and two-sided rows that bind: nothing to
+    reduce, and the reduced LP is the input, array for array."""
+    from igaos_gb300 import capi
+    rng = np.random.default_rng(5)
+    m, n = 6, 9
+    r, c_ = np.nonzero(np.ones((m, n)))
+    lp = tiny(r, c_, rng.uniform(0.5, 1.5, m * n), rng.standard_normal(n), np.zeros(n),
+              np.full(n, 10.0), np.full(m, 1.0), np.full(m, 3.0))
+    P = capi.Presolved(lp)
+    assert sum(P.counts.values()) == 0
+    for k in ("ap", "ai", "ax", "c", "cl", "cu", "rmin", "rmax"):
+        assert np.array_equal(getattr(P.lp, k), getattr(lp, k)), k
+    x, y = P.postsolve(np.arange(n, dtype=float), np.arange(m, dtype=float))
+    assert np.array_equal(x, np.arange(n)) and np.array_equal(y, np.arange(m))
+
+
+NETLIB = ["afiro", "kb2", "sc50a", "adlittle", "bandm", "grow22", "boeing1", "degen2",
+          "etamacro", "forplan"]
+
+
+@pytest.mark.skipif(reference_dir() is None, reason="reference tree not present")
+@pytest.mark.parametrize("name", NETLIB)
+def test_netlib_postsolve(native, orc, name):
+    """Netlib LPs read by the engine's MPS reader: the postsolved HiGHS pair
+    of the reduced LP is optimal for the original."""
+    from igaos_gb300 import build, capi
+    path = os.path.join(reference_dir(), "demo", "models", "netlib_full", name + ".mps")
+    if not os.path.exists(path):
+        pytest.skip("netlib file missing")
+    build.build()
+    from igaos_gb300 import _core
+    M = _core.read_mps(path)
+    a = lambda v, t=float: np.asarray(v, t)
+    lp = G.LPData(M.m, M.n, a(M.ap, np.int32), a(M.ai, np.int32), a(M.ax), a(M.cp, np.int32),
+                  a(M.ci, np.int32), a(M.acx), a(M.c), a(M.cl), a(M.cu), a(M.rmin), a(M.rmax),
+                  float(M.obj_const))
+    P = capi.Presolved(lp)
+    assert P.outcome == "reduced"
+    xr, yr, _ = highs(P.lp)
+    x, y = P.postsolve(xr, yr)
+    assert_optimal(metrics(orc, lp, x, y), 1e-8)
+    _, _, f = highs(lp)
+    assert abs(lp.c @ x - f) <= 1e-8 * (1.0 + abs(f))
