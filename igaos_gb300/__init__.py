@@ -9,9 +9,10 @@ kernels through the C ABI in include/igaos_pdhg.h.
 
 GB300 extensions:
     solve(..., precision="fp64"|"fp32-refine"|"fp32", detect_infeasibility=False,
-          pdhg_presolve=False)
+          pdhg_presolve=False, crossover=False)
     capi.Problem / capi.solve_lp  -- LPs given as CSR arrays (C ABI via ctypes)
     capi.Presolved                -- the engine's presolve / postsolve on the host
+    capi.crossover                -- host crossover from any point to an optimal vertex
     generators                    -- seeded synthetic LPs of the benchmark shapes
 """
 from __future__ import annotations

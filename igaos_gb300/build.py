@@ -26,7 +26,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", INC, "-I", CSRC] + ARCH
 CU_SOURCES = ["engine.cu", "capi.cu", "batch.cu", "kkt_noalloc.cu", "unrolled.cu", "repair.cu",
-              "calibrate.cu", "certificate.cu", "presolve.cu"]
+              "calibrate.cu", "certificate.cu", "presolve.cu",
+              "crossover.cu"]
 # host code whose arithmetic must not be contracted into FMAs on any host
 # (dual repair: bit-identical to the reference host code on x86 and Arm)
 EXTRA_FLAGS = {"repair.cu": ["-Xcompiler", "-ffp-contract=off"]}

@@ -32,7 +32,7 @@ class Options(C.Structure):
         ("restarts", C.c_int), ("verbosity", C.c_int), ("precision", C.c_int),
         ("check_period", C.c_int), ("inner_tolerance", C.c_double),
         ("max_refinements", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
-        ("detect_infeasibility", C.c_int), ("pdhg_presolve", C.c_int),
+        ("detect_infeasibility", C.c_int), ("pdhg_presolve", C.c_int), ("crossover", C.c_int),
     ]
 
 
@@ -63,6 +63,18 @@ class BatchResult(C.Structure):
         ("restarts", C.c_int64), ("kernel_time_ms", C.c_double), ("total_time_ms", C.c_double),
         ("instance_time_ms", C.c_double),
     ]
+
+
+class CrossoverInfo(C.Structure):
+    _fields_ = [
+        ("status", C.c_int), ("pad", C.c_int), ("pushes", C.c_int64), ("pivots", C.c_int64),
+        ("bound_flips", C.c_int64), ("phase1_iterations", C.c_int64),
+        ("refactorizations", C.c_int64), ("basis_repairs", C.c_int64),
+        ("superbasic_left", C.c_int64), ("time_ms", C.c_double),
+    ]
+
+
+CROSSOVER_STATUS = ["optimal", "pivot-cap", "singular", "unbounded", "infeasible", "too-large"]
 
 
 class UnrolledLayout(C.Structure):
@@ -119,6 +131,9 @@ def lib():
         L.igaos_pdhg_postsolve.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.igaos_pdhg_presolved_destroy.argtypes = [C.c_void_p]
         L.igaos_pdhg_presolved_destroy.restype = None
+        L.igaos_pdhg_crossover.argtypes = [
+            C.c_int, C.c_int, C.c_int64, _ip, _ip] + [_dp] * 9 + [
+            C.POINTER(C.c_byte), C.POINTER(CrossoverInfo)]
         L.igaos_pdhg_dual_repair_device.argtypes = [C.c_void_p, _dp, _dp, C.c_double,
                                                     C.c_double, _dp, C.POINTER(C.c_int), _dp]
         L.igaos_pdhg_solve_batch.argtypes = [
@@ -221,6 +236,27 @@ class Presolved:
             self.h = None
 
     __del__ = close
+
+
+def crossover(lp, x0):
+    """(x, y, basis, info): an optimal vertex of the LP reached from the start
+    point x0 by the engine's host crossover (igaos_pdhg_crossover; no GPU
+    needed, m <= 2048). basis codes: 0 at lower, 1 at upper, 2 basic, 3
+    inside its bounds; n structurals, then m row activities. info is a dict
+    with "status" (CROSSOVER_STATUS name) and the pivot counts."""
+    a = _arrays(lp, with_transpose=False)
+    m, n = int(lp.m), int(lp.n)
+    x0 = np.ascontiguousarray(x0, np.float64)
+    x, y = np.zeros(n), np.zeros(m)
+    basis = np.zeros(n + m, np.int8)
+    info = CrossoverInfo()
+    _check(lib().igaos_pdhg_crossover(
+        m, n, int(a["ap"][m]), _i(a["ap"]), _i(a["ai"]), _d(a["ax"]),
+        *[_d(a[k]) for k in ("c", "cl", "cu", "rmin", "rmax")], _d(x0), _d(x), _d(y),
+        basis.ctypes.data_as(C.POINTER(C.c_byte)), C.byref(info)))
+    d = {f: getattr(info, f) for f, _ in CrossoverInfo._fields_ if f != "pad"}
+    d["status"] = CROSSOVER_STATUS[info.status]
+    return x, y, basis, d
 
 
 def last_error() -> str:

@@ -12,6 +12,7 @@
 
 #include "engine.hpp"
 #include "certificate.hpp"
+#include "crossover.hpp"
 #include "presolve.hpp"
 #include "repair.hpp"
 
@@ -24,6 +25,8 @@ struct igaos_pdhg_problem {
     igx::HostLP orig;
     double obj_const = 0.0;
     double presolve_ms = 0.0;
+    // crossover: requested at create (m <= 2048); orig then also holds A as CSC
+    bool xo = false;
 };
 
 struct igaos_pdhg_presolved {
@@ -233,6 +236,58 @@ int solve_presolved(igaos_pdhg_problem* p, const igaos_pdhg_options& o, igaos_pd
     if (y) std::memcpy(y, yo.data(), sizeof(double) * m0);
     return ok();
 }
+// Crossover after a solve (crossover option): from the answer's x to a
+// vertex of the original LP; the vertex replaces the answer (status
+// IGAOS_STATUS_OPTIMAL) when crossover ends at an optimal basis whose pair
+// passes the tolerance on the original LP. Rays and errors are left alone.
+void run_crossover(igaos_pdhg_problem* p, const igaos_pdhg_options& o, igaos_pdhg_result* res,
+                   double* x, double* y) {
+    const int st = res->status;
+    if (st == IGAOS_STATUS_ERROR || st == IGAOS_STATUS_INFEASIBLE ||
+        st == IGAOS_STATUS_UNBOUNDED)
+        return;
+    const igx::HostLP& L = p->orig;
+    std::vector<double> xv(L.n), yv(L.m), ax(L.m), d(L.n);
+    igx::CrossoverInfo info;
+    igx::crossover(L.m, L.n, L.cp.data(), L.ci.data(), L.acx.data(), L.c.data(), L.cl.data(),
+                   L.cu.data(), L.rmin.data(), L.rmax.data(), x, xv.data(), yv.data(), nullptr,
+                   info);
+    res->solve_time_ms += info.time_ms;
+    bool taken = false;
+    if (info.status == igx::kXoOptimal) {
+        for (int j = 0; j < L.n; ++j) {
+            double dj = L.c[j];
+            for (int q = L.cp[j]; q < L.cp[j + 1]; ++q) {
+                ax[L.ci[q]] += L.acx[q] * xv[j];
+                dj += L.acx[q] * yv[L.ci[q]];
+            }
+            d[j] = dj;
+        }
+        const igx::HostMetrics mt = igx::host_evaluate(L, xv.data(), yv.data(), ax.data(), d.data());
+        if (mt.pinf <= o.tolerance && mt.dinf <= o.tolerance && mt.prow <= o.tolerance &&
+            std::isfinite(mt.gap) && mt.gap <= o.tolerance) {
+            taken = true;
+            res->status = IGAOS_STATUS_OPTIMAL;
+            res->objective = mt.op + p->obj_const;
+            res->pinf = mt.pinf;
+            res->dinf = mt.dinf;
+            res->rel_gap = mt.gap;
+            res->prow = mt.prow;
+            std::memcpy(x, xv.data(), sizeof(double) * L.n);
+            std::memcpy(y, yv.data(), sizeof(double) * L.m);
+        }
+    }
+    static const char* kNames[] = {"optimal", "pivot cap", "singular basis", "unbounded edge",
+                                   "infeasible", "too large"};
+    char note[96];
+    std::snprintf(note, sizeof(note), "crossover: %s, %lld pivots, %.0f ms",
+                  taken ? "optimal vertex" : kNames[info.status], (long long)info.pivots,
+                  info.time_ms);
+    char msg[sizeof(res->message)];
+    std::snprintf(msg, sizeof(msg), "%.*s; %s", (int)(sizeof(msg) - std::strlen(note) - 3),
+                  res->message, note);
+    std::memcpy(res->message, msg, sizeof(msg));
+}
 }  // namespace
 
 int igx::igx_set_error(int code, const char* msg) {
@@ -331,6 +386,19 @@ int igaos_pdhg_create(igaos_pdhg_problem** out, int m, int n, int64_t nnz, const
             p->eng = new igx::Engine(m, n, nnz, ap, ai, ax, cp, ci, acx, c, cl, cu, rmin, rmax,
                                      obj_const, dev);
         }
+        if (opt && opt->crossover && m <= igx::kCrossoverMaxRows) {
+            p->xo = true;
+            igx::HostLP& o = p->orig;
+            o.m = m;
+            o.n = n;
+            o.c.assign(c, c + n);
+            o.cl.assign(cl, cl + n);
+            o.cu.assign(cu, cu + n);
+            o.rmin.assign(rmin, rmin + m);
+            o.rmax.assign(rmax, rmax + m);
+            transpose_host(m, n, ap, ai, ax, o.cp, o.ci, o.acx);
+            p->obj_const = obj_const;
+        }
         *out = p.release();
     });
 }
@@ -344,16 +412,30 @@ int igaos_pdhg_solve(igaos_pdhg_problem* p, const igaos_pdhg_options* opt,
     else igaos_pdhg_default_options(&o);
     if (!(o.tolerance > 0)) return fail(IGAOS_PDHG_ERR_INVALID, "tolerance must be positive");
     if (o.precision < 0 || o.precision > 2) return fail(IGAOS_PDHG_ERR_INVALID, "unknown precision");
-    if (p->pre) return solve_presolved(p, o, res, x, y);
-    int rc = guarded([&] { p->eng->solve(o, *res, x, y); });
-    if (rc != IGAOS_PDHG_OK) {
-        std::memset(res, 0, sizeof(*res));
-        res->status = IGAOS_STATUS_ERROR;
-        res->error_code = rc;
-        std::snprintf(res->message, sizeof(res->message), "%.159s", g_msg);
-        return rc;
+    std::vector<double> xb, yb;  // the answer, when crossover needs it and the caller does not
+    if (p->xo && !x) {
+        xb.resize(p->orig.n);
+        x = xb.data();
     }
-    if (res->error_code != IGAOS_PDHG_OK) return fail(res->error_code, res->message);
+    if (p->xo && !y) {
+        yb.resize(p->orig.m);
+        y = yb.data();
+    }
+    int rc;
+    if (p->pre) {
+        rc = solve_presolved(p, o, res, x, y);
+    } else {
+        rc = guarded([&] { p->eng->solve(o, *res, x, y); });
+        if (rc != IGAOS_PDHG_OK) {
+            std::memset(res, 0, sizeof(*res));
+            res->status = IGAOS_STATUS_ERROR;
+            res->error_code = rc;
+            std::snprintf(res->message, sizeof(res->message), "%.159s", g_msg);
+            return rc;
+        }
+        if (res->error_code != IGAOS_PDHG_OK) return fail(res->error_code, res->message);
+    }
+    if (rc == IGAOS_PDHG_OK && p->xo) rc = guarded([&] { run_crossover(p, o, res, x, y); });
     return rc;
 }
 
@@ -531,5 +613,35 @@ int igaos_pdhg_postsolve(const igaos_pdhg_presolved* p, const double* x_red,
 }
 
 void igaos_pdhg_presolved_destroy(igaos_pdhg_presolved* p) { delete p; }
+
+int igaos_pdhg_crossover(int m, int n, int64_t nnz, const int* ap, const int* ai,
+                         const double* ax, const double* c, const double* cl, const double* cu,
+                         const double* rmin, const double* rmax, const double* x0, double* x,
+                         double* y, signed char* basis, igaos_pdhg_crossover_info* info) {
+    if (!x0 || !x || !y || !info) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    return guarded([&] {
+        validate(m, n, nnz, ap, ai, ax, nullptr, nullptr, nullptr, c, cl, cu, rmin, rmax);
+        for (int j = 0; j < n; ++j)
+            if (!std::isfinite(x0[j])) throw std::invalid_argument("x0 must be finite");
+        if (m > igx::kCrossoverMaxRows)
+            throw std::invalid_argument("crossover needs m <= 2048 (dense basis inverse)");
+        std::vector<int> cp, ci;
+        std::vector<double> acx;
+        transpose_host(m, n, ap, ai, ax, cp, ci, acx);
+        igx::CrossoverInfo ci_;
+        igx::crossover(m, n, cp.data(), ci.data(), acx.data(), c, cl, cu, rmin, rmax, x0, x, y,
+                       basis, ci_);
+        std::memset(info, 0, sizeof(*info));
+        info->status = ci_.status;
+        info->pushes = ci_.pushes;
+        info->pivots = ci_.pivots;
+        info->bound_flips = ci_.bound_flips;
+        info->phase1_iterations = ci_.phase1_iters;
+        info->refactorizations = ci_.refactors;
+        info->basis_repairs = ci_.basis_repairs;
+        info->superbasic_left = ci_.superbasic_left;
+        info->time_ms = ci_.time_ms;
+    });
+}
 
 }  // extern "C"

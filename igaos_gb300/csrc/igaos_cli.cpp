@@ -34,7 +34,8 @@ void usage() {
         "  --precision <p>         fp64|fp32-refine|fp32 (default fp64)\n"
         "  --verbose               engine progress to stderr (repeat for more)\n"
         "  --detect-infeasibility  stop with infeasible/unbounded on a ray certificate\n"
-        "  --pdhg-presolve         reduce the LP on the host first (exact dual postsolve)\n");
+        "  --pdhg-presolve         reduce the LP on the host first (exact dual postsolve)\n"
+        "  --crossover             finish at an optimal vertex (host simplex, m <= 2048)\n");
 }
 
 struct Args {
@@ -43,6 +44,7 @@ struct Args {
     int precision = IGAOS_PDHG_FP64;
     bool detect = false;
     bool reduce = false;
+    bool xo = false;
     bool ok = true;
 };
 
@@ -66,6 +68,7 @@ Args parse(int argc, char** argv) {
         else if (f == "--verbose") ++a.opts.verbosity;
         else if (f == "--detect-infeasibility") a.detect = true;
         else if (f == "--pdhg-presolve") a.reduce = true;
+        else if (f == "--crossover") a.xo = true;
         else if (f == "--out" && has) a.out = argv[++i];
         else if (f == "--engine" && has) {
             a.engine = argv[++i];
@@ -190,12 +193,13 @@ int main(int argc, char** argv) {
     }
     if (a.cmd == "info") return info(M);
     igaos::Solution s;
-    if (a.engine == "pdhg" && (a.precision != IGAOS_PDHG_FP64 || a.detect || a.reduce)) {
+    if (a.engine == "pdhg" && (a.precision != IGAOS_PDHG_FP64 || a.detect || a.reduce || a.xo)) {
         igaos_pdhg_options o;
         igaos_pdhg_default_options(&o);
         o.precision = a.precision;
         o.detect_infeasibility = a.detect ? 1 : 0;
         o.pdhg_presolve = a.reduce ? 1 : 0;
+        o.crossover = a.xo ? 1 : 0;
         s = igaos::pdhg::solve_ex(M, a.opts, &o);
     } else {
         s = igaos::solve_with_engine(M, a.opts, a.engine);

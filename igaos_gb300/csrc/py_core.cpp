@@ -25,7 +25,7 @@ namespace {
 Solution py_solve(const std::string& path, double time_limit, double tolerance,
                   long max_iterations, bool presolve, long seed, const std::string& engine,
                   const std::string& precision, bool detect_infeasibility,
-                  bool pdhg_presolve) {
+                  bool pdhg_presolve, bool crossover) {
     static const char* kEngines[] = {"auto", "simplex", "pdhg", "milp", "qp"};
     bool valid = false;
     for (const char* e : kEngines) valid |= engine == e;
@@ -46,12 +46,14 @@ Solution py_solve(const std::string& path, double time_limit, double tolerance,
     o.presolve = presolve;
     o.seed = static_cast<int>(seed);
     py::gil_scoped_release nogil;
-    if (engine == "pdhg" && (prec != IGAOS_PDHG_FP64 || detect_infeasibility || pdhg_presolve)) {
+    if (engine == "pdhg" && (prec != IGAOS_PDHG_FP64 || detect_infeasibility || pdhg_presolve ||
+                             crossover)) {
         igaos_pdhg_options eo;
         igaos_pdhg_default_options(&eo);
         eo.precision = prec;
         eo.detect_infeasibility = detect_infeasibility ? 1 : 0;
         eo.pdhg_presolve = pdhg_presolve ? 1 : 0;
+        eo.crossover = crossover ? 1 : 0;
         return igaos::pdhg::solve_ex(mdl, o, &eo);
     }
     return igaos::solve_with_engine(mdl, o, engine);
@@ -160,7 +162,7 @@ PYBIND11_MODULE(_core, m) {
           py::arg("tolerance") = 1e-4, py::arg("max_iterations") = 500000L,
           py::arg("presolve") = true, py::arg("seed") = 0L, py::arg("engine") = "auto",
           py::arg("precision") = "fp64", py::arg("detect_infeasibility") = false,
-          py::arg("pdhg_presolve") = false);
+          py::arg("pdhg_presolve") = false, py::arg("crossover") = false);
 
     m.def(
         "read_mps",

@@ -96,6 +96,13 @@ typedef struct igaos_pdhg_options {
      * engine, which ignores `presolve`. Read by igaos_pdhg_create. Added in
      * ABI 3. */
     int pdhg_presolve;
+    /* 1: after the solve, run igaos_pdhg_crossover on the host from the
+     * answer's x (LPs with m <= 2048); when it ends at an optimal basis whose
+     * pair passes the tolerance on the original LP, that vertex replaces the
+     * answer and the status is IGAOS_STATUS_OPTIMAL (the PDHG answer alone is
+     * NEAR_OPTIMAL). Read by igaos_pdhg_create. 0 (default): off. Added in
+     * ABI 3. */
+    int crossover;
 } igaos_pdhg_options;
 
 typedef struct igaos_pdhg_result {
@@ -177,6 +184,33 @@ int igaos_pdhg_postsolve(const igaos_pdhg_presolved* p, const double* x_red,
                          const double* y_red, double* x, double* y);
 
 void igaos_pdhg_presolved_destroy(igaos_pdhg_presolved* p);
+
+/* ---- crossover (host only; no device needed) ----------------------------
+ * From a start point x0 (n; a PDHG answer, or any point) to an optimal
+ * vertex of the LP: primal push of the structurals inside their bounds from
+ * the slack basis, then a composite primal simplex (phase 1 on the basic
+ * bound violations, phase 2 on the cost) with a dense explicit basis
+ * inverse, so m <= 2048. No reference counterpart: the reference's PDHG
+ * returns its last iterate, its simplex (src/simplex/simplex.hpp:12-28)
+ * takes no start point. On status 0, x (n) and y (m; d = c + A^T y) are an
+ * optimal basic pair and basis (n + m, may be NULL) holds 0 at lower, 1 at
+ * upper, 2 basic, 3 inside its bounds (nonbasic with reduced cost 0) for
+ * the structurals and then the row activities. */
+typedef struct igaos_pdhg_crossover_info {
+    int status;               /* 0 optimal vertex, 1 pivot cap, 2 singular basis,
+                                 3 unbounded edge, 4 infeasible (phase 1), 5 m > 2048 */
+    int pad;
+    int64_t pushes, pivots, bound_flips, phase1_iterations, refactorizations;
+    int64_t basis_repairs;    /* dependent basis columns swapped for row slacks */
+    int64_t superbasic_left;  /* structurals left inside their bounds, nonbasic */
+    double time_ms;
+} igaos_pdhg_crossover_info;
+
+int igaos_pdhg_crossover(int m, int n, int64_t nnz, const int* ap, const int* ai,
+                         const double* ax, const double* c, const double* cl,
+                         const double* cu, const double* rmin, const double* rmax,
+                         const double* x0, double* x, double* y, signed char* basis,
+                         igaos_pdhg_crossover_info* info);
 
 /* Number of visible CUDA devices (0 when none). Replaces the handle-creation
  * probe of src/pdhg/pdhg.cu:459-465. */

@@ -38,6 +38,7 @@ def test_abi_version_and_defaults(native):
     assert o.precision == capi.FP64 and o.check_period == 64 and o.use_graphs == 1
     assert o.detect_infeasibility == 0  # off, as the reference engine
     assert o.pdhg_presolve == 0  # off: the reference engine ignores `presolve`
+    assert o.crossover == 0
     assert C.sizeof(o) == 80  # ABI 3 layout of igaos_pdhg_options
 
 

@@ -1,0 +1,141 @@
+"""The engine's host crossover (igaos_pdhg_crossover; no GPU needed).
+
+From a start point (a PDHG-like answer near the optimum, a vertex, or a point
+far from it) crossover must end at an optimal VERTEX:
+* the pair is optimal for the oracle's restatement of the reference
+  evaluate() (1e-9) and its objective is HiGHS's;
+* exactly m variables are basic, their columns of [A -I] have full rank, and
+  every nonbasic variable sits exactly on a bound.
+"""
+import os
+
+import numpy as np
+import pytest
+
+from conftest import reference_dir
+from igaos_gb300 import generators as G
+from test_presolve_cpu import assert_optimal, highs, metrics, tiny
+
+INF = float("inf")
+
+
+def assert_vertex(lp, x, basis, info):
+    import scipy.sparse as sp
+    A = sp.csr_matrix((lp.ax, lp.ai, lp.ap), shape=(lp.m, lp.n)).toarray()
+    full = np.hstack([A, -np.eye(lp.m)])
+    vals = np.concatenate([x, A @ x])
+    lo = np.concatenate([lp.cl, lp.rmin])
+    hi = np.concatenate([lp.cu, lp.rmax])
+    basic = basis == 2
+    assert basic.sum() == lp.m
+    assert np.linalg.matrix_rank(full[:, basic]) == lp.m
+    at_lo, at_hi = basis == 0, basis == 1
+    assert np.array_equal(vals[:lp.n][at_lo[:lp.n]], lo[:lp.n][at_lo[:lp.n]])
+    assert np.array_equal(vals[:lp.n][at_hi[:lp.n]], hi[:lp.n][at_hi[:lp.n]])
+    assert (basis == 3).sum() == info["superbasic_left"]
+
+
+def starts(lp, xs, rng):
+    fin = np.isfinite(lp.cl) & np.isfinite(lp.cu)
+    box = np.where(fin, 0.5 * (np.where(fin, lp.cl, 0.0) + np.where(fin, lp.cu, 0.0)), 0.0)
+    return {
+        "vertex": xs,
+        "near": xs + 1e-7 * (1 + np.abs(xs)) * rng.standard_normal(lp.n),
+        "rough": xs + 1e-2 * (1 + np.abs(xs)) * rng.standard_normal(lp.n),
+        "zero": np.zeros(lp.n),
+        "box": box,
+    }
+
+
+LPS = {
+    "random": lambda s: G.random_lp(60, 150, 250, s),
+    "mixed": lambda s: G.mixed_bounds_lp(40, 90, 150, s),
+    "presolvable": lambda s: G.presolvable_lp(60, 150, 250, s),
+    "known": lambda s: G.known_optimum_lp(50, 120, 200, s)[0],
+}
+
+
+@pytest.mark.parametrize("kind", sorted(LPS))
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_crossover_reaches_an_optimal_vertex(native, orc, kind, seed):
+    from igaos_gb300 import capi
+    lp = LPS[kind](seed)
+    xs, _, f = highs(lp)
+    for name, x0 in starts(lp, xs, np.random.default_rng(seed)).items():
+        x, y, basis, info = capi.crossover(lp, x0)
+        assert info["status"] == "optimal", (name, info)
+        assert_optimal(metrics(orc, lp, x, y), 1e-9)
+        assert abs(lp.c @ x - f) <= 1e-9 * (1.0 + abs(f)), (name, lp.c @ x, f)
+        assert_vertex(lp, x, basis, info)
+
+
+def test_free_empty_column_with_zero_cost_stays_inside(native, orc):
+    """A free column with no entries and zero cost can neither enter the
+    basis nor reach a bound: it is reported as left inside its bounds."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 1], [0, 0], [1.0, 1.0], [1.0, 0.0], [0.0, -INF], [10.0, INF], [1.0, -INF],
+              [INF, 5.0])
+    x, y, basis, info = capi.crossover(lp, np.array([3.0, 0.7]))
+    assert info["status"] == "optimal" and info["superbasic_left"] == 1
+    assert x[0] == 1.0 and basis[1] == 3 and x[1] == 0.7
+    assert_optimal(metrics(orc, lp, x, y), 0.0)
+
+
+@pytest.mark.parametrize("case, status", [
+    ("infeasible", "infeasible"),
+    ("unbounded", "unbounded"),
+])
+def test_outcomes(native, case, status):
+    from igaos_gb300 import capi
+    lp = {
+        # x1 + x2 <= 1 and x1 + x2 >= 3 on [0, 5]^2
+        "infeasible": tiny([0, 0, 1, 1], [0, 1, 0, 1], [1.0] * 4, [1.0, 1.0], [0.0, 0.0],
+                           [5.0, 5.0], [-INF, 3.0], [1.0, INF]),
+        # min -x1 s.t. x1 - x2 <= 1, x >= 0
+        "unbounded": tiny([0, 0], [0, 1], [1.0, -1.0], [-1.0, 0.0], [0.0, 0.0], [INF, INF],
+                          [-INF], [1.0]),
+    }[case]
+    _, _, _, info = capi.crossover(lp, np.zeros(lp.n))
+    assert info["status"] == status
+
+
+def test_arguments_are_checked(native):
+    from igaos_gb300 import capi
+    lp = G.random_lp(8, 12, 10, 0)
+    with pytest.raises(capi.EngineError, match="finite"):
+        capi.crossover(lp, np.full(lp.n, np.nan))
+    big = G.random_lp(2049, 2100, 10, 0)
+    with pytest.raises(capi.EngineError, match="m <= 2048"):
+        capi.crossover(big, np.zeros(big.n))
+
+
+NETLIB = ["afiro", "kb2", "sc50a", "adlittle", "bandm", "grow22", "boeing1", "degen2",
+          "etamacro", "forplan", "share2b", "sc205", "israel", "scagr25", "stocfor1", "agg",
+          "brandy", "e226", "scfxm1", "capri"]
+
+
+@pytest.mark.skipif(reference_dir() is None, reason="reference tree not present")
+@pytest.mark.parametrize("name", NETLIB)
+def test_netlib(native, orc, name):
+    """Netlib LPs read by the engine's MPS reader, from a point 1e-4 off the
+    HiGHS optimum and from zero (brandy has dependent rows: a basis repair
+    case; grow22's rows reach 1e-10 only, rounding of its large data)."""
+    from igaos_gb300 import build, capi
+    path = os.path.join(reference_dir(), "demo", "models", "netlib_full", name + ".mps")
+    if not os.path.exists(path):
+        pytest.skip("netlib file missing")
+    build.build()
+    from igaos_gb300 import _core
+    M = _core.read_mps(path)
+    a = lambda v, t=float: np.asarray(v, t)
+    lp = G.LPData(M.m, M.n, a(M.ap, np.int32), a(M.ai, np.int32), a(M.ax), a(M.cp, np.int32),
+                  a(M.ci, np.int32), a(M.acx), a(M.c), a(M.cl), a(M.cu), a(M.rmin), a(M.rmax),
+                  float(M.obj_const))
+    xs, _, f = highs(lp)
+    rng = np.random.default_rng(1)
+    for x0 in (xs + 1e-4 * (1 + np.abs(xs)) * rng.standard_normal(lp.n), np.zeros(lp.n)):
+        x, y, basis, info = capi.crossover(lp, x0)
+        assert info["status"] == "optimal", info
+        assert_optimal(metrics(orc, lp, x, y), 1e-9)
+        assert abs(lp.c @ x - f) <= 1e-9 * (1.0 + abs(f))
+        assert (basis == 2).sum() == lp.m
