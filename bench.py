@@ -10,7 +10,9 @@ iterations), from a cold start on device-resident data.
 Also reported (extra keys): time to 1e-8 relative KKT on the small random LP
 (m=2,000, n=5,000) for FP32+refine vs plain FP64 and the CPU oracle, where
 all of them converge; the large LP is not solved to 1e-8 by either
-precision in a bench-sized budget (see --tol-probe).
+precision in a bench-sized budget (see --tol-probe). With it,
+`crossover_from_fp32_refine`: the host crossover (igaos_pdhg_crossover) from
+the FP32+refine answer to an optimal vertex, wall time and pivots.
 `time_to_1e-8_multicommodity_lp`: the same comparison on the 1.08M x 2.87M
 multicommodity-flow LP. `batched_small_lps`:
 4,096 uneven small LPs solved to 1e-6 in one persistent launch vs
@@ -362,8 +364,20 @@ def main():
                 r = P.solve(precision=prec, tolerance=1e-8, time_limit=60.0)
                 small[prec] = {"status": r["status_name"], "s": r["device_time_ms"] / 1e3,
                                "iterations": r["iterations"], "objective": r["objective"]}
+                x_last = r["x"]
         if small["fp64"]["status"] == small["fp32-refine"]["status"] == "near-optimal":
             small["speedup_fp32_refine_vs_fp64"] = small["fp64"]["s"] / small["fp32-refine"]["s"]
+        # host crossover from the FP32 + refinement answer to an optimal vertex
+        # (a probe: the line does not depend on it)
+        try:
+            t0 = time.perf_counter()
+            xv, _, _, xi = capi.crossover(slp, x_last)
+            small["crossover_from_fp32_refine"] = {
+                "status": xi["status"], "s": time.perf_counter() - t0, "pivots": xi["pivots"],
+                "host_threads": min(16, os.cpu_count() or 1),
+                "objective": float(slp.c @ xv + slp.obj_const)}
+        except Exception as e:
+            small["crossover_from_fp32_refine"] = {"error": str(e)[:200]}
         from oracle import oracle as O
         rr = O.pdhg_solve(O.lp_from(slp), tolerance=1e-8, time_limit=120.0,
                           threads=os.cpu_count() or 1)
