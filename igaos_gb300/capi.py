@@ -129,6 +129,8 @@ def lib():
                                                 C.POINTER(C.c_int64)]
         L.igaos_pdhg_presolved_lp.argtypes = [C.c_void_p, _ip, _ip] + [_dp] * 6
         L.igaos_pdhg_postsolve.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        L.igaos_pdhg_postsolve_ray.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
+        L.igaos_pdhg_presolved_ray.argtypes = [C.c_void_p, _dp]
         L.igaos_pdhg_presolved_destroy.argtypes = [C.c_void_p]
         L.igaos_pdhg_presolved_destroy.restype = None
         L.igaos_pdhg_crossover.argtypes = [
@@ -189,7 +191,9 @@ class Presolved:
     """The engine's presolve of an LP on the host (igaos_pdhg_presolve; no
     GPU needed): `outcome` is "reduced", "infeasible" or "unbounded"; when
     reduced, `lp` is the reduced LP (an LPData), `counts` the reductions made,
-    and postsolve(x_red, y_red) maps a pair of the reduced LP back."""
+    postsolve(x_red, y_red) maps a pair of the reduced LP back and
+    postsolve_ray(x_red, y_red) a ray; when unbounded, unbounded_ray() is the
+    primal ray presolve found."""
 
     def __init__(self, lp):
         from . import generators as G
@@ -202,9 +206,9 @@ class Presolved:
             _d(a["c"]), _d(a["cl"]), _d(a["cu"]), _d(a["rmin"]), _d(a["rmax"]),
             float(getattr(lp, "obj_const", 0.0)), C.byref(h), C.byref(oc)))
         self.outcome = {0: "reduced", 3: "infeasible", 4: "unbounded"}[oc.value]
-        self.h = h if oc.value == 0 else None
+        self.h = h if oc.value in (0, 4) else None
         self.lp, self.counts = None, None
-        if self.h is None:
+        if oc.value != 0:
             return
         m, n, nnz = C.c_int(), C.c_int(), C.c_int64()
         k = C.c_double()
@@ -229,6 +233,18 @@ class Presolved:
         x, y = np.zeros(self.n0), np.zeros(self.m0)
         _check(lib().igaos_pdhg_postsolve(self.h, _d(xr), _d(yr), _d(x), _d(y)))
         return x, y
+
+    def postsolve_ray(self, x_red, y_red):
+        f = lambda a: np.ascontiguousarray(a, np.float64)
+        xr, yr = f(x_red), f(y_red)
+        x, y = np.zeros(self.n0), np.zeros(self.m0)
+        _check(lib().igaos_pdhg_postsolve_ray(self.h, _d(xr), _d(yr), _d(x), _d(y)))
+        return x, y
+
+    def unbounded_ray(self):
+        x = np.zeros(self.n0)
+        _check(lib().igaos_pdhg_presolved_ray(self.h, _d(x)))
+        return x
 
     def close(self):
         if getattr(self, "h", None):

@@ -122,9 +122,35 @@ void transpose_host(int m, int n, const int* ap, const int* ai, const double* ax
             ++next[j];
         }
 }
+constexpr const char* kNotReduced = "presolve found the LP unbounded: only its ray is available";
 constexpr const char* kPresolvedInspect =
     "inspection entry points see the engine's LP, which a presolved handle does not share "
     "with its caller";
+
+// A ray (xr, yr) of the ORIGINAL LP checked with the certificate test: true
+// and the normalised ray in x / y (whichever are non-NULL; the other part 0)
+// when it is a ray of the expected kind (1 dual, 2 primal).
+bool original_ray(const igaos_pdhg_problem* p, const double* xr, const double* yr, int kind,
+                  double* x, double* y) {
+    const igx::Presolved& R = *p->pre;
+    const igx::HostLP& L = p->orig;
+    const int m0 = R.m0, n0 = R.n0;
+    std::vector<double> ax(m0, 0.0), aty(n0, 0.0), xn(n0, 0.0), yn(m0, 0.0);
+    for (int j = 0; j < n0; ++j)
+        for (int q = R.cp0[j]; q < R.cp0[j + 1]; ++q) {
+            ax[R.ci0[q]] += R.acx0[q] * xr[j];
+            aty[j] += R.acx0[q] * yr[R.ci0[q]];
+        }
+    const int got = igx::ray_certificate(m0, n0, xr, ax.data(), yr, aty.data(), L.c.data(),
+                                         L.cl.data(), L.cu.data(), L.rmin.data(), L.rmax.data(),
+                                         xn.data(), yn.data());
+    if (got != kind) return false;
+    if (kind == 1) std::fill(xn.begin(), xn.end(), 0.0);
+    else std::fill(yn.begin(), yn.end(), 0.0);
+    if (x) std::memcpy(x, xn.data(), sizeof(double) * n0);
+    if (y) std::memcpy(y, yn.data(), sizeof(double) * m0);
+    return true;
+}
 
 // igaos_pdhg_solve of a handle made with pdhg_presolve: the engine solves the
 // reduced LP, postsolve maps the pair back, and the metrics are taken again
@@ -144,9 +170,13 @@ int solve_presolved(igaos_pdhg_problem* p, const igaos_pdhg_options& o, igaos_pd
                       p->pre_outcome == igx::kPresolveInfeasible
                           ? "presolve: the LP is infeasible"
                           : "presolve: a column's cost runs to an infinite bound (unbounded if "
-                            "feasible)");
+                            "feasible); x = its ray");
         if (x) std::fill(x, x + n0, 0.0);
         if (y) std::fill(y, y + m0, 0.0);
+        std::vector<double> xr(n0), zy(m0, 0.0);
+        if (x && igx::unbounded_ray(R, xr.data()) && original_ray(p, xr.data(), zy.data(), 2, x, y))
+            return ok();
+        if (x) std::fill(x, x + n0, 0.0);
         return ok();
     }
     std::vector<double> xr(R.n), yr(R.m), xo(n0), yo(m0), ax(m0), d(n0);
@@ -186,16 +216,27 @@ int solve_presolved(igaos_pdhg_problem* p, const igaos_pdhg_options& o, igaos_pd
         res->launches += rr.launches;
         if (round == 0) res->setup_time_ms += rr.setup_time_ms;
         if (rr.status == IGAOS_STATUS_INFEASIBLE || rr.status == IGAOS_STATUS_UNBOUNDED) {
-            // a ray of the reduced LP, on the surviving rows and columns
+            // a ray of the reduced LP: mapped to the original and checked there
             res->status = rr.status;
             res->objective = rr.objective;
             res->pinf = rr.pinf;
             res->dinf = rr.dinf;
             res->rel_gap = rr.rel_gap;
             res->prow = rr.prow;
-            std::snprintf(res->message, sizeof(res->message), "%.120s (reduced LP)", rr.message);
-            for (int j = 0; j < n0 && x; ++j) x[j] = R.col_red[j] >= 0 ? xr[R.col_red[j]] : 0.0;
-            for (int i = 0; i < m0 && y; ++i) y[i] = R.row_red[i] >= 0 ? yr[R.row_red[i]] : 0.0;
+            const bool dual = rr.status == IGAOS_STATUS_INFEASIBLE;
+            if (dual) std::fill(xr.begin(), xr.end(), 0.0);
+            else std::fill(yr.begin(), yr.end(), 0.0);
+            igx::postsolve_ray(R, xr.data(), yr.data(), xo.data(), yo.data());
+            if (original_ray(p, xo.data(), yo.data(), dual ? 1 : 2, x, y)) {
+                std::snprintf(res->message, sizeof(res->message), "%.159s", rr.message);
+            } else {
+                std::snprintf(res->message, sizeof(res->message),
+                              "%.120s (reduced LP's ray)", rr.message);
+                for (int j = 0; j < n0 && x; ++j)
+                    x[j] = R.col_red[j] >= 0 ? xr[R.col_red[j]] : 0.0;
+                for (int i = 0; i < m0 && y; ++i)
+                    y[i] = R.row_red[i] >= 0 ? yr[R.row_red[i]] : 0.0;
+            }
             return ok();
         }
         igx::postsolve(R, xr.data(), yr.data(), xo.data(), yo.data());
@@ -566,13 +607,14 @@ int igaos_pdhg_presolve(int m, int n, int64_t nnz, const int* ap, const int* ai,
         validate(m, n, nnz, ap, ai, ax, nullptr, nullptr, nullptr, c, cl, cu, rmin, rmax);
         std::unique_ptr<igaos_pdhg_presolved> h(new igaos_pdhg_presolved);
         *outcome = igx::presolve(m, n, ap, ai, ax, c, cl, cu, rmin, rmax, obj_const, h->p);
-        if (*outcome == igx::kPresolveReduced) *out = h.release();
+        if (*outcome != igx::kPresolveInfeasible) *out = h.release();
     });
 }
 
 int igaos_pdhg_presolved_info(const igaos_pdhg_presolved* p, int* m, int* n, int64_t* nnz,
                               double* obj_const, int64_t* counts6) {
     if (!p) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (p->p.unbounded_col >= 0) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
     const igx::Presolved& R = p->p;
     if (m) *m = R.m;
     if (n) *n = R.n;
@@ -592,6 +634,7 @@ int igaos_pdhg_presolved_lp(const igaos_pdhg_presolved* p, int* ap, int* ai, dou
     if (!p || !ap || !c || !cl || !cu || !rmin || !rmax ||
         (!p->p.ai.empty() && (!ai || !ax)))
         return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (p->p.unbounded_col >= 0) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
     const igx::Presolved& R = p->p;
     std::copy(R.ap.begin(), R.ap.end(), ap);
     std::copy(R.ai.begin(), R.ai.end(), ai);
@@ -608,7 +651,24 @@ int igaos_pdhg_postsolve(const igaos_pdhg_presolved* p, const double* x_red,
                          const double* y_red, double* x, double* y) {
     if (!p || !x || !y || (p->p.n > 0 && !x_red) || (p->p.m > 0 && !y_red))
         return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (p->p.unbounded_col >= 0) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
     igx::postsolve(p->p, x_red, y_red, x, y);
+    return ok();
+}
+
+int igaos_pdhg_postsolve_ray(const igaos_pdhg_presolved* p, const double* x_red,
+                             const double* y_red, double* x, double* y) {
+    if (!p || !x || !y || (p->p.n > 0 && !x_red) || (p->p.m > 0 && !y_red))
+        return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (p->p.unbounded_col >= 0) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
+    igx::postsolve_ray(p->p, x_red, y_red, x, y);
+    return ok();
+}
+
+int igaos_pdhg_presolved_ray(const igaos_pdhg_presolved* p, double* x) {
+    if (!p || !x) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    if (!igx::unbounded_ray(p->p, x))
+        return fail(IGAOS_PDHG_ERR_INVALID, "presolve did not find the LP unbounded");
     return ok();
 }
 

@@ -110,10 +110,18 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
     auto empty_col = [&](int j) -> bool {  // false: the cost runs to an infinite bound
         double v;
         if (cost[j] > 0.0) {
-            if (!std::isfinite(lo[j])) return false;
+            if (!std::isfinite(lo[j])) {
+                P.unbounded_col = j;
+                P.ray_step = -1.0;
+                return false;
+            }
             v = lo[j];
         } else if (cost[j] < 0.0) {
-            if (!std::isfinite(hi[j])) return false;
+            if (!std::isfinite(hi[j])) {
+                P.unbounded_col = j;
+                P.ray_step = 1.0;
+                return false;
+            }
             v = hi[j];
         } else {
             v = std::isfinite(lo[j]) ? lo[j] : (std::isfinite(hi[j]) ? hi[j] : 0.0);
@@ -200,11 +208,21 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
             const double a = ca[p];
             const double q = cost[j] / a;
             double t;
+            // unbounded: x_j alone moves the row's activity toward its open
+            // side, and the cost falls (c_j dx_j = q a dx_j < 0)
             if (q > 0.0) {
-                if (!std::isfinite(rlo[i])) return kPresolveUnbounded;
+                if (!std::isfinite(rlo[i])) {
+                    P.unbounded_col = j;
+                    P.ray_step = -1.0 / a;
+                    return kPresolveUnbounded;
+                }
                 t = rlo[i];
             } else if (q < 0.0) {
-                if (!std::isfinite(rhi[i])) return kPresolveUnbounded;
+                if (!std::isfinite(rhi[i])) {
+                    P.unbounded_col = j;
+                    P.ray_step = 1.0 / a;
+                    return kPresolveUnbounded;
+                }
                 t = rhi[i];
             } else {
                 t = std::isfinite(rlo[i]) ? rlo[i] : (std::isfinite(rhi[i]) ? rhi[i] : 0.0);
@@ -278,34 +296,63 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
     return kPresolveReduced;
 }
 
-void postsolve(const Presolved& P, const double* x_red, const double* y_red, double* x, double* y) {
+namespace {
+
+// ray: costs, fixed values and row targets taken as 0
+void undo(const Presolved& P, const double* x_red, const double* y_red, double* x, double* y,
+          bool ray) {
     for (int j = 0; j < P.n0; ++j) x[j] = P.col_red[j] >= 0 ? x_red[P.col_red[j]] : 0.0;
     for (int i = 0; i < P.m0; ++i) y[i] = P.row_red[i] >= 0 ? y_red[P.row_red[i]] : 0.0;
     // the duals of substituted rows do not depend on the solution; every
     // reduced cost below needs them
-    for (const PresolveRec& r : P.recs)
-        if (r.kind == PresolveRec::FreeSingleton) y[r.i] = -r.q;
+    if (!ray)
+        for (const PresolveRec& r : P.recs)
+            if (r.kind == PresolveRec::FreeSingleton) y[r.i] = -r.q;
     for (auto it = P.recs.rbegin(); it != P.recs.rend(); ++it) {
         const PresolveRec& r = *it;
         switch (r.kind) {
             case PresolveRec::FixVal:
-                x[r.j] = r.val;
+                x[r.j] = ray ? 0.0 : r.val;
                 break;
             case PresolveRec::FreeSingleton: {
                 double s = 0.0;
                 for (int64_t t = r.t0; t < r.t1; ++t) s += P.term_a[t] * x[P.term_col[t]];
-                x[r.j] = (r.val - s) / r.a;
+                x[r.j] = ((ray ? 0.0 : r.val) - s) / r.a;
                 break;
             }
             case PresolveRec::SingletonRow: {
                 // rows removed before this one still hold y = 0 here
-                double d = P.c0[r.j];
+                double d = ray ? 0.0 : P.c0[r.j];
                 for (int p = P.cp0[r.j]; p < P.cp0[r.j + 1]; ++p) d += P.acx0[p] * y[P.ci0[p]];
                 if ((r.lo_from_row && d > 0.0) || (r.hi_from_row && d < 0.0)) y[r.i] = -d / r.a;
                 break;
             }
         }
     }
+}
+
+}  // namespace
+
+void postsolve(const Presolved& P, const double* x_red, const double* y_red, double* x, double* y) {
+    undo(P, x_red, y_red, x, y, false);
+}
+
+void postsolve_ray(const Presolved& P, const double* x_red, const double* y_red, double* x,
+                   double* y) {
+    undo(P, x_red, y_red, x, y, true);
+}
+
+bool unbounded_ray(const Presolved& P, double* x) {
+    if (P.unbounded_col < 0) return false;
+    std::fill(x, x + P.n0, 0.0);
+    x[P.unbounded_col] = P.ray_step;
+    for (auto it = P.recs.rbegin(); it != P.recs.rend(); ++it) {
+        if (it->kind != PresolveRec::FreeSingleton) continue;
+        double s = 0.0;
+        for (int64_t t = it->t0; t < it->t1; ++t) s += P.term_a[t] * x[P.term_col[t]];
+        x[it->j] = -s / it->a;
+    }
+    return true;
 }
 
 }  // namespace igx

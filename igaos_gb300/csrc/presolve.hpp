@@ -66,6 +66,10 @@ struct Presolved {
     std::vector<double> term_a;
     PresolveCounts counts;
     int rounds = 0;
+    // kPresolveUnbounded: the column whose cost runs to an infinite bound and
+    // its primal ray (x_j moves by ray_step per unit; every other entry 0)
+    int unbounded_col = -1;
+    double ray_step = 0.0;
 };
 
 // Reduces the LP (CSR, original units). Returns kPresolveReduced (out holds
@@ -78,5 +82,18 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
 // x (n0) and y (m0) of the original LP from x_red (n) and y_red (m) of the
 // reduced one: records undone in reverse order.
 void postsolve(const Presolved& p, const double* x_red, const double* y_red, double* x, double* y);
+
+// The same map for a ray of the reduced LP (a direction: zero costs, fixed
+// values and row targets): a dual ray y_red maps to a dual ray of the
+// original (reduced costs pressing on a bound a singleton row set move into
+// that row), a primal ray x_red to a primal ray (substituted columns follow
+// their rows).
+void postsolve_ray(const Presolved& p, const double* x_red, const double* y_red, double* x,
+                   double* y);
+
+// kPresolveUnbounded: x (n0) = the primal ray of the column presolve found
+// running to an infinite bound, with the columns substituted before it
+// following their rows. False for the other outcomes.
+bool unbounded_ray(const Presolved& p, double* x);
 
 }  // namespace igx

@@ -90,11 +90,13 @@ typedef struct igaos_pdhg_options {
      * redundant rows; fixed, empty and free-singleton columns; see
      * igaos_pdhg_presolve) and map the answer back with exact duals; the
      * result's metrics are then those of the ORIGINAL LP. The handle's
-     * inspection entry points (get_scaling ... spmv) see the reduced LP, and
-     * a ray of detect_infeasibility is the reduced LP's, on the surviving
-     * rows and columns (0 elsewhere). 0 (default): off, as the reference
-     * engine, which ignores `presolve`. Read by igaos_pdhg_create. Added in
-     * ABI 3. */
+     * inspection entry points (get_scaling ... spmv) refuse it. A ray of
+     * detect_infeasibility, and the primal ray of a column presolve finds
+     * unbounded, are mapped to the original LP and checked there with
+     * igaos_pdhg_ray_certificate's test; if that check fails, x / y hold
+     * the reduced LP's ray on the surviving rows and columns (0 elsewhere).
+     * 0 (default): off, as the reference engine, which ignores `presolve`.
+     * Read by igaos_pdhg_create. Added in ABI 3. */
     int pdhg_presolve;
     /* 1: after the solve, run igaos_pdhg_crossover on the host from the
      * answer's x (LPs with m <= 2048); when it ends at an optimal basis whose
@@ -159,9 +161,10 @@ int igaos_pdhg_ray_certificate(int m, int n, const double* x, const double* ax, 
  * every reduction has an exact dual postsolve: an optimal pair of the reduced
  * LP maps to an optimal pair of the original.
  * igaos_pdhg_presolve reduces the CSR LP; *outcome = 0 (reduced: *out holds
- * it, possibly with no rows and no columns), IGAOS_STATUS_INFEASIBLE or
- * IGAOS_STATUS_UNBOUNDED (a column whose cost runs to an infinite bound: the
- * LP is unbounded if it is feasible), with *out = NULL. */
+ * it, possibly with no rows and no columns), IGAOS_STATUS_INFEASIBLE (*out =
+ * NULL) or IGAOS_STATUS_UNBOUNDED (a column whose cost runs to an infinite
+ * bound: the LP is unbounded if it is feasible; *out holds the handle for
+ * igaos_pdhg_presolved_ray, and the other accessors refuse it). */
 typedef struct igaos_pdhg_presolved igaos_pdhg_presolved;
 
 int igaos_pdhg_presolve(int m, int n, int64_t nnz, const int* ap, const int* ai,
@@ -182,6 +185,18 @@ int igaos_pdhg_presolved_lp(const igaos_pdhg_presolved* p, int* ap, int* ai, dou
 /* x (original n) and y (original m) from x_red, y_red of the reduced LP. */
 int igaos_pdhg_postsolve(const igaos_pdhg_presolved* p, const double* x_red,
                          const double* y_red, double* x, double* y);
+
+/* The same map for a ray of the reduced LP (costs, fixed values and row
+ * targets taken as 0): a dual ray y_red (reduced costs pressing on a bound a
+ * singleton row set move into that row) and a primal ray x_red map to rays
+ * of the original LP. */
+int igaos_pdhg_postsolve_ray(const igaos_pdhg_presolved* p, const double* x_red,
+                             const double* y_red, double* x, double* y);
+
+/* Outcome IGAOS_STATUS_UNBOUNDED: x (original n) = the primal ray of the
+ * column whose cost runs to an infinite bound (columns substituted before it
+ * follow their rows). */
+int igaos_pdhg_presolved_ray(const igaos_pdhg_presolved* p, double* x);
 
 void igaos_pdhg_presolved_destroy(igaos_pdhg_presolved* p);
 

@@ -93,3 +93,22 @@ def test_cli_and_pybind_pdhg_presolve(native, tmp_path):
     s = ig.solve(str(p), time_limit=60.0, tolerance=1e-6, engine="pdhg", pdhg_presolve=True)
     assert s.status == "near-optimal" and len(s.x) == lp.n and len(s.y) == lp.m
     assert abs(s.objective - ref) <= 1e-5 * max(1.0, abs(ref))
+
+
+def test_rays_come_back_as_certificates_of_the_original(native):
+    """detect_infeasibility with presolve. x1 + x2 >= 3 with x1 <= 1 and
+    x2 <= 1 as singleton rows, x free: the engine's dual ray of the reduced
+    LP, mapped back, is a certificate of the ORIGINAL LP. And presolve's own
+    unbounded column comes back as a primal ray with its substituted column
+    following."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 0, 1, 2], [0, 1, 0, 1], [1.0] * 4, [1.0, 1.0], [-INF, -INF], [INF, INF],
+              [3.0, -INF, -INF], [INF, 1.0, 1.0])
+    r = capi.solve_lp(lp, tolerance=1e-6, time_limit=60.0, detect_infeasibility=1,
+                      pdhg_presolve=1)
+    assert r["status_name"] == "infeasible" and "reduced LP" not in r["message"], r["message"]
+    assert capi.ray_certificate(lp, np.zeros(2), r["y"])[0] == 1
+    lp = tiny([0, 0, 0], [0, 1, 2], [1.0, 1.0, 1.0], [0.0, 1.0, 0.5], [0.0, -INF, 0.0],
+              [5.0, INF, INF], [2.0], [2.0])
+    r = capi.solve_lp(lp, tolerance=1e-6, pdhg_presolve=1)
+    assert r["status_name"] == "unbounded" and np.array_equal(r["x"], [0.0, -1.0, 1.0]), r

@@ -210,3 +210,39 @@ def test_netlib_postsolve(native, orc, name):
     assert_optimal(metrics(orc, lp, x, y), 1e-8)
     _, _, f = highs(lp)
     assert abs(lp.c @ x - f) <= 1e-8 * (1.0 + abs(f))
+
+
+def test_dual_ray_of_the_reduced_lp_maps_to_a_certificate(native):
+    """x1 + x2 >= 3 with x1 <= 1 and x2 <= 1 as singleton rows, x free: the
+    reduced LP (one row, bounds from the singleton rows) has the dual ray
+    y = -1. Scattered with zeros it is no certificate of the original (its
+    columns are free); mapped like a postsolve with zero costs, the reduced
+    costs move into the singleton rows: y = (-1, 1, 1)."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 0, 1, 2], [0, 1, 0, 1], [1.0] * 4, [1.0, 1.0], [-INF, -INF], [INF, INF],
+              [3.0, -INF, -INF], [INF, 1.0, 1.0])
+    P = capi.Presolved(lp)
+    assert (P.lp.m, P.counts["singleton_rows"]) == (1, 2)
+    yr = np.array([-1.0])
+    assert capi.ray_certificate(P.lp, np.zeros(P.lp.n), yr)[0] == 1
+    assert capi.ray_certificate(lp, np.zeros(2), np.array([-1.0, 0.0, 0.0]))[0] == 0
+    x, y = P.postsolve_ray(np.zeros(P.lp.n), yr)
+    assert np.array_equal(y, [-1.0, 1.0, 1.0]) and not x.any()
+    assert capi.ray_certificate(lp, x, y)[0] == 1
+
+
+def test_unbounded_column_ray_follows_substitutions(native):
+    """min x2 + 0.5 x4 s.t. x1 + x2 + x4 = 2, x1 in [0, 5], x2 free, x4 >= 0:
+    substituting the free singleton x2 leaves x4 empty at cost -0.5 with no
+    upper bound. Its ray x4 = +1 needs x2 = -1 to keep the row: the ray
+    presolve returns is a primal certificate of the original LP."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 0, 0], [0, 1, 2], [1.0, 1.0, 1.0], [0.0, 1.0, 0.5], [0.0, -INF, 0.0],
+              [5.0, INF, INF], [2.0], [2.0])
+    P = capi.Presolved(lp)
+    assert P.outcome == "unbounded" and P.lp is None
+    r = P.unbounded_ray()
+    assert np.array_equal(r, [0.0, -1.0, 1.0])
+    assert capi.ray_certificate(lp, r, np.zeros(1))[0] == 2
+    with pytest.raises(capi.EngineError, match="only its ray"):
+        P.postsolve(np.zeros(1), np.zeros(1))
