@@ -118,3 +118,53 @@ def test_presolve_entries_reject_bad_arguments(native):
     assert native.igaos_pdhg_presolved_info(None, None, None, None, None, None) == capi.ERR_INVALID
     assert native.igaos_pdhg_postsolve(None, None, None, None, None) == capi.ERR_INVALID
     native.igaos_pdhg_presolved_destroy(None)  # no-op
+
+
+C_PROGRAM = r"""
+#include <math.h>
+#include <stdio.h>
+#include "igaos_pdhg.h"
+int main(void) {
+    /* min x1 + 2 x2 + 3 x3 s.t. x1 + x2 + x3 = 4, x1, x2 in [0, 10], x3 free */
+    const int ap[2] = {0, 3}, ai[3] = {0, 1, 2};
+    const double ax[3] = {1, 1, 1}, c[3] = {1, 2, 3}, cl[3] = {0, 0, -INFINITY};
+    const double cu[3] = {10, 10, INFINITY}, rmin[1] = {4}, rmax[1] = {4};
+    igaos_pdhg_presolved* ps = NULL;
+    int outcome = -1, m = -1, n = -1;
+    int64_t nnz = -1, counts[6];
+    double k = 0.0, x[3], y[1], x0[3] = {0, 0, 0}, xv[3], yv[1];
+    signed char basis[4];
+    igaos_pdhg_crossover_info info;
+    if (igaos_pdhg_presolve(1, 3, 3, ap, ai, ax, c, cl, cu, rmin, rmax, 0.0, &ps, &outcome))
+        return 1;
+    igaos_pdhg_presolved_info(ps, &m, &n, &nnz, &k, counts);
+    igaos_pdhg_postsolve(ps, NULL, NULL, x, y);
+    igaos_pdhg_presolved_destroy(ps);
+    if (igaos_pdhg_crossover(1, 3, 3, ap, ai, ax, c, cl, cu, rmin, rmax, x0, xv, yv, basis,
+                             &info))
+        return 2;
+    printf("%d %d %d %g | %g %g %g %g | %d %g %g %g %g\n", outcome, m, n, k, x[0], x[1], x[2],
+           y[0], info.status, xv[0], xv[1], xv[2], yv[0]);
+    return 0;
+}
+"""
+
+
+def test_c_program_calls_the_host_entries(native, tmp_path):
+    """The header is plain C99 and the library links into a C program, which
+    presolves, postsolves and crosses over an LP with no device: the binding
+    a cgo / FFI user writes."""
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("gcc not present")
+    src = tmp_path / "t.c"
+    src.write_text(C_PROGRAM)
+    pkg = os.path.join(ROOT, "igaos_gb300")
+    exe = tmp_path / "t"
+    subprocess.run(["gcc", "-std=c99", "-Wall", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    str(src), "-L", pkg, "-ligaos_pdhg", f"-Wl,-rpath,{pkg}", "-lm", "-o",
+                    str(exe)], check=True, capture_output=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()
+    assert out == ["0", "0", "0", "-18", "|", "10", "10", "-16", "-3", "|", "0", "10", "10",
+                   "-16", "-3"], out
