@@ -131,6 +131,24 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
         return true;
     };
 
+    // a singleton column j of row i whose bounds the row implies: with the
+    // other columns inside their bounds and the activity inside [rlo, rhi],
+    // x_j = (activity - others) / a already lies in [lo_j, hi_j], so those
+    // bounds never bind and j is substituted like a free column
+    auto implied_free = [&](int i, int j, double a) -> bool {
+        double L = 0.0, U = 0.0;  // activity range of the row's other columns
+        for (int s = rp[i]; s < rp[i + 1]; ++s) {
+            const int k = rj[s];
+            if (k == j || !calive[k]) continue;
+            const double b = ra[s];
+            L += b > 0.0 ? b * lo[k] : b * hi[k];
+            U += b > 0.0 ? b * hi[k] : b * lo[k];
+        }
+        const double ilo = a > 0.0 ? (rlo[i] - U) / a : (rhi[i] - L) / a;
+        const double ihi = a > 0.0 ? (rhi[i] - L) / a : (rlo[i] - U) / a;
+        return ilo >= lo[j] && ihi <= hi[j];
+    };
+
     bool changed = true;
     while (changed && P.rounds < kMaxRounds) {
         changed = false;
@@ -201,11 +219,12 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
                 changed = true;
                 continue;
             }
-            if (ccnt[j] != 1 || lo[j] != -kInf || hi[j] != kInf) continue;
+            if (ccnt[j] != 1) continue;
             int p = cp[j];
             while (!ralive[ci[p]]) ++p;
             const int i = ci[p];
             const double a = ca[p];
+            if ((lo[j] != -kInf || hi[j] != kInf) && !implied_free(i, j, a)) continue;
             const double q = cost[j] / a;
             double t;
             // unbounded: x_j alone moves the row's activity toward its open

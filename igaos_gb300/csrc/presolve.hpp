@@ -17,8 +17,10 @@
 //   fixed column     -- l_j = u_j: removed, row bounds shifted by a x_j;
 //   empty column     -- x_j at the bound its cost prefers (the LP is
 //                       unbounded or infeasible when that bound is infinite);
-//   free singleton   -- a free column j met by one row i: x_j takes up the
-//                       row (activity pinned at the row bound the sign of
+//   free singleton   -- a column j met by one row i, free or with bounds
+//                       the row implies (the other columns' bounds and the
+//                       row's keep x_j inside them): x_j takes up the row
+//                       (activity pinned at the row bound the sign of
 //                       q = c_j / a selects), the row's other columns pay
 //                       c_k -= q a_ik, and y_i = -q.
 // Exact zeros of A are dropped. Rounds repeat until nothing changes.

@@ -79,7 +79,7 @@ def test_presolved_handle_refuses_inspection(native):
 
 def test_cli_and_pybind_pdhg_presolve(native, tmp_path):
     import igaos_gb300 as ig
-    lp = G.presolvable_lp(60, 150, 250, 2)
+    lp = G.presolvable_lp(60, 150, 250, 1)
     _, _, ref = highs(lp)
     p = tmp_path / "p.mps"
     write_mps(lp, p)

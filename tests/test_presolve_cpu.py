@@ -246,3 +246,45 @@ def test_unbounded_column_ray_follows_substitutions(native):
     assert capi.ray_certificate(lp, r, np.zeros(1))[0] == 2
     with pytest.raises(capi.EngineError, match="only its ray"):
         P.postsolve(np.zeros(1), np.zeros(1))
+
+
+def test_implied_free_singleton_is_substituted(native, orc):
+    """min x1 + 2 x2 - s s.t. x1 + x2 + s = 5, x1, x2 in [0, 2], s in [0, 10]:
+    the row keeps s in [1, 5], inside its bounds, so s is substituted like a
+    free column (y = 1; x1, x2 then cost 2 and 3 and go to 0, s = 5)."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 0, 0], [0, 1, 2], [1.0, 1.0, 1.0], [1.0, 2.0, -1.0], [0.0, 0.0, 0.0],
+              [2.0, 2.0, 10.0], [5.0], [5.0])
+    P = capi.Presolved(lp)
+    assert P.counts["free_singletons"] == 1 and (P.lp.m, P.lp.n) == (0, 0)
+    x, y = P.postsolve(np.zeros(0), np.zeros(0))
+    assert np.array_equal(x, [0.0, 0.0, 5.0]) and np.array_equal(y, [1.0])
+    assert_optimal(metrics(orc, lp, x, y), 0.0)
+    # with s in [0, 4] the row could need s = 5: the bounds bind, no substitution
+    lp = tiny([0, 0, 0], [0, 1, 2], [1.0, 1.0, 1.0], [1.0, 2.0, -1.0], [0.0, 0.0, 0.0],
+              [2.0, 2.0, 4.0], [5.0], [5.0])
+    assert capi.Presolved(lp).counts["free_singletons"] == 0
+
+
+def test_implied_free_singletons_keep_postsolve_exact(native, orc):
+    """Seeded LPs with a slack-like singleton column of wide bounds in every
+    row: those of the equality rows qualify (a <= row leaves the column's
+    lower side open), and the postsolved HiGHS pair stays optimal."""
+    from igaos_gb300 import capi
+    for seed in range(4):
+        base = G.random_lp(40, 90, 150, seed)
+        rows = np.repeat(np.arange(base.m), np.diff(base.ap))
+        m, n = base.m, base.n + base.m
+        lp = G.from_triplets(m, n, np.concatenate([rows, np.arange(m)]),
+                             np.concatenate([base.ai, base.n + np.arange(m)]),
+                             np.concatenate([base.ax, np.ones(m)]),
+                             np.concatenate([base.c, np.full(m, 0.1)]),
+                             np.concatenate([base.cl, np.full(m, -1e4)]),
+                             np.concatenate([base.cu, np.full(m, 1e4)]), base.rmin, base.rmax)
+        P = capi.Presolved(lp)
+        assert P.counts["free_singletons"] >= m // 4
+        xr, yr, _ = highs(P.lp)
+        x, y = P.postsolve(xr, yr)
+        assert_optimal(metrics(orc, lp, x, y), 1e-9)
+        _, _, f = highs(lp)
+        assert abs(lp.c @ x - f) <= 1e-8 * (1.0 + abs(f))
