@@ -130,7 +130,7 @@ def lib():
         L.igaos_pdhg_presolved_lp.argtypes = [C.c_void_p, _ip, _ip] + [_dp] * 6
         L.igaos_pdhg_postsolve.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
         L.igaos_pdhg_postsolve_ray.argtypes = [C.c_void_p, _dp, _dp, _dp, _dp]
-        L.igaos_pdhg_presolved_ray.argtypes = [C.c_void_p, _dp]
+        L.igaos_pdhg_presolved_ray.argtypes = [C.c_void_p, _dp, _dp]
         L.igaos_pdhg_presolved_destroy.argtypes = [C.c_void_p]
         L.igaos_pdhg_presolved_destroy.restype = None
         L.igaos_pdhg_crossover.argtypes = [
@@ -192,8 +192,8 @@ class Presolved:
     GPU needed): `outcome` is "reduced", "infeasible" or "unbounded"; when
     reduced, `lp` is the reduced LP (an LPData), `counts` the reductions made,
     postsolve(x_red, y_red) maps a pair of the reduced LP back and
-    postsolve_ray(x_red, y_red) a ray; when unbounded, unbounded_ray() is the
-    primal ray presolve found."""
+    postsolve_ray(x_red, y_red) a ray; when infeasible or unbounded, ray() is
+    the (x, y) certificate presolve found in the original LP."""
 
     def __init__(self, lp):
         from . import generators as G
@@ -206,7 +206,7 @@ class Presolved:
             _d(a["c"]), _d(a["cl"]), _d(a["cu"]), _d(a["rmin"]), _d(a["rmax"]),
             float(getattr(lp, "obj_const", 0.0)), C.byref(h), C.byref(oc)))
         self.outcome = {0: "reduced", 3: "infeasible", 4: "unbounded"}[oc.value]
-        self.h = h if oc.value in (0, 4) else None
+        self.h = h
         self.lp, self.counts = None, None
         if oc.value != 0:
             return
@@ -241,10 +241,10 @@ class Presolved:
         _check(lib().igaos_pdhg_postsolve_ray(self.h, _d(xr), _d(yr), _d(x), _d(y)))
         return x, y
 
-    def unbounded_ray(self):
-        x = np.zeros(self.n0)
-        _check(lib().igaos_pdhg_presolved_ray(self.h, _d(x)))
-        return x
+    def ray(self):
+        x, y = np.zeros(self.n0), np.zeros(self.m0)
+        _check(lib().igaos_pdhg_presolved_ray(self.h, _d(x), _d(y)))
+        return x, y
 
     def close(self):
         if getattr(self, "h", None):

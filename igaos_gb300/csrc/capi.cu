@@ -122,7 +122,12 @@ void transpose_host(int m, int n, const int* ap, const int* ai, const double* ax
             ++next[j];
         }
 }
-constexpr const char* kNotReduced = "presolve found the LP unbounded: only its ray is available";
+constexpr const char* kNotReduced =
+    "presolve found the LP infeasible or unbounded: only its ray is available";
+bool reduced(const igaos_pdhg_presolved* p) {
+    return p->p.unbounded_col < 0 && p->p.infeasible_row < 0 && !p->p.row_red.empty();
+}
+
 constexpr const char* kPresolvedInspect =
     "inspection entry points see the engine's LP, which a presolved handle does not share "
     "with its caller";
@@ -164,19 +169,23 @@ int solve_presolved(igaos_pdhg_problem* p, const igaos_pdhg_options& o, igaos_pd
     std::memset(res, 0, sizeof(*res));
     res->setup_time_ms = p->presolve_ms;
     if (p->pre_outcome != igx::kPresolveReduced) {
+        const bool inf = p->pre_outcome == igx::kPresolveInfeasible;
         res->status = p->pre_outcome;
         res->objective = res->pinf = res->dinf = res->rel_gap = res->prow = std::nan("");
         std::snprintf(res->message, sizeof(res->message), "%s",
-                      p->pre_outcome == igx::kPresolveInfeasible
-                          ? "presolve: the LP is infeasible"
+                      inf ? "presolve: the LP is infeasible; y = a dual ray"
                           : "presolve: a column's cost runs to an infinite bound (unbounded if "
                             "feasible); x = its ray");
-        if (x) std::fill(x, x + n0, 0.0);
-        if (y) std::fill(y, y + m0, 0.0);
-        std::vector<double> xr(n0), zy(m0, 0.0);
-        if (x && igx::unbounded_ray(R, xr.data()) && original_ray(p, xr.data(), zy.data(), 2, x, y))
-            return ok();
-        if (x) std::fill(x, x + n0, 0.0);
+        std::vector<double> xr(n0, 0.0), yr(m0, 0.0);
+        const bool have = inf ? igx::infeasible_ray(R, yr.data()) : igx::unbounded_ray(R, xr.data());
+        if (!have || !original_ray(p, xr.data(), yr.data(), inf ? 1 : 2, x, y)) {
+            if (x) std::fill(x, x + n0, 0.0);
+            if (y) std::fill(y, y + m0, 0.0);
+            std::snprintf(res->message, sizeof(res->message), "%s",
+                          inf ? "presolve: the LP is infeasible"
+                              : "presolve: a column's cost runs to an infinite bound "
+                                "(unbounded if feasible)");
+        }
         return ok();
     }
     std::vector<double> xr(R.n), yr(R.m), xo(n0), yo(m0), ax(m0), d(n0);
@@ -607,14 +616,14 @@ int igaos_pdhg_presolve(int m, int n, int64_t nnz, const int* ap, const int* ai,
         validate(m, n, nnz, ap, ai, ax, nullptr, nullptr, nullptr, c, cl, cu, rmin, rmax);
         std::unique_ptr<igaos_pdhg_presolved> h(new igaos_pdhg_presolved);
         *outcome = igx::presolve(m, n, ap, ai, ax, c, cl, cu, rmin, rmax, obj_const, h->p);
-        if (*outcome != igx::kPresolveInfeasible) *out = h.release();
+        *out = h.release();
     });
 }
 
 int igaos_pdhg_presolved_info(const igaos_pdhg_presolved* p, int* m, int* n, int64_t* nnz,
                               double* obj_const, int64_t* counts6) {
     if (!p) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
-    if (p->p.unbounded_col >= 0) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
+    if (!reduced(p)) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
     const igx::Presolved& R = p->p;
     if (m) *m = R.m;
     if (n) *n = R.n;
@@ -634,7 +643,7 @@ int igaos_pdhg_presolved_lp(const igaos_pdhg_presolved* p, int* ap, int* ai, dou
     if (!p || !ap || !c || !cl || !cu || !rmin || !rmax ||
         (!p->p.ai.empty() && (!ai || !ax)))
         return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
-    if (p->p.unbounded_col >= 0) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
+    if (!reduced(p)) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
     const igx::Presolved& R = p->p;
     std::copy(R.ap.begin(), R.ap.end(), ap);
     std::copy(R.ai.begin(), R.ai.end(), ai);
@@ -651,7 +660,7 @@ int igaos_pdhg_postsolve(const igaos_pdhg_presolved* p, const double* x_red,
                          const double* y_red, double* x, double* y) {
     if (!p || !x || !y || (p->p.n > 0 && !x_red) || (p->p.m > 0 && !y_red))
         return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
-    if (p->p.unbounded_col >= 0) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
+    if (!reduced(p)) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
     igx::postsolve(p->p, x_red, y_red, x, y);
     return ok();
 }
@@ -660,15 +669,17 @@ int igaos_pdhg_postsolve_ray(const igaos_pdhg_presolved* p, const double* x_red,
                              const double* y_red, double* x, double* y) {
     if (!p || !x || !y || (p->p.n > 0 && !x_red) || (p->p.m > 0 && !y_red))
         return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
-    if (p->p.unbounded_col >= 0) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
+    if (!reduced(p)) return fail(IGAOS_PDHG_ERR_INVALID, kNotReduced);
     igx::postsolve_ray(p->p, x_red, y_red, x, y);
     return ok();
 }
 
-int igaos_pdhg_presolved_ray(const igaos_pdhg_presolved* p, double* x) {
-    if (!p || !x) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
-    if (!igx::unbounded_ray(p->p, x))
-        return fail(IGAOS_PDHG_ERR_INVALID, "presolve did not find the LP unbounded");
+int igaos_pdhg_presolved_ray(const igaos_pdhg_presolved* p, double* x, double* y) {
+    if (!p || !x || !y) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
+    std::fill(x, x + p->p.n0, 0.0);
+    std::fill(y, y + p->p.m0, 0.0);
+    if (!igx::unbounded_ray(p->p, x) && !igx::infeasible_ray(p->p, y))
+        return fail(IGAOS_PDHG_ERR_INVALID, "presolve found no ray for this LP");
     return ok();
 }
 

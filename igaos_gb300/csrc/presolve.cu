@@ -11,6 +11,7 @@ namespace {
 constexpr double kInf = std::numeric_limits<double>::infinity();
 constexpr int kMaxRounds = 64;
 constexpr double kFeasTol = 1e-9;
+constexpr double kForceTol = 1e-12;  // activity bound this close to a row bound: forcing
 
 inline double mag(double b) { return std::isfinite(b) ? std::fabs(b) : 0.0; }
 
@@ -100,9 +101,18 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
         P.recs.push_back(r);
         kill_col(j);
     };
+    auto infeasible = [&](int i, int side) {
+        P.infeasible_row = i;
+        P.infeasible_side = side;
+        return kPresolveInfeasible;
+    };
     auto empty_row = [&](int i) -> bool {  // false: 0 is outside the row's range
         const double t = kFeasTol * rscale[i];
-        if (rlo[i] > t || rhi[i] < -t) return false;
+        if (rlo[i] > t || rhi[i] < -t) {
+            P.infeasible_row = i;
+            P.infeasible_side = rlo[i] > t ? -1 : 1;
+            return false;
+        }
         kill_row(i);
         ++K.empty_rows;
         return true;
@@ -171,8 +181,10 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
                 const bool tl = blo > lo[j], th = bhi < hi[j];
                 double nlo = tl ? blo : lo[j], nhi = th ? bhi : hi[j];
                 if (nlo > nhi) {
+                    // the row's own range is not empty: it crosses a column
+                    // bound from the side it tightened
                     if (nlo - nhi > kFeasTol * (1.0 + mag(nlo) + mag(nhi)))
-                        return kPresolveInfeasible;
+                        return infeasible(i, tl ? (a > 0.0 ? -1 : 1) : (a > 0.0 ? 1 : -1));
                     if (tl && !th) nlo = nhi;  // crossing by rounding only
                     else nhi = nlo;
                 }
@@ -204,7 +216,35 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
                 kill_row(i);
                 ++K.redundant_rows;
                 changed = true;
+                continue;
             }
+            const double tf = kFeasTol * rscale[i], te = kForceTol * rscale[i];
+            if (L > rhi[i] + tf) return infeasible(i, 1);
+            if (U < rlo[i] - tf) return infeasible(i, -1);
+            const int side = std::fabs(L - rhi[i]) <= te ? 1 : (std::fabs(U - rlo[i]) <= te ? -1 : 0);
+            if (side == 0) continue;
+            // forcing: least activity at rmax (side +1) or largest at rmin (-1)
+            PresolveRec r;
+            r.kind = PresolveRec::Forcing;
+            r.i = i;
+            r.side = side;
+            r.t0 = (int64_t)P.term_col.size();
+            for (int q = rp[i]; q < rp[i + 1]; ++q) {
+                const int k = rj[q];
+                if (!calive[k]) continue;
+                const double b = ra[q];
+                const bool upper = (b > 0.0) == (side < 0);  // the bound that achieves it
+                P.term_col.push_back(k);
+                P.term_a.push_back(b);
+                P.term_at.push_back(lo[k] == hi[k] ? 2 : (upper ? 1 : 0));
+                if (upper) lo[k] = hi[k];
+                else hi[k] = lo[k];
+            }
+            r.t1 = (int64_t)P.term_col.size();
+            P.recs.push_back(r);
+            kill_row(i);
+            ++K.redundant_rows;
+            changed = true;
         }
         for (int j = 0; j < n; ++j) {
             if (!calive[j]) continue;
@@ -259,6 +299,7 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
                 if (k == j || !calive[k]) continue;
                 P.term_col.push_back(k);
                 P.term_a.push_back(ra[s]);
+                P.term_at.push_back(2);
                 cost[k] -= q * ra[s];
             }
             r.t1 = (int64_t)P.term_col.size();
@@ -317,11 +358,9 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
 
 namespace {
 
-// ray: costs, fixed values and row targets taken as 0
-void undo(const Presolved& P, const double* x_red, const double* y_red, double* x, double* y,
-          bool ray) {
-    for (int j = 0; j < P.n0; ++j) x[j] = P.col_red[j] >= 0 ? x_red[P.col_red[j]] : 0.0;
-    for (int i = 0; i < P.m0; ++i) y[i] = P.row_red[i] >= 0 ? y_red[P.row_red[i]] : 0.0;
+// x, y: the reduced LP's pair scattered to the original (0 elsewhere). ray:
+// costs, fixed values and row targets taken as 0
+void undo(const Presolved& P, double* x, double* y, bool ray) {
     // the duals of substituted rows do not depend on the solution; every
     // reduced cost below needs them
     if (!ray)
@@ -346,19 +385,53 @@ void undo(const Presolved& P, const double* x_red, const double* y_red, double* 
                 if ((r.lo_from_row && d > 0.0) || (r.hi_from_row && d < 0.0)) y[r.i] = -d / r.a;
                 break;
             }
+            case PresolveRec::Forcing: {
+                // y_i on the row's active side (>= 0 at rmax, <= 0 at rmin)
+                // with d_k + a_ik y_i >= 0 for columns at lower, <= 0 at upper
+                double ylo = r.side > 0 ? 0.0 : -kInf, yhi = r.side > 0 ? kInf : 0.0;
+                for (int64_t t = r.t0; t < r.t1; ++t) {
+                    if (P.term_at[t] == 2) continue;
+                    const int k = P.term_col[t];
+                    const double a = P.term_a[t];
+                    double d = ray ? 0.0 : P.c0[k];
+                    for (int p = P.cp0[k]; p < P.cp0[k + 1]; ++p) d += P.acx0[p] * y[P.ci0[p]];
+                    const double v = -d / a;
+                    if ((P.term_at[t] == 0) == (a > 0.0)) ylo = std::max(ylo, v);
+                    else yhi = std::min(yhi, v);
+                }
+                // nearest 0 inside [ylo, yhi]; rounding can cross them: midpoint
+                y[r.i] = ylo > yhi ? 0.5 * (ylo + yhi) : std::min(std::max(0.0, ylo), yhi);
+                break;
+            }
         }
     }
+}
+
+void scatter(const Presolved& P, const double* x_red, const double* y_red, double* x, double* y) {
+    for (int j = 0; j < P.n0; ++j) x[j] = P.col_red[j] >= 0 ? x_red[P.col_red[j]] : 0.0;
+    for (int i = 0; i < P.m0; ++i) y[i] = P.row_red[i] >= 0 ? y_red[P.row_red[i]] : 0.0;
 }
 
 }  // namespace
 
 void postsolve(const Presolved& P, const double* x_red, const double* y_red, double* x, double* y) {
-    undo(P, x_red, y_red, x, y, false);
+    scatter(P, x_red, y_red, x, y);
+    undo(P, x, y, false);
 }
 
 void postsolve_ray(const Presolved& P, const double* x_red, const double* y_red, double* x,
                    double* y) {
-    undo(P, x_red, y_red, x, y, true);
+    scatter(P, x_red, y_red, x, y);
+    undo(P, x, y, true);
+}
+
+bool infeasible_ray(const Presolved& P, double* y) {
+    if (P.infeasible_row < 0) return false;
+    std::vector<double> x(P.n0, 0.0);
+    std::fill(y, y + P.m0, 0.0);
+    y[P.infeasible_row] = P.infeasible_side;
+    undo(P, x.data(), y, true);
+    return true;
 }
 
 bool unbounded_ray(const Presolved& P, double* x) {

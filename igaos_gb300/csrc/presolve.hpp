@@ -14,6 +14,12 @@
 //                       into y_i = -d_j / a;
 //   redundant row    -- its activity range over the column bounds lies in
 //                       [rmin, rmax]; y_i = 0;
+//   forcing row      -- its least activity is rmax (or its largest rmin):
+//                       every column goes to the bound that achieves it and
+//                       the row is removed; postsolve takes y_i nearest 0 on
+//                       the row's active side with every such column's
+//                       reduced cost of the sign its bound needs (an
+//                       activity range beyond the row's bounds: infeasible);
 //   fixed column     -- l_j = u_j: removed, row bounds shifted by a x_j;
 //   empty column     -- x_j at the bound its cost prefers (the LP is
 //                       unbounded or infeasible when that bound is infinite);
@@ -32,6 +38,7 @@
 namespace igx {
 
 struct PresolveCounts {
+    // forcing rows are counted with the redundant ones
     int64_t empty_rows = 0, singleton_rows = 0, redundant_rows = 0;
     int64_t fixed_cols = 0, empty_cols = 0, free_singletons = 0;
 };
@@ -42,13 +49,15 @@ constexpr int kPresolveInfeasible = 3;
 constexpr int kPresolveUnbounded = 4;  // dual infeasible: unbounded if feasible
 
 struct PresolveRec {
-    enum Kind : unsigned char { FixVal = 0, SingletonRow = 1, FreeSingleton = 2 } kind;
+    enum Kind : unsigned char { FixVal = 0, SingletonRow = 1, FreeSingleton = 2, Forcing = 3 } kind;
     bool lo_from_row = false, hi_from_row = false;  // SingletonRow
     int i = -1, j = -1;
     double a = 0.0;    // SingletonRow / FreeSingleton: the entry a_ij
     double val = 0.0;  // FixVal: x_j; FreeSingleton: the row target t
     double q = 0.0;    // FreeSingleton: c_j / a_ij (y_i = -q)
-    int64_t t0 = 0, t1 = 0;  // FreeSingleton: its row's other entries in terms
+    int64_t t0 = 0, t1 = 0;  // FreeSingleton: its row's other entries in terms;
+                             // Forcing: the row's columns (term_at: the bound)
+    int side = 0;            // Forcing: +1 activity pinned at rmax, -1 at rmin
 };
 
 struct Presolved {
@@ -66,12 +75,17 @@ struct Presolved {
     std::vector<PresolveRec> recs;
     std::vector<int> term_col;
     std::vector<double> term_a;
+    std::vector<signed char> term_at;  // Forcing: 0 lower, 1 upper, 2 fixed
     PresolveCounts counts;
     int rounds = 0;
     // kPresolveUnbounded: the column whose cost runs to an infinite bound and
     // its primal ray (x_j moves by ray_step per unit; every other entry 0)
     int unbounded_col = -1;
     double ray_step = 0.0;
+    // kPresolveInfeasible: the row whose bounds the activity cannot meet and
+    // the sign of its dual ray (+1 at rmax, -1 at rmin); -1 when none
+    int infeasible_row = -1;
+    int infeasible_side = 0;
 };
 
 // Reduces the LP (CSR, original units). Returns kPresolveReduced (out holds
@@ -97,5 +111,10 @@ void postsolve_ray(const Presolved& p, const double* x_red, const double* y_red,
 // running to an infinite bound, with the columns substituted before it
 // following their rows. False for the other outcomes.
 bool unbounded_ray(const Presolved& p, double* x);
+
+// kPresolveInfeasible: y (m0) = a dual ray of the original LP: the row that
+// proved it (y_i = +-1 in the LP presolve had reduced so far), mapped back
+// through the records made before it. False when no row proved it.
+bool infeasible_ray(const Presolved& p, double* y);
 
 }  // namespace igx

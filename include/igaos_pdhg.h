@@ -91,8 +91,8 @@ typedef struct igaos_pdhg_options {
      * igaos_pdhg_presolve) and map the answer back with exact duals; the
      * result's metrics are then those of the ORIGINAL LP. The handle's
      * inspection entry points (get_scaling ... spmv) refuse it. A ray of
-     * detect_infeasibility, and the primal ray of a column presolve finds
-     * unbounded, are mapped to the original LP and checked there with
+     * detect_infeasibility, and the ray behind a presolve outcome of
+     * infeasible / unbounded, are mapped to the original LP and checked there with
      * igaos_pdhg_ray_certificate's test; if that check fails, x / y hold
      * the reduced LP's ray on the surviving rows and columns (0 elsewhere).
      * 0 (default): off, as the reference engine, which ignores `presolve`.
@@ -161,10 +161,11 @@ int igaos_pdhg_ray_certificate(int m, int n, const double* x, const double* ax, 
  * every reduction has an exact dual postsolve: an optimal pair of the reduced
  * LP maps to an optimal pair of the original.
  * igaos_pdhg_presolve reduces the CSR LP; *outcome = 0 (reduced: *out holds
- * it, possibly with no rows and no columns), IGAOS_STATUS_INFEASIBLE (*out =
- * NULL) or IGAOS_STATUS_UNBOUNDED (a column whose cost runs to an infinite
- * bound: the LP is unbounded if it is feasible; *out holds the handle for
- * igaos_pdhg_presolved_ray, and the other accessors refuse it). */
+ * it, possibly with no rows and no columns), IGAOS_STATUS_INFEASIBLE (a row
+ * whose bounds its activity cannot meet) or IGAOS_STATUS_UNBOUNDED (a column
+ * whose cost runs to an infinite bound: the LP is unbounded if it is
+ * feasible). *out is a handle for every outcome; for the last two only
+ * igaos_pdhg_presolved_ray and _destroy accept it. */
 typedef struct igaos_pdhg_presolved igaos_pdhg_presolved;
 
 int igaos_pdhg_presolve(int m, int n, int64_t nnz, const int* ap, const int* ai,
@@ -193,10 +194,14 @@ int igaos_pdhg_postsolve(const igaos_pdhg_presolved* p, const double* x_red,
 int igaos_pdhg_postsolve_ray(const igaos_pdhg_presolved* p, const double* x_red,
                              const double* y_red, double* x, double* y);
 
-/* Outcome IGAOS_STATUS_UNBOUNDED: x (original n) = the primal ray of the
- * column whose cost runs to an infinite bound (columns substituted before it
- * follow their rows). */
-int igaos_pdhg_presolved_ray(const igaos_pdhg_presolved* p, double* x);
+/* The certificate behind presolve's outcome, in the original LP: for
+ * IGAOS_STATUS_UNBOUNDED, x (n) = the primal ray of the column whose cost
+ * runs to an infinite bound (columns substituted before it follow their
+ * rows); for IGAOS_STATUS_INFEASIBLE, y (m) = a dual ray: +-1 on the row
+ * that proved it, mapped back through the reductions made before (e.g. onto
+ * the singleton rows that set the bounds it crossed). The other vector is
+ * 0. IGAOS_PDHG_ERR_INVALID when presolve found no such ray. */
+int igaos_pdhg_presolved_ray(const igaos_pdhg_presolved* p, double* x, double* y);
 
 void igaos_pdhg_presolved_destroy(igaos_pdhg_presolved* p);
 

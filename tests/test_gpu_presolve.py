@@ -96,9 +96,10 @@ def test_cli_and_pybind_pdhg_presolve(native, tmp_path):
 
 
 def test_rays_come_back_as_certificates_of_the_original(native):
-    """detect_infeasibility with presolve. x1 + x2 >= 3 with x1 <= 1 and
-    x2 <= 1 as singleton rows, x free: the engine's dual ray of the reduced
-    LP, mapped back, is a certificate of the ORIGINAL LP. And presolve's own
+    """Rays through a presolved solve. x1 + x2 >= 3 with x1 <= 1 and x2 <= 1
+    as singleton rows, x free: presolve proves it infeasible (largest
+    activity 2 < 3) and the answer's y is that row's ray mapped back through
+    the singleton rows, a certificate of the ORIGINAL LP. And presolve's own
     unbounded column comes back as a primal ray with its substituted column
     following."""
     from igaos_gb300 import capi

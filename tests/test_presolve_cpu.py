@@ -184,7 +184,8 @@ def test_no_reduction_leaves_the_lp_unchanged(native):
 
 
 NETLIB = ["afiro", "kb2", "sc50a", "adlittle", "bandm", "grow22", "boeing1", "degen2",
-          "etamacro", "forplan"]
+          "etamacro", "forplan", "agg", "brandy", "e226", "scfxm1", "capri", "stocfor1",
+          "scagr25", "sc205", "share2b", "israel"]
 
 
 @pytest.mark.skipif(reference_dir() is None, reason="reference tree not present")
@@ -213,22 +214,48 @@ def test_netlib_postsolve(native, orc, name):
 
 
 def test_dual_ray_of_the_reduced_lp_maps_to_a_certificate(native):
-    """x1 + x2 >= 3 with x1 <= 1 and x2 <= 1 as singleton rows, x free: the
-    reduced LP (one row, bounds from the singleton rows) has the dual ray
-    y = -1. Scattered with zeros it is no certificate of the original (its
-    columns are free); mapped like a postsolve with zero costs, the reduced
-    costs move into the singleton rows: y = (-1, 1, 1)."""
+    """x1 + x2 >= 3 and x1 - x2 >= 2 (together x1 >= 2.5) with x1 <= 2 as a
+    singleton row, x free: no single row shows the infeasibility, so the
+    reduced LP keeps both rows, with x1 <= 2 as a column bound, and has the
+    dual ray y = (-1, -1). Scattered with zeros it is no certificate of the
+    original (x1 is free there); mapped like a postsolve with zero costs,
+    the reduced cost -2 of x1 moves into the singleton row: y = (-1, -1, 2)."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 0, 1, 1, 2], [0, 1, 0, 1, 0], [1.0, 1.0, 1.0, -1.0, 1.0], [1.0, 1.0],
+              [-INF, -INF], [INF, INF], [3.0, 2.0, -INF], [INF, INF, 2.0])
+    P = capi.Presolved(lp)
+    assert P.outcome == "reduced" and (P.lp.m, P.lp.n) == (2, 2)
+    assert P.counts["singleton_rows"] == 1 and P.lp.cu[0] == 2.0
+    yr = np.array([-1.0, -1.0])
+    assert capi.ray_certificate(P.lp, np.zeros(2), yr)[0] == 1
+    assert capi.ray_certificate(lp, np.zeros(2), np.array([-1.0, -1.0, 0.0]))[0] == 0
+    x, y = P.postsolve_ray(np.zeros(2), yr)
+    assert np.array_equal(y, [-1.0, -1.0, 2.0]) and not x.any()
+    assert capi.ray_certificate(lp, x, y)[0] == 1
+
+
+def test_presolve_infeasibility_comes_with_a_dual_ray(native):
+    """x1 + x2 >= 3 with x1 <= 1 and x2 <= 1 as singleton rows, x free: after
+    the singleton rows, the row's largest activity is 2 < 3 and presolve
+    stops. Its ray, -1 on that row mapped back through the singleton rows,
+    is y = (-1, 1, 1): a certificate of the original LP. The same for an
+    empty row outside its bounds and for crossing singleton rows."""
     from igaos_gb300 import capi
     lp = tiny([0, 0, 1, 2], [0, 1, 0, 1], [1.0] * 4, [1.0, 1.0], [-INF, -INF], [INF, INF],
               [3.0, -INF, -INF], [INF, 1.0, 1.0])
     P = capi.Presolved(lp)
-    assert (P.lp.m, P.counts["singleton_rows"]) == (1, 2)
-    yr = np.array([-1.0])
-    assert capi.ray_certificate(P.lp, np.zeros(P.lp.n), yr)[0] == 1
-    assert capi.ray_certificate(lp, np.zeros(2), np.array([-1.0, 0.0, 0.0]))[0] == 0
-    x, y = P.postsolve_ray(np.zeros(P.lp.n), yr)
+    assert P.outcome == "infeasible"
+    x, y = P.ray()
     assert np.array_equal(y, [-1.0, 1.0, 1.0]) and not x.any()
     assert capi.ray_certificate(lp, x, y)[0] == 1
+    for lp in (tiny([0, 1], [0, 0], [1.0, 1.0], [1.0], [0.0], [10.0], [-INF, 3.0], [1.0, INF]),
+               tiny([0, 1], [0, 0], [2.0, -1.0], [1.0], [-INF], [INF], [-INF, -INF], [2.0, -3.0]),
+               tiny([0, 1], [0, 1], [1.0, 1.0], [1.0, 1.0], [2.0, 0.0], [2.0, 1.0],
+                    [0.0, -INF], [1.0, INF])):
+        P = capi.Presolved(lp)
+        assert P.outcome == "infeasible"
+        x, y = P.ray()
+        assert capi.ray_certificate(lp, x, y)[0] == 1, (lp.rmin, lp.rmax, y)
 
 
 def test_unbounded_column_ray_follows_substitutions(native):
@@ -241,8 +268,8 @@ def test_unbounded_column_ray_follows_substitutions(native):
               [5.0, INF, INF], [2.0], [2.0])
     P = capi.Presolved(lp)
     assert P.outcome == "unbounded" and P.lp is None
-    r = P.unbounded_ray()
-    assert np.array_equal(r, [0.0, -1.0, 1.0])
+    r, yr = P.ray()
+    assert np.array_equal(r, [0.0, -1.0, 1.0]) and not yr.any()
     assert capi.ray_certificate(lp, r, np.zeros(1))[0] == 2
     with pytest.raises(capi.EngineError, match="only its ray"):
         P.postsolve(np.zeros(1), np.zeros(1))
