@@ -139,3 +139,21 @@ def test_netlib(native, orc, name):
         assert_optimal(metrics(orc, lp, x, y), 1e-9)
         assert abs(lp.c @ x - f) <= 1e-9 * (1.0 + abs(f))
         assert (basis == 2).sum() == lp.m
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_presolve_then_crossover(native, orc, seed):
+    """The chain of a solve with pdhg_presolve and crossover: an optimal pair
+    of the reduced LP (HiGHS), postsolved, then crossover on the ORIGINAL LP
+    from that x: an optimal vertex with HiGHS's objective."""
+    from igaos_gb300 import capi
+    lp = G.presolvable_lp(60, 150, 250, seed)
+    P = capi.Presolved(lp)
+    xr, yr, _ = highs(P.lp)
+    x0, _ = P.postsolve(xr, yr)
+    x, y, basis, info = capi.crossover(lp, x0)
+    _, _, f = highs(lp)
+    assert info["status"] == "optimal"
+    assert_optimal(metrics(orc, lp, x, y), 1e-9)
+    assert abs(lp.c @ x - f) <= 1e-9 * (1.0 + abs(f))
+    assert_vertex(lp, x, basis, info)
