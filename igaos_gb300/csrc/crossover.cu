@@ -22,6 +22,7 @@ constexpr double kPivTol = 1e-7;     // pivots at least this large are preferred
 constexpr double kSnap = 1e-9;       // start values this close to a bound sit on it
 constexpr int kDegenerateRun = 100;  // degenerate steps before Bland's rule
 constexpr double kDevexReset = 1e6;  // reference weights reset above this
+constexpr double kCrashRoom = 1e-6;  // a row this close to a bound (relative) is active
 
 // Host threads for the dense O(m^2) loops: run(count, f) calls f(begin, end)
 // on contiguous slices of [0, count), one per thread, the caller's included.
@@ -348,6 +349,7 @@ private:
         ++I_.pivots;
     }
     bool push(int j, bool& pi_valid, bool zero_cost_only);
+    bool crash();
     int simplex(int64_t& it, int64_t cap, bool& pi_valid);
     int n_rejected_ = 0;
     bool retried_ = false;
@@ -426,7 +428,7 @@ int Simplex::ratio(int q, int dir, double& theta, bool& leave_upper) {
     return best;
 }
 
-// Moves structural j (nonbasic, inside its bounds) to a bound or into the
+// Moves variable j (nonbasic, inside its bounds) to a bound or into the
 // basis along the edge its phase-2 reduced cost does not worsen; either way
 // (nearer bound first) when that cost is within tolerance of 0. With
 // zero_cost_only, j moves only in that last case. False: j did not move.
@@ -568,6 +570,53 @@ bool Simplex::clean() const {
     return q < 0;
 }
 
+// Crash basis: the structurals strictly inside their bounds (most interior
+// first) enter at once in place of the slacks of the rows with the least
+// room, whose activities go to their nearest bound; one factorisation
+// (dependent columns go back out) replaces that many one-pivot pushes, and
+// the basic values follow from the nonbasic ones. False: the slack basis
+// stays (no structural inside its bounds, or the factorisation failed).
+bool Simplex::crash() {
+    std::vector<std::pair<double, int>> inner, room;
+    for (int j = 0; j < n_; ++j) {
+        if (st[j] != kSuperbasic) continue;
+        const double d = std::min(val[j] - lb[j], ub[j] - val[j]);  // inf when free
+        inner.push_back({-d / (1.0 + std::fabs(val[j])), j});
+    }
+    for (int i = 0; i < m_; ++i) {
+        const int s = n_ + i;
+        const double d = std::min(val[s] - lb[s], ub[s] - val[s]);
+        const double r = d / (1.0 + std::fabs(val[s]));
+        if (r <= kCrashRoom) room.push_back({r, i});  // only rows at a bound swap their slack
+    }
+    const int out = (int)std::min(inner.size(), room.size());
+    if (out == 0) return false;
+    std::sort(inner.begin(), inner.end());
+    std::sort(room.begin(), room.end());  // least room first: these slacks leave
+    const std::vector<double> val0 = val;
+    const std::vector<signed char> st0 = st;
+    for (int t = 0; t < out; ++t) {
+        const int i = room[t].second, s = n_ + i, j = inner[t].second;
+        const bool up = ub[s] - val[s] < val[s] - lb[s];
+        val[s] = up ? ub[s] : lb[s];
+        st[s] = up ? kAtUpper : kAtLower;
+        head_[i] = j;
+        st[j] = kBasic;
+    }
+    if (refactor()) {
+        recompute_basics();
+        return true;
+    }
+    val = val0;  // back to the slack basis
+    st = st0;
+    std::fill(binv_.begin(), binv_.end(), 0.0);
+    for (int i = 0; i < m_; ++i) {
+        head_[i] = n_ + i;
+        binv_[(size_t)i * m_ + i] = -1.0;
+    }
+    return false;
+}
+
 int Simplex::run(const double* x0) {
     val.assign(nt_, 0.0);
     st.assign(nt_, kBasic);
@@ -600,8 +649,9 @@ int Simplex::run(const double* x0) {
     for (int j = 0; j < n_; ++j)
         for (int p = cp_[j]; p < cp_[j + 1]; ++p) val[n_ + ci_[p]] += acx_[p] * val[j];
     bool pi_valid = true;  // slack costs are 0, so pi = 0
+    if (crash()) pi_valid = false;
 
-    for (int j = 0; j < n_; ++j) {  // 1. primal push
+    for (int j = 0; j < nt_; ++j) {  // 1. primal push
         if (st[j] != kSuperbasic) continue;
         push(j, pi_valid, false);
         if (!maybe_refactor(pi_valid)) return kXoSingular;
@@ -615,7 +665,7 @@ int Simplex::run(const double* x0) {
         if (rc != kXoOptimal) return rc;
         clear_rejected();
         retried_ = false;
-        for (int j = 0; j < n_; ++j) {
+        for (int j = 0; j < nt_; ++j) {  // a basis repair can leave a slack inside
             if (st[j] != kSuperbasic) continue;
             push(j, pi_valid, true);
             if (!maybe_refactor(pi_valid)) return kXoSingular;
@@ -626,7 +676,7 @@ int Simplex::run(const double* x0) {
         pi_valid = true;
         if (clean() || pass == 3) break;
     }
-    for (int j = 0; j < n_; ++j) I_.superbasic_left += st[j] == kSuperbasic;
+    for (int j = 0; j < nt_; ++j) I_.superbasic_left += st[j] == kSuperbasic;
     return kXoOptimal;
 }
 

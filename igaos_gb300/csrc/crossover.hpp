@@ -6,17 +6,19 @@
 // The LP is put in the bounded form [A  -I] (x, s) = 0 with x in [cl, cu]
 // and the row activities s in [rmin, rmax]. From the slack basis (B = -I)
 // and the start point x0 (values within 1e-9 of a bound are snapped to it),
-//   1. primal push: every structural strictly inside its bounds moves along
+//   1. crash: the structurals strictly inside their bounds enter the basis
+//      at once in place of the slacks of rows at a bound (1e-6, relative);
+//   2. primal push: every variable still inside its bounds moves along
 //      the edge its phase-2 reduced cost improves (either way when that cost
 //      is 0) until it reaches a bound or a basic variable blocks, which
-//      then leaves the basis (the structural enters);
-//   2. a composite primal simplex: phase 1 minimises the sum of the basic
+//      then leaves the basis (the moving variable enters);
+//   3. a composite primal simplex: phase 1 minimises the sum of the basic
 //      variables' bound violations (a violated basic blocks at the bound it
 //      reaches), phase 2 the cost; Devex pricing, a two-pass (Harris)
 //      ratio test preferring large pivots, Bland's rule after 100
 //      consecutive degenerate steps; repeated until a fresh factorisation's
 //      values and duals are clean;
-//   3. a last push of structurals still inside their bounds (reduced cost
+//   4. a last push of variables still inside their bounds (reduced cost
 //      0, so the objective does not move).
 // B^-1 is kept explicitly (dense, m x m; product-form updates, Gauss-Jordan
 // refactorisation with partial pivoting every m pivots), so the host work
@@ -45,7 +47,7 @@ struct CrossoverInfo {
     int status = kXoOptimal;
     int64_t pushes = 0, pivots = 0, bound_flips = 0, phase1_iters = 0, refactors = 0;
     int64_t basis_repairs = 0;    // dependent basis columns swapped for slacks
-    int64_t superbasic_left = 0;  // structurals not at a bound and not basic
+    int64_t superbasic_left = 0;  // variables not at a bound and not basic
     double time_ms = 0.0;
 };
 

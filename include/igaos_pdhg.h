@@ -222,7 +222,7 @@ typedef struct igaos_pdhg_crossover_info {
     int pad;
     int64_t pushes, pivots, bound_flips, phase1_iterations, refactorizations;
     int64_t basis_repairs;    /* dependent basis columns swapped for row slacks */
-    int64_t superbasic_left;  /* structurals left inside their bounds, nonbasic */
+    int64_t superbasic_left;  /* variables left inside their bounds, nonbasic */
     double time_ms;
 } igaos_pdhg_crossover_info;
 
