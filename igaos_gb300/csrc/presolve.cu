@@ -3,7 +3,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <limits>
+#include <unordered_map>
 
 namespace igx {
 namespace {
@@ -12,6 +14,7 @@ constexpr double kInf = std::numeric_limits<double>::infinity();
 constexpr int kMaxRounds = 64;
 constexpr double kFeasTol = 1e-9;
 constexpr double kForceTol = 1e-12;  // activity bound this close to a row bound: forcing
+constexpr double kParallelTol = 1e-12;  // rows proportional to within this (relative)
 
 inline double mag(double b) { return std::isfinite(b) ? std::fabs(b) : 0.0; }
 
@@ -159,6 +162,87 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
         return ilo >= lo[j] && ihi <= hi[j];
     };
 
+    // Parallel rows: rows with the same live columns and proportional values
+    // (grouped by a hash of the columns and the values over the first one),
+    // the later merged into the earlier.
+    std::vector<std::pair<int, double>> ea, eb;  // (column, value) of two rows
+    auto live = [&](int i, std::vector<std::pair<int, double>>& e) {
+        e.clear();
+        for (int q = rp[i]; q < rp[i + 1]; ++q)
+            if (calive[rj[q]]) e.push_back({rj[q], ra[q]});
+        std::sort(e.begin(), e.end());
+    };
+    auto parallel_rows = [&](bool& changed_out) -> int {
+        std::unordered_map<uint64_t, std::vector<int>> groups;
+        std::vector<uint64_t> hash(m, 0);
+        for (int i = 0; i < m; ++i) {
+            if (!ralive[i] || rcnt[i] < 2) continue;
+            live(i, ea);
+            uint64_t h = 1469598103934665603ull;
+            auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
+            for (const auto& e : ea) {
+                double r = e.second / ea[0].second;
+                r = std::round(r * 1e9) / 1e9;  // hash only; equality is checked below
+                uint64_t bits;
+                std::memcpy(&bits, &r, sizeof(bits));
+                mix((uint64_t)e.first);
+                mix(bits);
+            }
+            groups[h].push_back(i);
+            hash[i] = h;
+        }
+        // rows in index order, each against the earlier rows of its group
+        // (deterministic whatever the map's bucket order)
+        for (int i = 0; i < m; ++i) {
+            if (!ralive[i] || rcnt[i] < 2) continue;
+            const std::vector<int>& rows = groups[hash[i]];
+            if (rows.size() < 2 || rows[0] == i) continue;
+            live(i, ea);
+            {
+                for (size_t v = 0; v < rows.size() && rows[v] < i; ++v) {
+                    const int k = rows[v];  // candidate to keep
+                    if (!ralive[k] || !ralive[i]) continue;
+                    live(k, eb);
+                    if (ea.size() != eb.size()) continue;
+                    const double sr = ea[0].second / eb[0].second;
+                    bool same = true;
+                    for (size_t t = 0; t < ea.size() && same; ++t)
+                        same = ea[t].first == eb[t].first &&
+                               std::fabs(ea[t].second - sr * eb[t].second) <=
+                                   kParallelTol * std::fabs(ea[t].second);
+                    if (!same) continue;
+                    // row i's range in row k's units
+                    const double ilo = sr > 0.0 ? rlo[i] / sr : rhi[i] / sr;
+                    const double ihi = sr > 0.0 ? rhi[i] / sr : rlo[i] / sr;
+                    const bool tl = ilo > rlo[k], th = ihi < rhi[k];
+                    double nlo = tl ? ilo : rlo[k], nhi = th ? ihi : rhi[k];
+                    if (nlo > nhi) {
+                        if (nlo - nhi > kFeasTol * (1.0 + mag(nlo) + mag(nhi)))
+                            return kPresolveInfeasible;
+                        if (tl && !th) nlo = nhi;
+                        else nhi = nlo;
+                    }
+                    rlo[k] = nlo;
+                    rhi[k] = nhi;
+                    rscale[k] = std::max(rscale[k], rscale[i] / std::fabs(sr));
+                    PresolveRec r;
+                    r.kind = PresolveRec::ParallelRow;
+                    r.i = i;
+                    r.j = k;
+                    r.a = sr;
+                    r.lo_from_row = tl;
+                    r.hi_from_row = th;
+                    P.recs.push_back(r);
+                    kill_row(i);
+                    ++K.redundant_rows;
+                    changed_out = true;
+                    break;
+                }
+            }
+        }
+        return kPresolveReduced;
+    };
+
     bool changed = true;
     while (changed && P.rounds < kMaxRounds) {
         changed = false;
@@ -246,6 +330,7 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
             ++K.redundant_rows;
             changed = true;
         }
+        if (parallel_rows(changed) != kPresolveReduced) return kPresolveInfeasible;
         for (int j = 0; j < n; ++j) {
             if (!calive[j]) continue;
             if (lo[j] == hi[j]) {
@@ -383,6 +468,17 @@ void undo(const Presolved& P, double* x, double* y, bool ray) {
                 double d = ray ? 0.0 : P.c0[r.j];
                 for (int p = P.cp0[r.j]; p < P.cp0[r.j + 1]; ++p) d += P.acx0[p] * y[P.ci0[p]];
                 if ((r.lo_from_row && d > 0.0) || (r.hi_from_row && d < 0.0)) y[r.i] = -d / r.a;
+                break;
+            }
+            case PresolveRec::ParallelRow: {
+                // the kept row's dual moves to the removed one when it
+                // presses on a side that row set (a_i = s a_k: the same
+                // reduced costs)
+                const double yk = y[r.j];
+                if ((yk > 0.0 && r.hi_from_row) || (yk < 0.0 && r.lo_from_row)) {
+                    y[r.i] = yk / r.a;
+                    y[r.j] = 0.0;
+                }
                 break;
             }
             case PresolveRec::Forcing: {

@@ -14,6 +14,10 @@
 //                       into y_i = -d_j / a;
 //   redundant row    -- its activity range over the column bounds lies in
 //                       [rmin, rmax]; y_i = 0;
+//   parallel row     -- row i = s row k (same columns, values in ratio s):
+//                       row k keeps the intersection of both ranges and
+//                       row i goes; postsolve hands k's dual to i (y_i =
+//                       y_k / s, y_k = 0) when it presses on a side i set;
 //   forcing row      -- its least activity is rmax (or its largest rmin):
 //                       every column goes to the bound that achieves it and
 //                       the row is removed; postsolve takes y_i nearest 0 on
@@ -38,7 +42,7 @@
 namespace igx {
 
 struct PresolveCounts {
-    // forcing rows are counted with the redundant ones
+    // forcing and parallel rows are counted with the redundant ones
     int64_t empty_rows = 0, singleton_rows = 0, redundant_rows = 0;
     int64_t fixed_cols = 0, empty_cols = 0, free_singletons = 0;
 };
@@ -49,10 +53,15 @@ constexpr int kPresolveInfeasible = 3;
 constexpr int kPresolveUnbounded = 4;  // dual infeasible: unbounded if feasible
 
 struct PresolveRec {
-    enum Kind : unsigned char { FixVal = 0, SingletonRow = 1, FreeSingleton = 2, Forcing = 3 } kind;
-    bool lo_from_row = false, hi_from_row = false;  // SingletonRow
-    int i = -1, j = -1;
-    double a = 0.0;    // SingletonRow / FreeSingleton: the entry a_ij
+    enum Kind : unsigned char {
+        FixVal = 0, SingletonRow = 1, FreeSingleton = 2, Forcing = 3, ParallelRow = 4
+    } kind;
+    // SingletonRow: the sides of x_j's bounds the row set; ParallelRow: the
+    // sides of the kept row's bounds the removed row set
+    bool lo_from_row = false, hi_from_row = false;
+    int i = -1, j = -1;  // ParallelRow: i removed, j the row kept
+    double a = 0.0;    // SingletonRow / FreeSingleton: the entry a_ij; ParallelRow:
+                       // the ratio s of the rows (row i = s row j)
     double val = 0.0;  // FixVal: x_j; FreeSingleton: the row target t
     double q = 0.0;    // FreeSingleton: c_j / a_ij (y_i = -q)
     int64_t t0 = 0, t1 = 0;  // FreeSingleton: its row's other entries in terms;

@@ -315,3 +315,19 @@ def test_implied_free_singletons_keep_postsolve_exact(native, orc):
         assert_optimal(metrics(orc, lp, x, y), 1e-9)
         _, _, f = highs(lp)
         assert abs(lp.c @ x - f) <= 1e-8 * (1.0 + abs(f))
+
+
+def test_parallel_rows_merge_and_hand_over_the_dual(native, orc):
+    """min -x1 - x2 s.t. x1 + 2 x2 <= 4, 2 x1 + 4 x2 <= 6 (the same row at
+    ratio 2, tighter), -x1 - 2 x2 >= -5 (ratio -1, looser), x in [0, 2]: the
+    first row keeps x1 + 2 x2 <= 3 and the others go. At the optimum (2,
+    0.5) the binding side came from the second row, which gets the dual."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 0, 1, 1, 2, 2], [0, 1, 0, 1, 0, 1], [1.0, 2.0, 2.0, 4.0, -1.0, -2.0],
+              [-1.0, -1.0], [0.0, 0.0], [2.0, 2.0], [-INF, -INF, -5.0], [4.0, 6.0, INF])
+    P = capi.Presolved(lp)
+    assert P.counts["redundant_rows"] == 2 and P.lp.m == 1 and P.lp.rmax[0] == 3.0
+    xr, yr, _ = highs(P.lp)
+    x, y = P.postsolve(xr, yr)
+    assert np.allclose(x, [2.0, 0.5]) and y[0] == 0.0 and y[2] == 0.0 and y[1] > 0.0
+    assert_optimal(metrics(orc, lp, x, y), 1e-12)
