@@ -86,9 +86,10 @@ typedef struct igaos_pdhg_options {
      * restarts; the ray is returned in y / x (max-norm 1). 0 (default): off,
      * as the reference engine, which has no such test. Added in ABI 2. */
     int detect_infeasibility;
-    /* 1: reduce the LP on the host before the upload (empty, singleton and
-     * redundant rows; fixed, empty and free-singleton columns; see
-     * igaos_pdhg_presolve) and map the answer back with exact duals; the
+    /* 1: reduce the LP on the host before the upload (empty, singleton,
+     * redundant, forcing and parallel rows; fixed, empty and free or
+     * implied-free singleton columns; see igaos_pdhg_presolve) and map the
+     * answer back with exact duals; the
      * result's metrics are then those of the ORIGINAL LP. The handle's
      * inspection entry points (get_scaling ... spmv) refuse it. A ray of
      * detect_infeasibility, and the ray behind a presolve outcome of
@@ -174,8 +175,9 @@ int igaos_pdhg_presolve(int m, int n, int64_t nnz, const int* ap, const int* ai,
                         double obj_const, igaos_pdhg_presolved** out, int* outcome);
 
 /* Sizes and constant of the reduced LP; counts6 (may be NULL) = empty rows,
- * singleton rows, redundant rows, fixed columns, empty columns and free
- * singleton columns removed. */
+ * singleton rows, redundant rows (forcing and parallel ones included), fixed
+ * columns, empty columns and free or implied-free singleton columns
+ * removed. */
 int igaos_pdhg_presolved_info(const igaos_pdhg_presolved* p, int* m, int* n, int64_t* nnz,
                               double* obj_const, int64_t* counts6);
 
