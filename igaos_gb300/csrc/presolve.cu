@@ -26,23 +26,40 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
     P = Presolved();
     P.m0 = m;
     P.n0 = n;
-    // row-wise copy without exact zeros, and its column-wise counterpart
-    std::vector<int> rp(m + 1, 0);
-    for (int i = 0; i < m; ++i) {
-        int k = 0;
-        for (int p = ap[i]; p < ap[i + 1]; ++p) k += ax[p] != 0.0;
-        rp[i + 1] = rp[i] + k;
+    // row-wise copy with repeated (row, column) entries summed (the activity
+    // bounds below treat every entry as its own term) and exact zeros
+    // dropped, and its column-wise counterpart
+    std::vector<int> rp(m + 1, 0), rj;
+    std::vector<double> ra;
+    rj.reserve(ap[m]);
+    ra.reserve(ap[m]);
+    {
+        std::vector<int> at(n, -1);  // position of column j in the current row
+        for (int i = 0; i < m; ++i) {
+            const int start = (int)rj.size();
+            for (int p = ap[i]; p < ap[i + 1]; ++p) {
+                const int j = ai[p];
+                if (at[j] >= start) {
+                    ra[at[j]] += ax[p];
+                    continue;
+                }
+                at[j] = (int)rj.size();
+                rj.push_back(j);
+                ra.push_back(ax[p]);
+            }
+            int w = start;
+            for (int q = start; q < (int)rj.size(); ++q)
+                if (ra[q] != 0.0) {
+                    rj[w] = rj[q];
+                    ra[w] = ra[q];
+                    ++w;
+                }
+            rj.resize(w);
+            ra.resize(w);
+            rp[i + 1] = w;
+        }
     }
     const int64_t nz = rp[m];
-    std::vector<int> rj(nz);
-    std::vector<double> ra(nz);
-    for (int i = 0, w = 0; i < m; ++i)
-        for (int p = ap[i]; p < ap[i + 1]; ++p)
-            if (ax[p] != 0.0) {
-                rj[w] = ai[p];
-                ra[w] = ax[p];
-                ++w;
-            }
     std::vector<int>& cp = P.cp0;
     std::vector<int>& ci = P.ci0;
     std::vector<double>& ca = P.acx0;

@@ -331,3 +331,19 @@ def test_parallel_rows_merge_and_hand_over_the_dual(native, orc):
     x, y = P.postsolve(xr, yr)
     assert np.allclose(x, [2.0, 0.5]) and y[0] == 0.0 and y[2] == 0.0 and y[1] > 0.0
     assert_optimal(metrics(orc, lp, x, y), 1e-12)
+
+
+def test_repeated_entries_are_summed(native, orc):
+    """A column entered twice in a row (2 x1 and -1 x1: x1 in total) with
+    x2: x1 + x2 <= 0 on [0, 1]^2 forces both to 0. Were the entries taken
+    apart, the row's least activity would be 2*0 - 1*1 = -1 and nothing
+    forced; summed, the row forces, and the postsolved pair is optimal."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 0, 0, 1], [0, 0, 1, 1], [2.0, -1.0, 1.0, 1.0], [-1.0, -2.0], [0.0, 0.0],
+              [1.0, 1.0], [-INF, -INF], [0.0, 1.0])
+    P = capi.Presolved(lp)
+    assert P.outcome == "reduced" and P.counts["redundant_rows"] >= 1
+    xr, yr, _ = highs(P.lp) if P.lp.m else (np.zeros(P.lp.n), np.zeros(0), 0.0)
+    x, y = P.postsolve(xr, yr)
+    assert np.array_equal(x, [0.0, 0.0])
+    assert_optimal(metrics(orc, lp, x, y), 1e-12)
