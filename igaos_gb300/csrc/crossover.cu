@@ -233,8 +233,8 @@ private:
         for (int r = 0; r < m_; ++r) {
             const int j = head_[r];
             if (j >= n_) M[(size_t)(j - n_) * m_ + r] = -1.0;
-            else
-                for (int p = cp_[j]; p < cp_[j + 1]; ++p) M[(size_t)ci_[p] * m_ + r] = acx_[p];
+            else  // repeated (row, column) entries add up
+                for (int p = cp_[j]; p < cp_[j + 1]; ++p) M[(size_t)ci_[p] * m_ + r] += acx_[p];
             R[(size_t)r * m_ + r] = 1.0;
             rowid[r] = r;
         }

@@ -157,3 +157,17 @@ def test_presolve_then_crossover(native, orc, seed):
     assert_optimal(metrics(orc, lp, x, y), 1e-9)
     assert abs(lp.c @ x - f) <= 1e-9 * (1.0 + abs(f))
     assert_vertex(lp, x, basis, info)
+
+
+def test_repeated_entries(native, orc):
+    """A column entered twice in a row (1.5 x1 and 0.5 x1: 2 x1 in total):
+    crossover works on the summed matrix, as the LP means it."""
+    from igaos_gb300 import capi
+    lp = tiny([0, 0, 0, 1, 1], [0, 0, 1, 0, 1], [1.5, 0.5, 1.0, 1.0, -1.0], [-1.0, -1.0],
+              [0.0, 0.0], [4.0, 4.0], [-INF, -1.0], [6.0, 1.0])
+    xs, _, f = highs(lp)
+    for x0 in (np.zeros(2), xs + 0.01):
+        x, y, basis, info = capi.crossover(lp, x0)
+        assert info["status"] == "optimal"
+        assert_optimal(metrics(orc, lp, x, y), 1e-12)
+        assert abs(lp.c @ x - f) <= 1e-12 * (1.0 + abs(f))
