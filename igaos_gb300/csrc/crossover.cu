@@ -6,6 +6,7 @@
 #include <cmath>
 #include <condition_variable>
 #include <cstdint>
+#include <cstdlib>
 #include <functional>
 #include <limits>
 #include <memory>
@@ -90,10 +91,17 @@ private:
     bool stop_ = false;
 };
 
+// Up to 16 host threads from m = 768 on (below, the hand-offs cost more than
+// they save); IGAOS_PDHG_HOST_THREADS caps the count. Every thread owns whole
+// columns or rows of the dense loops, so the results do not depend on it.
 int pool_threads(int m) {
-    if (m < 768) return 1;  // below this the hand-offs cost more than they save
-    const unsigned hw = std::thread::hardware_concurrency();
-    return (int)std::min(16u, std::max(1u, hw));
+    if (m < 768) return 1;
+    unsigned t = std::min(16u, std::max(1u, std::thread::hardware_concurrency()));
+    if (const char* e = std::getenv("IGAOS_PDHG_HOST_THREADS")) {
+        const int v = std::atoi(e);
+        if (v >= 1) t = std::min(t, (unsigned)v);
+    }
+    return (int)t;
 }
 
 class Simplex {

@@ -171,3 +171,29 @@ def test_repeated_entries(native, orc):
         assert info["status"] == "optimal"
         assert_optimal(metrics(orc, lp, x, y), 1e-12)
         assert abs(lp.c @ x - f) <= 1e-12 * (1.0 + abs(f))
+
+
+def test_host_threads_do_not_change_the_result(native, tmp_path):
+    """An 800-row LP (the dense loops split over host threads from 768 rows
+    on): the vertex, duals and pivot count with 4 threads equal those with 1,
+    bit for bit (each thread owns whole columns or rows)."""
+    import json
+    import subprocess
+    import sys
+    code = (
+        "import json, sys, numpy as np\n"
+        "sys.path.insert(0, %r)\n"
+        "from igaos_gb300 import capi, generators as G\n"
+        "lp = G.random_lp(800, 1600, 2400, 5)\n"
+        "x0 = np.clip(lp.meta['x_star'], 0, 10)\n"
+        "x, y, b, info = capi.crossover(lp, x0)\n"
+        "print(json.dumps([x.tolist(), y.tolist(), b.tolist(), info['status'], info['pivots']]))\n"
+    ) % os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    out = []
+    for t in ("1", "4"):
+        env = dict(os.environ, IGAOS_PDHG_HOST_THREADS=t)
+        r = subprocess.run([sys.executable, "-c", code], env=env, capture_output=True, text=True,
+                           check=True)
+        out.append(json.loads(r.stdout))
+    assert out[0][3] == "optimal"
+    assert out[0] == out[1]
