@@ -5,7 +5,6 @@
 #include <cmath>
 #include <cstring>
 #include <limits>
-#include <unordered_map>
 
 namespace igx {
 namespace {
@@ -17,6 +16,13 @@ constexpr double kForceTol = 1e-12;  // activity bound this close to a row bound
 constexpr double kParallelTol = 1e-12;  // rows proportional to within this (relative)
 
 inline double mag(double b) { return std::isfinite(b) ? std::fabs(b) : 0.0; }
+
+// splitmix64 finaliser
+inline uint64_t mix64(uint64_t x) {
+    x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+    x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+    return x ^ (x >> 31);
+}
 
 }  // namespace
 
@@ -166,6 +172,13 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
     // x_j = (activity - others) / a already lies in [lo_j, hi_j], so those
     // bounds never bind and j is substituted like a free column
     auto implied_free = [&](int i, int j, double a) -> bool {
+        // a finite lower bound of x_j can only be implied through the row
+        // bound on its side (rmin for a > 0, rmax for a < 0), an upper one
+        // through the other: without it, no scan is needed
+        const double below = a > 0.0 ? rlo[i] : rhi[i], above = a > 0.0 ? rhi[i] : rlo[i];
+        if ((std::isfinite(lo[j]) && !std::isfinite(below)) ||
+            (std::isfinite(hi[j]) && !std::isfinite(above)))
+            return false;
         double L = 0.0, U = 0.0;  // activity range of the row's other columns
         for (int s = rp[i]; s < rp[i + 1]; ++s) {
             const int k = rj[s];
@@ -173,6 +186,7 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
             const double b = ra[s];
             L += b > 0.0 ? b * lo[k] : b * hi[k];
             U += b > 0.0 ? b * hi[k] : b * lo[k];
+            if (L == -kInf && U == kInf) return false;  // unbounded both ways
         }
         const double ilo = a > 0.0 ? (rlo[i] - U) / a : (rhi[i] - L) / a;
         const double ihi = a > 0.0 ? (rhi[i] - L) / a : (rlo[i] - U) / a;
@@ -190,35 +204,40 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
         std::sort(e.begin(), e.end());
     };
     auto parallel_rows = [&](bool& changed_out) -> int {
-        std::unordered_map<uint64_t, std::vector<int>> groups;
-        std::vector<uint64_t> hash(m, 0);
+        // one key per row: an order-free hash (a sum of per-entry hashes) of
+        // its live columns and their values over the entry of the smallest
+        // column; sorted by (key, row), equal keys form the candidate groups
+        std::vector<std::pair<uint64_t, int>> keys;
         for (int i = 0; i < m; ++i) {
             if (!ralive[i] || rcnt[i] < 2) continue;
-            live(i, ea);
-            uint64_t h = 1469598103934665603ull;
-            auto mix = [&](uint64_t v) { h = (h ^ v) * 1099511628211ull; };
-            for (const auto& e : ea) {
-                double r = e.second / ea[0].second;
-                r = std::round(r * 1e9) / 1e9;  // hash only; equality is checked below
+            int jmin = n;
+            double vmin = 0.0;
+            for (int q = rp[i]; q < rp[i + 1]; ++q)
+                if (calive[rj[q]] && rj[q] < jmin) {
+                    jmin = rj[q];
+                    vmin = ra[q];
+                }
+            uint64_t h = 0;
+            for (int q = rp[i]; q < rp[i + 1]; ++q) {
+                if (!calive[rj[q]]) continue;
+                const double r = std::round(ra[q] / vmin * 1e9) / 1e9;  // hash only
                 uint64_t bits;
                 std::memcpy(&bits, &r, sizeof(bits));
-                mix((uint64_t)e.first);
-                mix(bits);
+                h += mix64(((uint64_t)(uint32_t)rj[q] << 32) ^ mix64(bits));
             }
-            groups[h].push_back(i);
-            hash[i] = h;
+            keys.push_back({h, i});
         }
-        // rows in index order, each against the earlier rows of its group
-        // (deterministic whatever the map's bucket order)
-        for (int i = 0; i < m; ++i) {
-            if (!ralive[i] || rcnt[i] < 2) continue;
-            const std::vector<int>& rows = groups[hash[i]];
-            if (rows.size() < 2 || rows[0] == i) continue;
-            live(i, ea);
-            {
-                for (size_t v = 0; v < rows.size() && rows[v] < i; ++v) {
-                    const int k = rows[v];  // candidate to keep
-                    if (!ralive[k] || !ralive[i]) continue;
+        std::sort(keys.begin(), keys.end());
+        for (size_t g0 = 0, g1; g0 < keys.size(); g0 = g1) {
+            for (g1 = g0 + 1; g1 < keys.size() && keys[g1].first == keys[g0].first; ++g1) {
+            }
+            for (size_t u = g0 + 1; u < g1; ++u) {
+                const int i = keys[u].second;  // candidate to remove
+                if (!ralive[i]) continue;
+                live(i, ea);
+                for (size_t v = g0; v < u; ++v) {
+                    const int k = keys[v].second;  // earlier row: candidate to keep
+                    if (!ralive[k]) continue;
                     live(k, eb);
                     if (ea.size() != eb.size()) continue;
                     const double sr = ea[0].second / eb[0].second;
