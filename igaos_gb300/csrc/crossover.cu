@@ -113,7 +113,7 @@ public:
     std::vector<double> lb, ub, cost, val;
     std::vector<signed char> st;
 
-    int run(const double* x0);
+    int run(const double* x0, bool use_crash);
     void duals(double* y) const {
         for (int i = 0; i < m_; ++i) y[i] = -pi_[i];
     }
@@ -495,6 +495,11 @@ int Simplex::simplex(int64_t& it, int64_t cap, bool& pi_valid) {
         double dq = 0.0;
         price(phase1, q, dir, dq);
         if (q < 0) {
+            // phase 1 stuck: confirm on a fresh factorisation before ending
+            if (phase1 && n_rejected_ == 0 && since_ > 0) {
+                since_ = every_;
+                continue;
+            }
             if (n_rejected_ == 0) return phase1 ? kXoInfeasible : kXoOptimal;
             // only candidates with pivots below kPivTol are left: refactor
             // and give them one more chance before ending
@@ -510,7 +515,13 @@ int Simplex::simplex(int64_t& it, int64_t cap, bool& pi_valid) {
         const int r = ratio(q, dir, theta, up);
         // a phase-1 candidate always meets a violated basic on its way back,
         // unless rounding hid it: a numerical failure, not an unbounded edge
-        if (r == -2) return phase1 ? kXoSingular : kXoUnbounded;
+        if (r == -2) {
+            if (since_ > 0) {  // confirm on a fresh factorisation first
+                since_ = every_;
+                continue;
+            }
+            return phase1 ? kXoSingular : kXoUnbounded;
+        }
         if (r >= 0 && std::fabs(alpha_[r]) < kPivTol && !retried_) {
             rejected_[q] = 1;  // a poor pivot: try the other candidates first
             ++n_rejected_;
@@ -625,7 +636,7 @@ bool Simplex::crash() {
     return false;
 }
 
-int Simplex::run(const double* x0) {
+int Simplex::run(const double* x0, bool use_crash) {
     val.assign(nt_, 0.0);
     st.assign(nt_, kBasic);
     head_.resize(m_);
@@ -657,7 +668,7 @@ int Simplex::run(const double* x0) {
     for (int j = 0; j < n_; ++j)
         for (int p = cp_[j]; p < cp_[j + 1]; ++p) val[n_ + ci_[p]] += acx_[p] * val[j];
     bool pi_valid = true;  // slack costs are 0, so pi = 0
-    if (crash()) pi_valid = false;
+    if (use_crash && crash()) pi_valid = false;
 
     for (int j = 0; j < nt_; ++j) {  // 1. primal push
         if (st[j] != kSuperbasic) continue;
@@ -699,17 +710,23 @@ int crossover(int m, int n, const int* cp, const int* ci, const double* acx, con
         info.status = kXoTooLarge;
         return kXoTooLarge;
     }
-    Simplex S(m, n, cp, ci, acx, info);
-    S.lb.assign(cl, cl + n);
-    S.lb.insert(S.lb.end(), rmin, rmin + m);
-    S.ub.assign(cu, cu + n);
-    S.ub.insert(S.ub.end(), rmax, rmax + m);
-    S.cost.assign(c, c + n);
-    S.cost.resize(n + m, 0.0);
-    const int rc = S.run(x0);
-    std::copy(S.val.begin(), S.val.begin() + n, x);
-    S.duals(y);
-    if (basis) std::copy(S.st.begin(), S.st.end(), basis);
+    // with the crash basis first; a start it does not suit is run again
+    // from the slack basis
+    int rc = kXoSingular;
+    for (int attempt = 0; attempt < 2 && rc != kXoOptimal; ++attempt) {
+        if (attempt == 1) info = CrossoverInfo();
+        Simplex S(m, n, cp, ci, acx, info);
+        S.lb.assign(cl, cl + n);
+        S.lb.insert(S.lb.end(), rmin, rmin + m);
+        S.ub.assign(cu, cu + n);
+        S.ub.insert(S.ub.end(), rmax, rmax + m);
+        S.cost.assign(c, c + n);
+        S.cost.resize(n + m, 0.0);
+        rc = S.run(x0, attempt == 0);
+        std::copy(S.val.begin(), S.val.begin() + n, x);
+        S.duals(y);
+        if (basis) std::copy(S.st.begin(), S.st.end(), basis);
+    }
     info.status = rc;
     info.time_ms =
         std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();

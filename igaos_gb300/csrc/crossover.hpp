@@ -20,6 +20,9 @@
 //      values and duals are clean;
 //   4. a last push of variables still inside their bounds (reduced cost
 //      0, so the objective does not move).
+// An unbounded edge or a stuck phase 1 is confirmed on a fresh factorisation
+// before it ends the run, and a run from the crash basis that does not end
+// optimal is repeated once from the slack basis.
 // B^-1 is kept explicitly (dense, m x m; product-form updates, Gauss-Jordan
 // refactorisation with partial pivoting every m pivots), so the host work
 // per pivot is O(m^2), split over up to 16 host threads: LPs up to

@@ -197,3 +197,30 @@ def test_host_threads_do_not_change_the_result(native, tmp_path):
         out.append(json.loads(r.stdout))
     assert out[0][3] == "optimal"
     assert out[0] == out[1]
+
+
+@pytest.mark.skipif(reference_dir() is None, reason="reference tree not present")
+@pytest.mark.parametrize("name", ["scorpion", "modszk1", "wood1p", "qap8"])
+def test_netlib_hard_cases_from_near_the_optimum(native, orc, name):
+    """Netlib LPs that once ended wrongly from a start 1e-6 off the optimum:
+    scorpion (a crash basis with 47 dependent columns, then a false
+    infeasible), modszk1, wood1p and qap8 (heavy degeneracy). The run from
+    the crash basis, confirmed outcomes and the slack-basis rerun end them
+    at an optimal vertex."""
+    from igaos_gb300 import build, capi
+    path = os.path.join(reference_dir(), "demo", "models", "netlib_full", name + ".mps")
+    if not os.path.exists(path):
+        pytest.skip("netlib file missing")
+    build.build()
+    from igaos_gb300 import _core
+    M = _core.read_mps(path)
+    a = lambda v, t=float: np.asarray(v, t)
+    lp = G.LPData(M.m, M.n, a(M.ap, np.int32), a(M.ai, np.int32), a(M.ax), a(M.cp, np.int32),
+                  a(M.ci, np.int32), a(M.acx), a(M.c), a(M.cl), a(M.cu), a(M.rmin), a(M.rmax),
+                  float(M.obj_const))
+    xs, _, f = highs(lp)
+    x0 = xs + 1e-6 * (1 + np.abs(xs)) * np.random.default_rng(1).standard_normal(lp.n)
+    x, y, basis, info = capi.crossover(lp, x0)
+    assert info["status"] == "optimal", info
+    assert_optimal(metrics(orc, lp, x, y), 1e-9)
+    assert abs(lp.c @ x - f) <= 1e-9 * (1.0 + abs(f))
