@@ -23,13 +23,31 @@ _dp = C.POINTER(C.c_double)
 _ip = C.POINTER(C.c_int)
 
 
+STAGED = os.path.join(HERE, "_ref", "src")
+
+
+def reference_dir():
+    """The reference tree: $IGAOS_REFERENCE_DIR, else a `reference` directory
+    beside the repository; None when neither exists."""
+    d = os.environ.get("IGAOS_REFERENCE_DIR") or os.path.join(
+        os.path.dirname(os.path.dirname(HERE)), "reference")
+    return d if os.path.isdir(d) else None
+
+
 def build(ref: bool = False) -> None:
-    """Compile liborc.so (and the reference helpers when `ref` and the
-    reference tree exists)."""
-    targets = ["all"]
-    if ref and os.path.isdir(os.environ.get("REF", "/root/reference")):
-        targets.append("ref")
-    subprocess.run(["make", "-s", "-C", HERE, *targets], check=True)
+    """Compile liborc.so; with `ref`, also the reference helpers under _ref/:
+    from the reference tree when it exists (staging the files they read into
+    _ref/src on the way), else from an earlier staging in _ref/src."""
+    targets, args = ["all"], []
+    if ref:
+        rd = reference_dir()
+        if rd is not None:
+            targets += ["stage", "ref"]
+            args = [f"REF={rd}"]
+        elif os.path.isdir(STAGED):
+            targets += ["ref"]
+            args = [f"REF={STAGED}"]
+    subprocess.run(["make", "-s", "-C", HERE, *args, *targets], check=True)
 
 
 class orc_metrics(C.Structure):
@@ -352,3 +370,45 @@ def ref_simplex_solve(lp: LP, time_limit=600.0):
         _d(x), _d(y), msg, 256)
     return dict(status=STATUS_NAMES.get(st, "?"), objective=obj.value, iterations=its.value,
                 x=x, y=y, message=msg.value.decode())
+
+
+def ref_pdhg_available() -> bool:
+    """True when libref_eval.so was built with the reference's GPU solve."""
+    if not ref_available():
+        return False
+    return hasattr(_ref_eval(), "ref_pdhg_solve")
+
+
+# The reference's dense dual repair (src/pdhg/pdhg.cu:322-327) sizes and
+# indexes its m x m matrix with int arithmetic; above this many rows m*m
+# overflows int32, so a solve that reaches the repair schedule (k >= 5000,
+# pdhg.cu:854) is only run with fewer iterations than that.
+REF_REPAIR_MAX_ROWS = 46340
+REF_REPAIR_FIRST_K = 5000
+
+
+def ref_pdhg_solve(lp: LP, tolerance=1e-4, time_limit=120.0, max_iterations=500000,
+                   verbosity=0):
+    """The reference's own GPU PDHG (cuSPARSE path, compiled from its sources)
+    on `lp`: dict with status_name, objective, pinf, dinf, gap, iterations,
+    loop_ms (its own timer), wall_ms (the whole call), x, y, message.
+    LPs above REF_REPAIR_MAX_ROWS rows must be given a finite iteration budget
+    below REF_REPAIR_FIRST_K and no finite time limit."""
+    if lp.m > REF_REPAIR_MAX_ROWS and not (
+            max_iterations < REF_REPAIR_FIRST_K and not (0 < time_limit < 1e6)):
+        raise ValueError("the reference's dense dual repair overflows int32 above "
+                         f"{REF_REPAIR_MAX_ROWS} rows: give max_iterations < "
+                         f"{REF_REPAIR_FIRST_K} and time_limit >= 1e6")
+    L = _ref_eval()
+    L.ref_pdhg_solve.restype = C.c_int
+    out = np.zeros(7)
+    x = np.zeros(lp.n); y = np.zeros(lp.m)
+    msg = C.create_string_buffer(512)
+    st = L.ref_pdhg_solve(lp.m, lp.n, _i(lp.ap), _i(lp.ai), _d(lp.ax), _i(lp.cp), _i(lp.ci),
+                          _d(lp.acx), _d(lp.c), _d(lp.cl), _d(lp.cu), _d(lp.rmin),
+                          _d(lp.rmax), C.c_double(lp.obj_const), C.c_double(tolerance),
+                          C.c_double(time_limit), C.c_long(int(max_iterations)),
+                          C.c_int(verbosity), _d(out), _d(x), _d(y), msg, 512)
+    return dict(status_name=STATUS_NAMES.get(st, "exception"), objective=out[0],
+                pinf=out[1], dinf=out[2], gap=out[3], iterations=int(out[4]),
+                loop_ms=out[5], wall_ms=out[6], x=x, y=y, message=msg.value.decode())

@@ -5,7 +5,10 @@
 // Built by oracle/Makefile into oracle/_ref/; test infrastructure only.
 #include "pdhg.cu"  // reference src/pdhg/pdhg.cu (include path set by the Makefile)
 
+#include <chrono>
 #include <cstring>
+#include <exception>
+#include <string>
 #include <tuple>
 #include <vector>
 
@@ -115,6 +118,72 @@ int ref_dual_repair(int m, int n, const int* ap, const int* ai, const double* ax
     if ((int)out.size() == m) std::memcpy(y, out.data(), sizeof(double) * m);
     else for (int i = 0; i < m; ++i) y[i] = std::numeric_limits<double>::quiet_NaN();
     return ok ? 1 : 0;
+}
+
+// The reference's GPU PDHG solve (src/pdhg/pdhg.cu:457-1156, cuSPARSE and
+// cuBLAS on the legacy default stream) on a model given by arrays. Options
+// follow igaos::Options (include/igaos/options.h): max_iterations binds only
+// when time_limit is not in (0, 1e6) (pdhg.cu:669-671).
+// out[0..6] = objective, pinf, dinf, rel_gap, iterations, solve_time_ms
+// (the reference's own loop timer), wall_ms (the whole call: handles, Ruiz,
+// upload, power iteration, loop, download, frees). Returns the Status value,
+// or -1 when the call threw (the message says what).
+int ref_pdhg_solve(int m, int n, const int* ap, const int* ai, const double* ax,
+                   const int* cp, const int* ci, const double* acx, const double* c,
+                   const double* cl, const double* cu, const double* rmin,
+                   const double* rmax, double obj_const, double tolerance,
+                   double time_limit, long max_iterations, int verbosity,
+                   double* out, double* x, double* y, char* msg, int msglen) {
+    igaos::io::Model M;
+    M.m = m;
+    M.n = n;
+    const int nnz = ap[m];
+    M.ap.assign(ap, ap + m + 1);
+    M.ai.assign(ai, ai + nnz);
+    M.ax.assign(ax, ax + nnz);
+    M.cp.assign(cp, cp + n + 1);
+    M.ci.assign(ci, ci + nnz);
+    M.acx.assign(acx, acx + nnz);
+    M.c.assign(c, c + n);
+    M.cl.assign(cl, cl + n);
+    M.cu.assign(cu, cu + n);
+    M.rmin.assign(rmin, rmin + m);
+    M.rmax.assign(rmax, rmax + m);
+    M.integ.assign(n, 0);
+    M.obj_const = obj_const;
+    igaos::Options o;
+    o.tolerance = tolerance;
+    o.time_limit_s = time_limit;
+    o.max_iterations = max_iterations;
+    o.verbosity = verbosity;
+    int rc = -1;
+    std::string text;
+    auto t0 = std::chrono::steady_clock::now();
+    try {
+        igaos::Solution s = igaos::pdhg::solve(M, o);
+        cudaDeviceSynchronize();
+        auto t1 = std::chrono::steady_clock::now();
+        out[0] = s.objective;
+        out[1] = s.pinf;
+        out[2] = s.dinf;
+        out[3] = s.rel_gap;
+        out[4] = (double)s.iterations;
+        out[5] = s.solve_time_ms;
+        out[6] = std::chrono::duration<double, std::milli>(t1 - t0).count();
+        if ((int)s.x.size() == n) std::memcpy(x, s.x.data(), sizeof(double) * n);
+        if ((int)s.y.size() == m) std::memcpy(y, s.y.data(), sizeof(double) * m);
+        rc = (int)s.status;
+        text = s.message;
+    } catch (const std::exception& e) {
+        text = std::string("exception: ") + e.what();
+    } catch (...) {
+        text = "exception";
+    }
+    if (msg && msglen > 0) {
+        std::strncpy(msg, text.c_str(), (size_t)msglen - 1);
+        msg[msglen - 1] = 0;
+    }
+    return rc;
 }
 
 }  // extern "C"

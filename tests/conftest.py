@@ -8,7 +8,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = os.environ.get("IGAOS_REFERENCE_DIR", "/root/reference")
+# the reference tree: $IGAOS_REFERENCE_DIR, else `reference` beside the repository
+REFERENCE = os.environ.get("IGAOS_REFERENCE_DIR") or os.path.join(
+    os.path.dirname(ROOT), "reference")
 
 
 def pytest_configure(config):
