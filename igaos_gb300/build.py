@@ -25,12 +25,11 @@ CLI = os.path.join(PKG, "igaos")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
            "-I", INC, "-I", CSRC] + ARCH
-CU_SOURCES = ["engine.cu", "capi.cu", "batch.cu", "kkt_noalloc.cu", "unrolled.cu", "repair.cu",
+CU_SOURCES = ["engine.cu", "capi.cu", "batch.cu", "kkt_noalloc.cu", "unrolled.cu", "host_kkt.cu",
               "calibrate.cu", "certificate.cu", "presolve.cu",
               "crossover.cu"]
-# host code whose arithmetic must not be contracted into FMAs on any host
-# (dual repair: bit-identical to the reference host code on x86 and Arm)
-EXTRA_FLAGS = {"repair.cu": ["-Xcompiler", "-ffp-contract=off"]}
+# per-file extra nvcc flags
+EXTRA_FLAGS = {}
 CXX_HOST = ["model.cpp", "pdhg_solve.cpp"]
 
 

@@ -118,8 +118,6 @@ def lib():
         L.igaos_pdhg_iterate.argtypes = [C.c_void_p, C.c_int, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]
         L.igaos_pdhg_evaluate.argtypes = [C.c_void_p, _dp, _dp, _dp]
         L.igaos_pdhg_spmv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp]
-        L.igaos_pdhg_dual_repair.argtypes = [C.c_void_p, _dp, _dp, _dp, C.c_double, _dp,
-                                             C.POINTER(C.c_int)]
         L.igaos_pdhg_gather_rate.argtypes = [C.c_int, C.c_int, _dp]
         L.igaos_pdhg_ray_certificate.argtypes = [C.c_int, C.c_int] + [_dp] * 11 + [C.POINTER(C.c_int)]
         L.igaos_pdhg_presolve.argtypes = [
@@ -404,16 +402,6 @@ class Problem:
         out = np.zeros(6)
         _check(lib().igaos_pdhg_evaluate(self.h, _d(x), _d(y), _d(out)))
         return dict(zip(("pinf", "dinf", "gap", "op", "od", "prow"), out.tolist()))
-
-    def dual_repair(self, x, Ax, y_it, col_tol):
-        """(certified, y): the engine's dual repair at candidate x (A x = Ax)
-        from the dual estimate y_it, original units (m <= 4096)."""
-        a = [np.ascontiguousarray(v, np.float64) for v in (x, Ax, y_it)]
-        y = np.zeros(self.m)
-        ok = C.c_int(0)
-        _check(lib().igaos_pdhg_dual_repair(self.h, *[_d(v) for v in a], C.c_double(col_tol),
-                                            _d(y), C.byref(ok)))
-        return bool(ok.value), y
 
     def dual_repair_device(self, x, y_it, col_tol, tol):
         """(certified, y, metrics): the engine's matrix-free dual repair on the

@@ -14,7 +14,7 @@
 #include "certificate.hpp"
 #include "crossover.hpp"
 #include "presolve.hpp"
-#include "repair.hpp"
+#include "host_kkt.hpp"
 
 struct igaos_pdhg_problem {
     igx::Engine* eng = nullptr;  // NULL when presolve removed the whole LP
@@ -557,15 +557,6 @@ int igaos_pdhg_evaluate(igaos_pdhg_problem* p, const double* x, const double* y,
     if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng || !x || !y || !out6) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
     return guarded([&] { p->eng->evaluate(x, y, out6); });
-}
-
-int igaos_pdhg_dual_repair(igaos_pdhg_problem* p, const double* x, const double* Ax,
-                           const double* y_it, double col_tol, double* y, int* certified) {
-    if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
-    if (!p || !p->eng || !x || !Ax || !y_it || !y || !certified)
-        return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");
-    if (!(col_tol >= 0.0)) return fail(IGAOS_PDHG_ERR_INVALID, "col_tol must be >= 0");
-    return guarded([&] { *certified = p->eng->repair(x, Ax, y_it, col_tol, y) ? 1 : 0; });
 }
 
 int igaos_pdhg_dual_repair_device(igaos_pdhg_problem* p, const double* x, const double* y_it,

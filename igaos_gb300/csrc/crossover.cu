@@ -7,6 +7,7 @@
 #include <condition_variable>
 #include <cstdint>
 #include <cstdlib>
+#include <exception>
 #include <functional>
 #include <limits>
 #include <memory>
@@ -54,9 +55,20 @@ public:
             ++gen_;
         }
         cv_.notify_all();
-        slice(0, f);
+        std::exception_ptr own;
+        try {
+            slice(0, f);
+        } catch (...) {
+            own = std::current_exception();
+        }
         std::unique_lock<std::mutex> lk(mu_);
         done_.wait(lk, [&] { return pending_ == 0; });
+        // a worker's exception (e.g. bad_alloc) surfaces on the calling
+        // thread, where the C ABI turns it into an error code
+        std::exception_ptr err = own ? own : error_;
+        error_ = nullptr;
+        lk.unlock();
+        if (err) std::rethrow_exception(err);
     }
 
 private:
@@ -76,8 +88,14 @@ private:
                 if (stop_) return;
                 f = job_;
             }
-            slice(t, *f);
+            std::exception_ptr e;
+            try {
+                slice(t, *f);
+            } catch (...) {
+                e = std::current_exception();
+            }
             std::lock_guard<std::mutex> g(mu_);
+            if (e && !error_) error_ = e;
             if (--pending_ == 0) done_.notify_one();
         }
     }
@@ -89,6 +107,7 @@ private:
     int count_ = 0, pending_ = 0;
     uint64_t gen_ = 0;
     bool stop_ = false;
+    std::exception_ptr error_;  // first worker exception of the current job
 };
 
 // Up to 16 host threads from m = 768 on (below, the hand-offs cost more than

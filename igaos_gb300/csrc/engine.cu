@@ -273,26 +273,6 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     base_.rmax = vec(rmax, pr_);
     base_.cmax = 0.0;
     for (int j = 0; j < n; ++j) base_.cmax = std::max(base_.cmax, std::fabs(c[j]));
-    // IGAOS_PDHG_REPAIR=device: the matrix-free device repair for every m
-    // (by default it serves m > kRepairMaxRows only)
-    if (const char* e = std::getenv("IGAOS_PDHG_REPAIR")) force_dev_repair_ = std::strcmp(e, "device") == 0;
-    if (m <= kRepairMaxRows) {  // host copy for dual repair (original units and order)
-        hlp_.reset(new HostLP());
-        HostLP& h = *hlp_;
-        h.m = m;
-        h.n = n;
-        h.ap.assign(ap, ap + m + 1);
-        h.ai.assign(ai, ai + nnz);
-        h.ax.assign(ax, ax + nnz);
-        h.cp.assign(cp, cp + n + 1);
-        h.ci.assign(ci, ci + nnz);
-        h.acx.assign(acx, acx + nnz);
-        h.c.assign(c, c + n);
-        h.cl.assign(cl, cl + n);
-        h.cu.assign(cu, cu + n);
-        h.rmin.assign(rmin, rmin + m);
-        h.rmax.assign(rmax, rmax + m);
-    }
     base_.sc = ar_.alloc<double>(n);
     base_.scl = ar_.alloc<double>(n);
     base_.scu = ar_.alloc<double>(n);
@@ -673,103 +653,45 @@ bool Engine::try_repair(const Vecs& v, int p, bool anch, const DevMetrics& ma,
         if (verbosity > 1)
             std::fprintf(stderr, "[pdhg-gb300] dual repair @k=%lld candidate %d (pinf %.2e prow %.2e "
                                  "dinf %.2e)\n", k, cnd, t->pinf, t->prow, t->dinf);
-        if (!hlp_ || force_dev_repair_) {  // matrix-free repair on the device
-            ensure_rep();
-            const double *xs, *ys;
-            if (anch) {
-                xs = cnd == 1 ? anc_.xf[1] : anc_.xb;
-                ys = cnd == 1 ? anc_.yf[1] : anc_.yf[0];
-            } else if constexpr (std::is_same<T, double>::value) {
-                xs = cnd == 1 ? w.xavg[p] : w.xb;
-                ys = cnd == 1 ? w.yavg[p] : w.y[p];
-            } else {
-                k_convert<T, double><<<grid_for(n), kThreads, 0, st_>>>(n, cnd == 1 ? w.xavg[p] : w.xb,
-                                                                       rep_.xs);
-                k_convert<T, double><<<grid_for(m), kThreads, 0, st_>>>(m, cnd == 1 ? w.yavg[p] : w.y[p],
-                                                                       rep_.ys);
-                CU(cudaGetLastError());
-                xs = rep_.xs;
-                ys = rep_.ys;
-            }
-            for (const double col_tol : {1e-6, 1e-1}) {
-                DevMetrics mt{};
-                const bool ok = repair_dev(xs, ys, col_tol, tol, verbosity, mt);
-                if (verbosity > 1)
-                    std::fprintf(stderr, "[pdhg-gb300] device dual repair col_tol %.0e: gap %.3e\n",
-                                 col_tol, ok ? mt.gap : std::numeric_limits<double>::infinity());
-                if (!ok) continue;
-                std::vector<double> hx(n), hy(m);
-                CU(cudaMemcpyAsync(hx.data(), xs, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
-                CU(cudaMemcpyAsync(hy.data(), rep_.ybest, sizeof(double) * m, cudaMemcpyDeviceToHost,
-                                   st_));
-                CU(cudaStreamSynchronize(st_));
-                out.rx.assign(n, 0.0);
-                out.ry.assign(m, 0.0);
-                for (int j = 0; j < n; ++j) out.rx[pc_[j]] = hx[j] * hp_dc_[j];
-                for (int i = 0; i < m; ++i) out.ry[pr_[i]] = hy[i] / hp_dr_[i];
-                out.last = mt;
-                out.last_is_avg = cnd == 1;
-                out.use_inc = false;
-                out.repaired = true;
-                out.status = IGAOS_STATUS_NEAR_OPTIMAL;
-                return true;
-            }
-            continue;
-        }
-        // candidate in original units, device numbering
-        std::vector<double> hx(n), hy(m);
-        if (anch) {  // full FP64 iterates of this check (anchor + delta)
-            const double* sx = cnd == 1 ? anc_.xf[1] : anc_.xb;
-            const double* sy = cnd == 1 ? anc_.yf[1] : anc_.yf[0];
-            CU(cudaMemcpyAsync(hx.data(), sx, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
-            CU(cudaMemcpyAsync(hy.data(), sy, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
-            CU(cudaStreamSynchronize(st_));
-            for (int j = 0; j < n; ++j) hx[j] *= hp_dc_[j];
+        ensure_rep();
+        const double *xs, *ys;
+        if (anch) {
+            xs = cnd == 1 ? anc_.xf[1] : anc_.xb;
+            ys = cnd == 1 ? anc_.yf[1] : anc_.yf[0];
+        } else if constexpr (std::is_same<T, double>::value) {
+            xs = cnd == 1 ? w.xavg[p] : w.xb;
+            ys = cnd == 1 ? w.yavg[p] : w.y[p];
         } else {
-            unscale_cols<T>(cnd == 1 ? w.xavg[p] : w.xb, v, hx.data());
-            fetch_scaled<T>(cnd == 1 ? w.yavg[p] : w.y[p], m, hy.data());
+            k_convert<T, double><<<grid_for(n), kThreads, 0, st_>>>(n, cnd == 1 ? w.xavg[p] : w.xb,
+                                                                   rep_.xs);
+            k_convert<T, double><<<grid_for(m), kThreads, 0, st_>>>(m, cnd == 1 ? w.yavg[p] : w.y[p],
+                                                                   rep_.ys);
+            CU(cudaGetLastError());
+            xs = rep_.xs;
+            ys = rep_.ys;
         }
-        for (int i = 0; i < m; ++i) hy[i] = 1.0 * hy[i] / hp_dr_[i];
-        std::vector<double> rx(n), ry_it(m), rAx(m, 0.0);
-        for (int j = 0; j < n; ++j) rx[pc_[j]] = hx[j];
-        for (int i = 0; i < m; ++i) ry_it[pr_[i]] = hy[i];
-        const HostLP& lp = *hlp_;
-        for (int j = 0; j < n; ++j)
-            for (int q = lp.cp[j]; q < lp.cp[j + 1]; ++q) rAx[lp.ci[q]] += lp.acx[q] * rx[j];
         for (const double col_tol : {1e-6, 1e-1}) {
-            std::vector<double> ry;
-            if (!dual_repair(lp, rx.data(), rAx.data(), ry_it.data(), col_tol, ry)) continue;
-            std::vector<double> rd(n);
-            for (int j = 0; j < n; ++j) {
-                double d = lp.c[j];
-                for (int q = lp.cp[j]; q < lp.cp[j + 1]; ++q) d += lp.acx[q] * ry[lp.ci[q]];
-                rd[j] = d;
-            }
-            const HostMetrics hm = host_evaluate(lp, rx.data(), ry.data(), rAx.data(), rd.data());
+            DevMetrics mt{};
+            const bool ok = repair_dev(xs, ys, col_tol, tol, verbosity, mt);
             if (verbosity > 1)
-                std::fprintf(stderr, "[pdhg-gb300] dual repair col_tol %.0e: gap %.3e\n", col_tol,
-                             hm.gap);
-            // a repaired pair is certified by pinf, prow and the gap: the gap
-            // is a valid weak-duality bound for any dual in the cone
-            if (hm.pinf <= tol && hm.prow <= tol && std::isfinite(hm.gap) && hm.gap <= tol) {
-                DevMetrics mt{};
-                mt.pinf = hm.pinf;
-                mt.dinf = hm.dinf;
-                mt.gap = hm.gap;
-                mt.op = hm.op;
-                mt.od = hm.od;
-                mt.prow = hm.prow;
-                mt.err = std::max(hm.pinf, std::max(hm.dinf, hm.gap));
-                mt.finite = 1;
-                out.last = mt;
-                out.last_is_avg = cnd == 1;
-                out.use_inc = false;
-                out.repaired = true;
-                out.rx = std::move(rx);
-                out.ry = std::move(ry);
-                out.status = IGAOS_STATUS_NEAR_OPTIMAL;
-                return true;
-            }
+                std::fprintf(stderr, "[pdhg-gb300] device dual repair col_tol %.0e: gap %.3e\n",
+                             col_tol, ok ? mt.gap : std::numeric_limits<double>::infinity());
+            if (!ok) continue;
+            std::vector<double> hx(n), hy(m);
+            CU(cudaMemcpyAsync(hx.data(), xs, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
+            CU(cudaMemcpyAsync(hy.data(), rep_.ybest, sizeof(double) * m, cudaMemcpyDeviceToHost,
+                               st_));
+            CU(cudaStreamSynchronize(st_));
+            out.rx.assign(n, 0.0);
+            out.ry.assign(m, 0.0);
+            for (int j = 0; j < n; ++j) out.rx[pc_[j]] = hx[j] * hp_dc_[j];
+            for (int i = 0; i < m; ++i) out.ry[pr_[i]] = hy[i] / hp_dr_[i];
+            out.last = mt;
+            out.last_is_avg = cnd == 1;
+            out.use_inc = false;
+            out.repaired = true;
+            out.status = IGAOS_STATUS_NEAR_OPTIMAL;
+            return true;
         }
     }
     return false;
@@ -928,17 +850,6 @@ bool Engine::repair_device(const double* x, const double* y_it, double col_tol, 
     return ok;
 }
 
-bool Engine::repair(const double* x, const double* Ax, const double* y_it, double col_tol,
-                    double* y) {
-    if (!hlp_)
-        throw CudaError(IGAOS_PDHG_ERR_INVALID,
-                        "dual repair keeps a dense m x m factor: limited to m <= 4096 rows");
-    std::vector<double> out;
-    const bool ok = dual_repair(*hlp_, x, Ax, y_it, col_tol, out);
-    if ((int)out.size() == m) std::memcpy(y, out.data(), sizeof(double) * m);
-    else for (int i = 0; i < m; ++i) y[i] = std::numeric_limits<double>::quiet_NaN();
-    return ok;
-}
 
 // Infeasibility certificates (no counterpart in the reference engine): the
 // change between consecutive restart points of an LP without a solution

@@ -10,7 +10,7 @@
 
 #include "igaos_pdhg.h"
 #include "device.cuh"
-#include "repair.hpp"
+#include "host_kkt.hpp"
 
 #include <memory>
 
@@ -141,10 +141,6 @@ class Engine {
                  double* yavg, double* axc, double* st6);
     void evaluate(const double* x, const double* y, double* out6);
     void spmv(int transpose, int precision, const double* x, double* y);
-    // dual repair on the host copy of the LP (m <= kRepairMaxRows); original
-    // units, caller's numbering
-    bool repair(const double* x, const double* Ax, const double* y_it, double col_tol,
-                double* y);
     // matrix-free dual repair on the device (any m): original units, caller's
     // numbering; certified when pinf, prow and a finite gap are <= tol.
     // out6 = pinf, dinf, gap, op, od, prow of (x, y).
@@ -212,8 +208,6 @@ class Engine {
     template <typename T> void fetch_scaled(const T* src, int len, double* dst);
     template <typename T> void unscale_cols(const T* xs, const Vecs& v, double* host_out);
     // anchored (FP32 + FP64 refinement) iterations
-    // host copy of the original LP for dual repair (small m only)
-    std::unique_ptr<HostLP> hlp_;
     void emit_repaired(const LoopOut& out, igaos_pdhg_result& r, double* x, double* y);
     // infeasibility certificates from the change between restart points
     // (0: none, 1: dual ray, 2: primal ray; the ray in out.ry / out.rx)
@@ -233,7 +227,6 @@ class Engine {
     };
     RepBufs rep_{};
     bool have_rep_ = false;
-    bool force_dev_repair_ = false;
     // dynamic shared memory of the cluster attempt kernel for FP32 / FP64
     // (0: that precision uses the grid-wide kernels)
     int small_bytes_[2] = {0, 0};

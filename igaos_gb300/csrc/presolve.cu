@@ -220,7 +220,10 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
             uint64_t h = 0;
             for (int q = rp[i]; q < rp[i + 1]; ++q) {
                 if (!calive[rj[q]]) continue;
-                const double r = std::round(ra[q] / vmin * 1e9) / 1e9;  // hash only
+                // hash only: two ratios within 1e-12 that straddle a 1e-9
+                // rounding boundary land in different groups, so such a
+                // pair is not merged (a reduction missed, never a wrong one)
+                const double r = std::round(ra[q] / vmin * 1e9) / 1e9;
                 uint64_t bits;
                 std::memcpy(&bits, &r, sizeof(bits));
                 h += mix64(((uint64_t)(uint32_t)rj[q] << 32) ^ mix64(bits));
@@ -253,8 +256,15 @@ int presolve(int m, int n, const int* ap, const int* ai, const double* ax, const
                     const bool tl = ilo > rlo[k], th = ihi < rhi[k];
                     double nlo = tl ? ilo : rlo[k], nhi = th ? ihi : rhi[k];
                     if (nlo > nhi) {
-                        if (nlo - nhi > kFeasTol * (1.0 + mag(nlo) + mag(nhi)))
-                            return kPresolveInfeasible;
+                        if (nlo - nhi > kFeasTol * (1.0 + mag(nlo) + mag(nhi))) {
+                            // row i needs row k's activity above rhi[k]
+                            // (side +1) or below rlo[k] (side -1): the dual
+                            // ray y_k = side, y_i = -side / sr has A^T y = 0
+                            // on the live columns and a positive bound
+                            P.infeasible_row2 = i;
+                            P.infeasible_ratio = sr;
+                            return infeasible(k, ilo > rhi[k] ? 1 : -1);
+                        }
                         if (tl && !th) nlo = nhi;
                         else nhi = nlo;
                     }
@@ -562,6 +572,7 @@ bool infeasible_ray(const Presolved& P, double* y) {
     std::vector<double> x(P.n0, 0.0);
     std::fill(y, y + P.m0, 0.0);
     y[P.infeasible_row] = P.infeasible_side;
+    if (P.infeasible_row2 >= 0) y[P.infeasible_row2] = -P.infeasible_side / P.infeasible_ratio;
     undo(P, x.data(), y, true);
     return true;
 }

@@ -92,9 +92,15 @@ struct Presolved {
     int unbounded_col = -1;
     double ray_step = 0.0;
     // kPresolveInfeasible: the row whose bounds the activity cannot meet and
-    // the sign of its dual ray (+1 at rmax, -1 at rmin); -1 when none
+    // the sign of its dual ray (+1 at rmax, -1 at rmin); -1 when none. When
+    // two parallel rows (row infeasible_row2 = infeasible_ratio x row
+    // infeasible_row) have ranges that do not meet, the ray also holds
+    // y[infeasible_row2] = -infeasible_side / infeasible_ratio, which cancels
+    // their columns.
     int infeasible_row = -1;
     int infeasible_side = 0;
+    int infeasible_row2 = -1;
+    double infeasible_ratio = 0.0;
 };
 
 // Reduces the LP (CSR, original units). Returns kPresolveReduced (out holds
@@ -122,8 +128,10 @@ void postsolve_ray(const Presolved& p, const double* x_red, const double* y_red,
 bool unbounded_ray(const Presolved& p, double* x);
 
 // kPresolveInfeasible: y (m0) = a dual ray of the original LP: the row that
-// proved it (y_i = +-1 in the LP presolve had reduced so far), mapped back
-// through the records made before it. False when no row proved it.
+// proved it (y_i = +-1 in the LP presolve had reduced so far; for two
+// parallel rows with disjoint ranges, +-1 on the kept row and the opposite
+// multiple on the other), mapped back through the records made before it.
+// False when no row proved it.
 bool infeasible_ray(const Presolved& p, double* y);
 
 }  // namespace igx

@@ -303,21 +303,10 @@ int igaos_pdhg_iterate(igaos_pdhg_problem* p, int precision, int64_t iters,
                        double* x, double* y, double* xavg, double* yavg,
                        double* axcur, double* state6);
 
-/* Dual repair (the reference's dual_repair, src/pdhg/pdhg.cu:257-448): for a
- * primal candidate x with Ax = A x (ORIGINAL units, the caller's numbering)
- * and a dual estimate y_it, alternating projections onto {A_J^T y = -c_J}
- * (columns strictly inside their bounds by col_tol), the sign half-spaces of
- * columns with an infinite bound and the row cone. *certified = 1 when a
- * dual with a finite duality gap was found (y = the smallest-gap one), else
- * 0 (y = the point of least sign violation, or NaN when the dense
- * factorisation failed). Dense m x m normal equations on the host: problems
- * with m > 4096 return IGAOS_PDHG_ERR_INVALID. The solve loop runs the same
- * step from k = 5000 on (spacing 2000, x3 up to 30000), as the reference. */
-int igaos_pdhg_dual_repair(igaos_pdhg_problem* p, const double* x, const double* Ax,
-                           const double* y_it, double col_tol, double* y, int* certified);
-
-/* Matrix-free dual repair on the device, for any m (the solve loop uses it
- * in place of igaos_pdhg_dual_repair when m > 4096, on the same schedule).
+/* Matrix-free dual repair on the device, for any m (the solve loop runs the
+ * same step on the reference's schedule, src/pdhg/pdhg.cu:854-931: from
+ * k = 5000, spacing 2000 tripling up to 30000; col_tol tiers 1e-6, 1e-1).
+ * Replaces the reference's dual_repair (src/pdhg/pdhg.cu:257-448).
  * Same three sets as the reference's dual_repair (src/pdhg/pdhg.cu:288-448)
  * on the Ruiz-scaled LP: the regularised least-squares step onto
  * {A_J^T y = -c_J} by CGLS instead of a dense Cholesky solve, all violated
@@ -327,8 +316,8 @@ int igaos_pdhg_dual_repair(igaos_pdhg_problem* p, const double* x, const double*
  * caller's numbering. *certified = 1 when pinf, prow and a finite gap of
  * (x, y) are all <= tol; y = the dual with the smallest finite gap seen
  * (else the last iterate). metrics6 (may be NULL) = pinf, dinf, gap, op, od,
- * prow of (x, y). No reference counterpart: the reference's dense repair is
- * limited by its m x m factor. */
+ * prow of (x, y). Unlike the reference's dense m x m factor it needs no
+ * memory beyond a few n- and m-vectors. */
 int igaos_pdhg_dual_repair_device(igaos_pdhg_problem* p, const double* x, const double* y_it,
                                   double col_tol, double tol, double* y, int* certified,
                                   double* metrics6);

@@ -1,5 +1,5 @@
 """Matrix-free dual repair on the device (igaos_pdhg_dual_repair_device), the
-solve loop's repair step for LPs above the dense repair's m <= 4096.
+solve loop's repair step at every m.
 
 The reference's dual_repair (src/pdhg/pdhg.cu:288-448) needs a dense m x m
 Cholesky factor; the device path projects onto the same three sets
@@ -9,9 +9,9 @@ evaluate() (src/pdhg/pdhg.cu:173-254): every dual the device path reports
 certified has a finite gap <= tol at the candidate x.
 
 * LPs with a known optimal pair (x*, y*) and a perturbed dual (gap -inf):
-  certified at m = 3,000 (where the dense repair runs too) and m = 40,000.
-* Duals the dense repair certifies on the golden cases are certified by the
-  device path as well (at the reference's own gap, or 1e-6).
+  certified at m = 3,000 and m = 40,000.
+* Duals the reference's dense repair certifies on the golden cases are
+  certified by the device path as well (at the reference's own gap, or 1e-6).
 * A candidate off the feasible set is reported uncertified.
 * In a solve with m = 5,000 the scheduled repair step runs on the device and
   certifies the gap.
@@ -95,9 +95,9 @@ def test_device_repair_reports_uncertified_duals(native, orc):
     assert check["pinf"] == pytest.approx(mt["pinf"], rel=1e-9, abs=1e-15)
 
 
-def test_solve_above_dense_limit_certified_by_device_repair(native, orc):
-    """m = 5,000 (> 4,096): the solve loop's scheduled repair step runs on the
-    device and certifies the gap; the reported pair passes the oracle's
+def test_solve_certified_by_device_repair(native, orc):
+    """m = 5,000: the solve loop's scheduled repair step runs on the device
+    and certifies the gap; the reported pair passes the oracle's
     evaluate() at tol and the objective matches the known optimum."""
     from igaos_gb300 import capi
     lp, xs, ys = G.known_optimum_lp(5000, 12500, 10000, 0)
