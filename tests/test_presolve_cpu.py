@@ -258,6 +258,25 @@ def test_presolve_infeasibility_comes_with_a_dual_ray(native):
         assert capi.ray_certificate(lp, x, y)[0] == 1, (lp.rmin, lp.rmax, y)
 
 
+def test_parallel_rows_with_disjoint_ranges_come_with_a_dual_ray(native):
+    """x0 + x1 in [0, 1] and 2 x0 + 2 x1 in [4, 5] (x free): the second row
+    is twice the first, and in the first row's units it asks for [2, 2.5],
+    which misses [0, 1]. Presolve stops at the parallel-row merge; its ray
+    is +1 on the kept row and -1/2 on the other (A^T y = 0, bound 1 > 0).
+    The same with the ratio negative and with the other side crossing."""
+    from igaos_gb300 import capi
+    for vals, rmin, rmax in (([1.0, 1.0, 2.0, 2.0], [0.0, 4.0], [1.0, 5.0]),
+                             ([1.0, 1.0, -2.0, -2.0], [0.0, -5.0], [1.0, -4.0]),
+                             ([1.0, 1.0, 3.0, 3.0], [4.0, -3.0], [5.0, 6.0])):
+        lp = tiny([0, 0, 1, 1], [0, 1, 0, 1], vals, [1.0, 1.0], [-INF, -INF], [INF, INF],
+                  rmin, rmax)
+        P = capi.Presolved(lp)
+        assert P.outcome == "infeasible"
+        x, y = P.ray()
+        assert not x.any() and np.count_nonzero(y) == 2, y
+        assert capi.ray_certificate(lp, x, y)[0] == 1, (vals, rmin, rmax, y)
+
+
 def test_unbounded_column_ray_follows_substitutions(native):
     """min x2 + 0.5 x4 s.t. x1 + x2 + x4 = 2, x1 in [0, 5], x2 free, x4 >= 0:
     substituting the free singleton x2 leaves x4 empty at cost -0.5 with no
