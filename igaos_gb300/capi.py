@@ -18,6 +18,7 @@ LIB_PATH = os.environ.get("IGAOS_PDHG_LIB") or os.path.join(_PKG, "libigaos_pdhg
 OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_NODEVICE, ERR_NUMERIC, ERR_TIMEOUT = range(7)
 FP64, FP32_REFINE, FP32 = 0, 1, 2
 PRECISIONS = {"fp64": FP64, "fp32-refine": FP32_REFINE, "fp32": FP32}
+SCALINGS = {"ruiz": 0, "ruiz-pc": 1}
 STATUS_NAMES = ["optimal", "near-optimal", "feasible", "infeasible", "unbounded",
                 "iteration-limit", "time-limit", "error"]
 
@@ -33,6 +34,7 @@ class Options(C.Structure):
         ("check_period", C.c_int), ("inner_tolerance", C.c_double),
         ("max_refinements", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
         ("detect_infeasibility", C.c_int), ("pdhg_presolve", C.c_int), ("crossover", C.c_int),
+        ("scaling", C.c_int),
     ]
 
 
@@ -309,6 +311,8 @@ def default_options(**kw) -> Options:
         k = _ALIASES.get(k, k)
         if k == "precision" and isinstance(v, str):
             v = PRECISIONS[v]
+        if k == "scaling" and isinstance(v, str):
+            v = SCALINGS[v]
         if not hasattr(o, k):
             raise TypeError(f"unknown option {k!r}")
         setattr(o, k, v)

@@ -393,6 +393,9 @@ int igaos_pdhg_create(igaos_pdhg_problem** out, int m, int n, int64_t nnz, const
     *out = nullptr;
     return guarded([&] {
         validate(m, n, nnz, ap, ai, ax, cp, ci, acx, c, cl, cu, rmin, rmax);
+        if (opt && opt->scaling != IGAOS_PDHG_SCALING_RUIZ &&
+            opt->scaling != IGAOS_PDHG_SCALING_RUIZ_PC)
+            throw igx::CudaError(IGAOS_PDHG_ERR_INVALID, "unknown scaling");
         if (igaos_pdhg_device_count() == 0)
             throw igx::CudaError(IGAOS_PDHG_ERR_NODEVICE,
                                  "no CUDA device: PDHG engine unavailable");
@@ -425,7 +428,8 @@ int igaos_pdhg_create(igaos_pdhg_problem** out, int m, int n, int64_t nnz, const
                 p->eng = new igx::Engine(R.m, R.n, (int64_t)R.ai.size(), R.ap.data(),
                                          R.ai.data(), R.ax.data(), tcp.data(), tci.data(),
                                          tacx.data(), R.c.data(), R.cl.data(), R.cu.data(),
-                                         R.rmin.data(), R.rmax.data(), R.obj_const, dev);
+                                         R.rmin.data(), R.rmax.data(), R.obj_const, dev,
+                                         opt->scaling);
         } else {
             if (!cp) {
                 transpose_host(m, n, ap, ai, ax, tcp, tci, tacx);
@@ -434,7 +438,7 @@ int igaos_pdhg_create(igaos_pdhg_problem** out, int m, int n, int64_t nnz, const
                 acx = tacx.data();
             }
             p->eng = new igx::Engine(m, n, nnz, ap, ai, ax, cp, ci, acx, c, cl, cu, rmin, rmax,
-                                     obj_const, dev);
+                                     obj_const, dev, opt ? opt->scaling : IGAOS_PDHG_SCALING_RUIZ);
         }
         if (opt && opt->crossover && m <= igx::kCrossoverMaxRows) {
             p->xo = true;

@@ -193,8 +193,8 @@ static int grid_for(long long n, int per_block = kThreads, int cap = 152 * 16) {
 Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, const double* ax,
                const int* cp, const int* ci, const double* acx, const double* c,
                const double* cl, const double* cu, const double* rmin, const double* rmax,
-               double obj_const_, int device)
-    : m(m_), n(n_), nnz(nnz_), obj_const(obj_const_) {
+               double obj_const_, int device, int scaling)
+    : m(m_), n(n_), nnz(nnz_), obj_const(obj_const_), scaling_(scaling) {
     auto t_setup = std::chrono::steady_clock::now();
     if (device >= 0) CU(cudaSetDevice(device));
     CU(cudaGetDevice(&device_));
@@ -363,6 +363,13 @@ void Engine::setup_scaling() {
     for (int sweep = 0; sweep < 10; ++sweep) {
         k_ruiz_rows<<<sA_.ctas, kThreads, 0, st_>>>(sA_.view(), ap_, ai_, ax_, dc_, dr_);
         k_ruiz_cols<<<sAT_.ctas, kThreads, 0, st_>>>(sAT_.view(), cp_, ci_, acx_, dr_, dc_);
+    }
+    if (scaling_ == IGAOS_PDHG_SCALING_RUIZ_PC) {
+        k_pc_sums<<<sA_.ctas, kThreads, 0, st_>>>(sA_.view(), ap_, ai_, ax_, dr_, dc_, 1, tmp_m_);
+        k_pc_sums<<<sAT_.ctas, kThreads, 0, st_>>>(sAT_.view(), cp_, ci_, acx_, dr_, dc_, 0,
+                                                   tmp_n_);
+        k_pc_apply<<<grid_for(m), kThreads, 0, st_>>>(m, tmp_m_, 1, dr_);
+        k_pc_apply<<<grid_for(n), kThreads, 0, st_>>>(n, tmp_n_, 0, dc_);
     }
     k_fix_scale<<<grid_for(m), kThreads, 0, st_>>>(m, dr_);
     k_fix_scale<<<grid_for(n), kThreads, 0, st_>>>(n, dc_);

@@ -124,7 +124,7 @@ class Engine {
     Engine(int m, int n, long long nnz, const int* ap, const int* ai, const double* ax,
            const int* cp, const int* ci, const double* acx, const double* c,
            const double* cl, const double* cu, const double* rmin, const double* rmax,
-           double obj_const, int device);
+           double obj_const, int device, int scaling = IGAOS_PDHG_SCALING_RUIZ);
     ~Engine();
 
     void solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x, double* y);
@@ -247,6 +247,7 @@ class Engine {
     void download_ctl();
     double elapsed() const;
     void setup_scaling();
+    int scaling_ = IGAOS_PDHG_SCALING_RUIZ;  // igaos_pdhg_options.scaling
     void power_iteration();
     void solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x, double* y);
 };

@@ -35,7 +35,8 @@ void usage() {
         "  --verbose               engine progress to stderr (repeat for more)\n"
         "  --detect-infeasibility  stop with infeasible/unbounded on a ray certificate\n"
         "  --pdhg-presolve         reduce the LP on the host first (exact dual postsolve)\n"
-        "  --crossover             finish at an optimal vertex (host simplex, m <= 2048)\n");
+        "  --crossover             finish at an optimal vertex (host simplex, m <= 2048)\n"
+        "  --scaling <s>           ruiz|ruiz-pc (default ruiz; ruiz-pc adds a Pock-Chambolle pass)\n");
 }
 
 struct Args {
@@ -45,6 +46,7 @@ struct Args {
     bool detect = false;
     bool reduce = false;
     bool xo = false;
+    int scaling = IGAOS_PDHG_SCALING_RUIZ;
     bool ok = true;
 };
 
@@ -69,6 +71,12 @@ Args parse(int argc, char** argv) {
         else if (f == "--detect-infeasibility") a.detect = true;
         else if (f == "--pdhg-presolve") a.reduce = true;
         else if (f == "--crossover") a.xo = true;
+        else if (f == "--scaling" && has) {
+            const std::string s = argv[++i];
+            if (s == "ruiz") a.scaling = IGAOS_PDHG_SCALING_RUIZ;
+            else if (s == "ruiz-pc") a.scaling = IGAOS_PDHG_SCALING_RUIZ_PC;
+            else a.ok = false;
+        }
         else if (f == "--out" && has) a.out = argv[++i];
         else if (f == "--engine" && has) {
             a.engine = argv[++i];
@@ -193,13 +201,15 @@ int main(int argc, char** argv) {
     }
     if (a.cmd == "info") return info(M);
     igaos::Solution s;
-    if (a.engine == "pdhg" && (a.precision != IGAOS_PDHG_FP64 || a.detect || a.reduce || a.xo)) {
+    if (a.engine == "pdhg" && (a.precision != IGAOS_PDHG_FP64 || a.detect || a.reduce || a.xo ||
+                               a.scaling != IGAOS_PDHG_SCALING_RUIZ)) {
         igaos_pdhg_options o;
         igaos_pdhg_default_options(&o);
         o.precision = a.precision;
         o.detect_infeasibility = a.detect ? 1 : 0;
         o.pdhg_presolve = a.reduce ? 1 : 0;
         o.crossover = a.xo ? 1 : 0;
+        o.scaling = a.scaling;
         s = igaos::pdhg::solve_ex(M, a.opts, &o);
     } else {
         s = igaos::solve_with_engine(M, a.opts, a.engine);

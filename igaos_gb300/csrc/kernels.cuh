@@ -313,6 +313,44 @@ __global__ void __launch_bounds__(kThreads) k_ruiz_cols(WarpSched ws, const int*
     }
 }
 
+// Pock-Chambolle pass (alpha = 1) after Ruiz, opt-in (no reference
+// counterpart: the reference scales by Ruiz alone, src/pdhg/pdhg.cu:472-498).
+// sum[r] = sum over row r of |a_rj| dc_j / dr_r for rows of A (rowmajor = 1)
+// or over column r of |a_ir| dc_r / dr_i (rowmajor = 0), on the warp schedule
+// of that orientation; both sums come from the same scaled matrix.
+__global__ void __launch_bounds__(kThreads) k_pc_sums(WarpSched ws, const int* __restrict__ ptr,
+                                                        const int* __restrict__ idx,
+                                                        const double* __restrict__ val,
+                                                        const double* __restrict__ dr,
+                                                        const double* __restrict__ dc, int rowmajor,
+                                                        double* __restrict__ sum) {
+    const int lane = threadIdx.x & 31;
+    for (int w = blockIdx.x * kWarps + (threadIdx.x >> 5); w < ws.nwarps; w += gridDim.x * kWarps) {
+        const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
+        const int lg = __ldg(ws.lg + w), G = 1 << lg, gl = lane & (G - 1);
+        const int r = r0 + (lane >> lg);
+        double s = 0.0;
+        if (r < r1) {
+            for (int p = ptr[r] + gl; p < ptr[r + 1]; p += G) {
+                const int k = idx[p];
+                s += rowmajor ? fabs(val[p]) * dc[k] / dr[r] : fabs(val[p]) * dc[r] / dr[k];
+            }
+        }
+        for (int o = G >> 1; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o, G);
+        if (r < r1 && gl == 0) sum[r] = s;
+    }
+}
+
+// d *= sqrt(sum) (rows, mul = 1) or d /= sqrt(sum) (columns, mul = 0) where
+// the sum is positive and finite (empty rows and columns keep their factor).
+__global__ void k_pc_apply(int n, const double* __restrict__ sum, int mul, double* __restrict__ d) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const double s = sum[i];
+        if (!(s > 0) || !isfinite(s)) continue;
+        d[i] = mul ? d[i] * sqrt(s) : d[i] / sqrt(s);
+    }
+}
+
 __global__ void k_fill(int n, double v, double* __restrict__ out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         out[i] = v;

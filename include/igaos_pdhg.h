@@ -26,7 +26,7 @@
 extern "C" {
 #endif
 
-#define IGAOS_PDHG_ABI_VERSION 3
+#define IGAOS_PDHG_ABI_VERSION 4
 
 /* Return codes of every entry point. */
 enum {
@@ -106,7 +106,22 @@ typedef struct igaos_pdhg_options {
      * NEAR_OPTIMAL). Read by igaos_pdhg_create. 0 (default): off. Added in
      * ABI 3. */
     int crossover;
+    /* Diagonal scaling of the LP before the iterations:
+     * IGAOS_PDHG_SCALING_RUIZ (0, default): 10 Ruiz sweeps, as the reference
+     * (src/pdhg/pdhg.cu:472-492, cost scale 1 at :494-498).
+     * IGAOS_PDHG_SCALING_RUIZ_PC (1): the same sweeps, then one
+     * Pock-Chambolle pass with alpha = 1 (rows divided by the square root of
+     * their scaled 1-norm, columns likewise, both from the same matrix), the
+     * scaling of PDLP (Applegate et al. 2021). Read by igaos_pdhg_create.
+     * Added in ABI 4. */
+    int scaling;
 } igaos_pdhg_options;
+
+/* Values of igaos_pdhg_options.scaling. */
+enum {
+    IGAOS_PDHG_SCALING_RUIZ = 0,
+    IGAOS_PDHG_SCALING_RUIZ_PC = 1
+};
 
 typedef struct igaos_pdhg_result {
     int status;               /* IGAOS_STATUS_* */

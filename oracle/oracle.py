@@ -412,3 +412,22 @@ def ref_pdhg_solve(lp: LP, tolerance=1e-4, time_limit=120.0, max_iterations=5000
     return dict(status_name=STATUS_NAMES.get(st, "exception"), objective=out[0],
                 pinf=out[1], dinf=out[2], gap=out[3], iterations=int(out[4]),
                 loop_ms=out[5], wall_ms=out[6], x=x, y=y, message=msg.value.decode())
+
+
+def pock_chambolle(lp: LP, dr, dc):
+    """One Pock-Chambolle pass with alpha = 1 (Pock & Chambolle 2011, as PDLP
+    applies it after Ruiz; the reference has no such pass): on the scaled
+    matrix a~_ij = a_ij dc_j / dr_i, rows are divided by the square root of
+    their 1-norm and columns likewise, both norms taken from the same matrix.
+    Returns the new (dr, dc); rows and columns with no positive finite norm
+    keep their factor."""
+    dr, dc = f64(dr).copy(), f64(dc).copy()
+    rows = np.repeat(np.arange(lp.m), np.diff(lp.ap))
+    v = np.abs(lp.ax) * dc[lp.ai] / dr[rows]
+    rs = np.bincount(rows, weights=v, minlength=lp.m)
+    cs = np.bincount(lp.ai, weights=v, minlength=lp.n)
+    ok_r = (rs > 0) & np.isfinite(rs)
+    ok_c = (cs > 0) & np.isfinite(cs)
+    dr[ok_r] *= np.sqrt(rs[ok_r])
+    dc[ok_c] /= np.sqrt(cs[ok_c])
+    return dr, dc

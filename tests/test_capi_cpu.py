@@ -30,7 +30,7 @@ def test_exports_every_declared_symbol(native):
 def test_abi_version_and_defaults(native):
     import ctypes as C
     from igaos_gb300 import capi
-    assert native.igaos_pdhg_abi_version() == 3
+    assert native.igaos_pdhg_abi_version() == 4
     o = capi.default_options()
     # igaos::Options defaults (reference include/igaos/options.h:5-13)
     assert o.time_limit_s == 120.0 and o.tolerance == 1e-4 and o.max_iterations == 500000
@@ -39,7 +39,8 @@ def test_abi_version_and_defaults(native):
     assert o.detect_infeasibility == 0  # off, as the reference engine
     assert o.pdhg_presolve == 0  # off: the reference engine ignores `presolve`
     assert o.crossover == 0
-    assert C.sizeof(o) == 80  # ABI 3 layout of igaos_pdhg_options
+    assert o.scaling == capi.SCALINGS["ruiz"]  # the reference's Ruiz scaling alone
+    assert C.sizeof(o) == 88  # ABI 4 layout of igaos_pdhg_options
 
 
 def _tiny():
