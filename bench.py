@@ -273,8 +273,10 @@ def main():
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the LP (testing only)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true", help="skip the cpu_baseline sample")
-    ap.add_argument("--probe", choices=["batch", "layer"], default=None,
-                    help="run only that extra workload and print its JSON (profiling)")
+    ap.add_argument("--probe", choices=["batch", "layer", "attempts-c5"], default=None,
+                    help="run only that extra workload and print its JSON (profiling); "
+                         "attempts-c5: --iters iterations of the multicommodity LP at "
+                         "--precision, after one warming solve of the same length")
     ap.add_argument("--batch-count", type=int, default=4096,
                     help="LPs in the batched workload (smaller for profiling)")
     ap.add_argument("--batch-sample", type=int, default=24,
@@ -303,6 +305,22 @@ def main():
         td.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     from igaos_gb300 import capi
+    if args.probe == "attempts-c5":  # fixed-length solves of the multicommodity LP
+        flp = G.config5(seed=0)
+        cb = bytes_per_attempt(flp.m, flp.n, flp.nnz, 8 if args.precision == "fp64" else 4)
+        with capi.Problem(flp, device=local) as P:
+            o = dict(precision=args.precision, tolerance=1e-12, time_limit=1e9,
+                     max_iterations=args.iters)
+            P.solve(**o)
+            r = P.solve(**o)
+        us = 1e3 * r["attempt_time_ms"] / max(1, r["attempts"])
+        pk, pk_kind = peaks()
+        print(json.dumps({"workload": f"multicommodity flow m={flp.m} n={flp.n} nnz={flp.nnz}",
+                          "precision": args.precision, "iterations": r["iterations"],
+                          "attempts": r["attempts"], "attempt_us": us, "attempt_bytes": cb,
+                          "attempt_hbm_frac": cb / (us * 1e-6) / 1e9 / pk,
+                          "hbm_peak_kind": pk_kind}), flush=True)
+        return
     if args.probe:  # one extra workload alone (profiling runs)
         res = batch_probe(capi, G, sample=args.batch_sample, count=args.batch_count,
                           warm=False) if args.probe == "batch" else layer_probe(torch, G)

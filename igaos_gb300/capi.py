@@ -47,7 +47,7 @@ class Result(C.Structure):
         ("refinements", C.c_int), ("solve_time_ms", C.c_double),
         ("setup_time_ms", C.c_double), ("device_time_ms", C.c_double),
         ("attempt_time_ms", C.c_double), ("launches", C.c_int64),
-        ("message", C.c_char * 160),
+        ("rollbacks", C.c_int64), ("message", C.c_char * 160),
     ]
 
     def as_dict(self):

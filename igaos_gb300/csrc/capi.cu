@@ -223,6 +223,7 @@ int solve_presolved(igaos_pdhg_problem* p, const igaos_pdhg_options& o, igaos_pd
         res->device_time_ms += rr.device_time_ms;
         res->attempt_time_ms += rr.attempt_time_ms;
         res->launches += rr.launches;
+        res->rollbacks += rr.rollbacks;
         if (round == 0) res->setup_time_ms += rr.setup_time_ms;
         if (rr.status == IGAOS_STATUS_INFEASIBLE || rr.status == IGAOS_STATUS_UNBOUNDED) {
             // a ray of the reduced LP: mapped to the original and checked there

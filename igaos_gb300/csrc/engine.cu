@@ -952,7 +952,7 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
     double epoch_kkt = -1.0, prev_cand = kInf;
     long long epoch_start = 0, last_rollback = 0;
     long long next_repair = 5000, repair_spacing = 2000;  // src/pdhg/pdhg.cu:741-743
-    bool have_pe = false, have_last = false, have_inc = false;
+    bool have_pe = false, have_last = false, have_inc = false, perturbed = false;
     int ray_prev = 0;  // certificate kind found at the previous restart
     double inc_op = 0.0;
     DevMetrics inc{};
@@ -974,6 +974,11 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
         if (k_done % CHECK == 0) {
             ++out.checks;
             const int p = h_ctl_->parity;
+            if (o.perturb_at > 0 && k_done >= o.perturb_at && !perturbed) {
+                k_add_const<T><<<grid_for(n), kThreads, 0, st_>>>(n, (T)1e6, w.x[p]);
+                CU(cudaGetLastError());
+                perturbed = true;
+            }
             if (anch) {  // FP64 metrics of the full iterates anchor + delta
                 anchor_full(p);
                 kkt<double>(base_, anc_.xf[0], anc_.yf[0], anc_.xf[1], anc_.yf[1], 2);
@@ -1039,6 +1044,10 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
                 epoch_kkt = -1.0;
                 prev_cand = kInf;
                 last_rollback = k_done;
+                ++out.rollbacks;
+                if (o.verbosity > 1)
+                    std::fprintf(stderr, "[pdhg-gb300] rollback @k=%lld to the incumbent, eta %.6e\n",
+                                 k_done, h_ctl_->eta);
             }
             // restart + primal weight (src/pdhg/pdhg.cu:1001-1075)
             const double cand = std::min(ec, ea);
@@ -1216,6 +1225,7 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     lo.eta_init = eta0;
     lo.eta0 = eta0;
     lo.omega_init = omega0;
+    if (const char* e = std::getenv("IGAOS_PDHG_PERTURB_AT")) lo.perturb_at = std::atoll(e);
     LoopOut out;
     std::vector<double> hx(n), hy(m);
     if (o.precision == IGAOS_PDHG_FP32) {
@@ -1255,6 +1265,7 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     r.attempts = out.attempts;
     r.kkt_checks = out.checks;
     r.restarts = out.restarts;
+    r.rollbacks = out.rollbacks;
     r.kkt_passes = out.spmvs / 2;
     r.solve_time_ms = secs * 1000.0;
     if (out.numeric_failure) {
@@ -1540,6 +1551,7 @@ void Engine::solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, dou
     lo.eta_init = eta0;
     lo.eta0 = eta0;
     lo.omega_init = omega0;
+    if (const char* e = std::getenv("IGAOS_PDHG_PERTURB_AT")) lo.perturb_at = std::atoll(e);
     LoopOut out = loop<float>(av_, lo);
     // the answer: incumbent, or anchor + delta of the current / averaged iterate
     const double *fx, *fy;
@@ -1572,6 +1584,7 @@ void Engine::solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, dou
     r.attempts = out.attempts;
     r.kkt_checks = out.checks;
     r.restarts = out.restarts;
+    r.rollbacks = out.rollbacks;
     r.kkt_passes = out.spmvs / 2;
     r.refinements = (int)out.anchors;
     if (out.numeric_failure) {

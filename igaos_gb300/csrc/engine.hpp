@@ -104,6 +104,11 @@ struct LoopOpts {
     bool graphs = true;
     bool detect_inf = false;  // infeasibility certificates at restarts
     double eta_init = 1, omega_init = 1, eta0 = 1;
+    // testing knob (IGAOS_PDHG_PERTURB_AT): at the first KKT check at or after
+    // this iteration, 1e6 is added to every entry of the current x before its
+    // metrics are taken, a blown-up state that exercises the rollback to the
+    // incumbent (src/pdhg/pdhg.cu:965-988). 0: never.
+    long long perturb_at = 0;
 };
 
 struct LoopOut {
@@ -111,6 +116,7 @@ struct LoopOut {
     DevMetrics last{};
     bool last_is_avg = false, use_inc = false;
     long long iters = 0, attempts = 0, checks = 0, restarts = 0, spmvs = 0, anchors = 0;
+    long long rollbacks = 0;
     double eta = 0, omega = 0;
     int parity = 0;
     bool numeric_failure = false;

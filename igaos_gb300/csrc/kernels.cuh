@@ -479,6 +479,12 @@ __global__ void k_diffnorms(int n, const T* __restrict__ x, const T* __restrict_
     }
 }
 
+template <typename T>
+__global__ void k_add_const(int n, T v, T* __restrict__ x) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+        x[i] += v;
+}
+
 template <typename TI, typename TO>
 __global__ void k_convert(int n, const TI* __restrict__ in, TO* __restrict__ out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)

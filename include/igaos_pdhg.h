@@ -139,6 +139,8 @@ typedef struct igaos_pdhg_result {
     double device_time_ms;    /* solve, CUDA events on the engine stream */
     double attempt_time_ms;   /* of which in line-search attempt launches */
     int64_t launches;         /* engine kernel launches during the solve */
+    int64_t rollbacks;        /* restores of the incumbent after a blow-up
+                                 (src/pdhg/pdhg.cu:965-988); added in ABI 4 */
     char message[160];
 } igaos_pdhg_result;
 

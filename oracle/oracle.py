@@ -68,7 +68,7 @@ class orc_options(C.Structure):
     _fields_ = [
         ("time_limit_s", C.c_double), ("tolerance", C.c_double),
         ("max_iterations", C.c_int64), ("check_period", C.c_int),
-        ("threads", C.c_int), ("verbosity", C.c_int),
+        ("threads", C.c_int), ("verbosity", C.c_int), ("perturb_at", C.c_int64),
     ]
 
 
@@ -79,7 +79,7 @@ class orc_result(C.Structure):
         ("iterations", C.c_int64), ("attempts", C.c_int64),
         ("restarts", C.c_int64), ("checks", C.c_int64),
         ("seconds", C.c_double), ("loop_seconds", C.c_double),
-        ("eta", C.c_double), ("omega", C.c_double),
+        ("eta", C.c_double), ("omega", C.c_double), ("rollbacks", C.c_int64),
     ]
 
 
@@ -268,8 +268,9 @@ def iterate(lp: LP, sd, state: dict, iters: int, threads=1):
 
 
 def pdhg_solve(lp: LP, tolerance=1e-4, time_limit=120.0, max_iterations=500000,
-               threads=1, check_period=64, verbosity=0):
-    o = orc_options(time_limit, tolerance, max_iterations, check_period, threads, verbosity)
+               threads=1, check_period=64, verbosity=0, perturb_at=0):
+    o = orc_options(time_limit, tolerance, max_iterations, check_period, threads, verbosity,
+                    perturb_at)
     r = orc_result()
     x = np.zeros(lp.n); y = np.zeros(lp.m)
     s = lp.as_c()

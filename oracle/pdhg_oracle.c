@@ -43,6 +43,7 @@ void orc_default_options(orc_options* o) {
     o->check_period = 64;
     o->threads = 1;
     o->verbosity = 0;
+    o->perturb_at = 0;
 }
 
 /* ---------------------------------------------------------------- evaluate
@@ -474,7 +475,8 @@ int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
     double epoch_kkt = -1.0, prev_cand = ORC_INF;
     int64_t epoch_start = 0;
     int have_pe = 0;
-    int64_t iters_run = 0, attempts = 0, restarts = 0, checks = 0;
+    int64_t iters_run = 0, attempts = 0, restarts = 0, checks = 0, rollbacks = 0;
+    int perturbed = 0;
     int timed_out = 0;
     orc_metrics last, inc;
     memset(&last, 0, sizeof(last));
@@ -502,6 +504,10 @@ int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
                                   sacx, sc, scl, scu, srmin, srmax, &st, &w, th);
         if (k % CHECK != 0) continue;
         ++checks;
+        if (opt->perturb_at > 0 && k >= opt->perturb_at && !perturbed) {
+            for (int j = 0; j < n; ++j) st.x[j] += 1e6;
+            perturbed = 1;
+        }
         orc_metrics mc, ma;
         METRICS_OF(st.x, st.y, mc);
         METRICS_OF(st.xavg, st.yavg, ma);
@@ -550,6 +556,7 @@ int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
             prev_cand = ORC_INF;
             orc_spmv(m, lp->ap, lp->ai, sax, st.x, st.axcur, th);
             last_rollback = k;
+            ++rollbacks;
         }
         /* restart + primal weight, reference :1001-1075 */
         const double cand = smin(ec, ea);
@@ -636,6 +643,7 @@ int orc_pdhg_solve(const orc_lp* lp, const orc_options* opt, orc_result* res,
     res->iterations = iters_run;
     res->attempts = attempts;
     res->restarts = restarts;
+    res->rollbacks = rollbacks;
     res->checks = checks;
     res->seconds = secs;
     res->loop_seconds = now_s() - t_loop;

@@ -45,6 +45,10 @@ typedef struct {
     int check_period; /* 64 in the reference */
     int threads;      /* OpenMP threads for SpMV / vector loops (1 = serial) */
     int verbosity;
+    /* test perturbation: at the first check at or after this iteration, 1e6
+     * is added to every entry of the current (scaled) x before its metrics
+     * are taken, as the engine's IGAOS_PDHG_PERTURB_AT does; 0: never */
+    int64_t perturb_at;
 } orc_options;
 
 typedef struct {
@@ -54,6 +58,7 @@ typedef struct {
     double seconds;      /* power iteration + iteration loop */
     double loop_seconds; /* iteration loop only */
     double eta, omega; /* final step controller state (scaled units) */
+    int64_t rollbacks; /* incumbent restores (reference :965-988) */
 } orc_result;
 
 /* reference src/pdhg/pdhg.cu:173-254 */

@@ -51,7 +51,8 @@ def load_case(name):
         lp, exact, _ = MN.load(name[len("netlib-"):])
         return lp, exact
     if name == "c1-s0":
-        return O.lp_from(G.config1(seed=0)), None
+        c1 = json.load(open(os.path.join(GOLD, "c1_objectives.json")))["c1-s0"]
+        return O.lp_from(G.config1(seed=0)), c1["simplex_objective"]
     e = json.load(open(os.path.join(GOLD, "lp_objectives.json")))[name]
     return O.lp_from(MG.make_lp(e["generator"], e["kwargs"])), e["simplex_objective"]
 

@@ -7,7 +7,9 @@ and the engine adds none.
 
 Checked through the C ABI against the existing entry point
 igaos_pdhg_evaluate on the same candidates, twice in a row (the scratch array
-is shared between calls and keeps the previous call's contents). This file
+is shared between calls and keeps the previous call's contents), and against
+the oracle's restatement of the reference evaluate() (src/pdhg/pdhg.cu:
+173-254) on A x and c + A^T y formed in FP64 by numpy. This file
 sorts last so that a run stopping at the first failure has run every other
 test first; it also passes alone in a fresh process.
 """
@@ -36,7 +38,8 @@ def _candidates(lp, seed):
     return out
 
 
-def test_noalloc_evaluate_matches_evaluate_twice(native):
+def test_noalloc_evaluate_matches_evaluate_twice(native, orc):
+    import scipy.sparse as sp
     import torch
     from igaos_gb300 import capi, generators as G
     assert torch.cuda.is_available()
@@ -52,9 +55,12 @@ def test_noalloc_evaluate_matches_evaluate_twice(native):
             t[k] = t[k].to(torch.int32)
         out = torch.empty(6, dtype=torch.float64, device=dev)
         stream = torch.cuda.current_stream(dev).cuda_stream
+        olp = orc.lp_from(prob)
+        A = sp.csr_matrix((olp.ax, olp.ai, olp.ap), shape=(olp.m, olp.n))
         with capi.Problem(prob) as P:
             for x, y in _candidates(prob, 7):
                 want = P.evaluate(x, y)
+                ref = orc.evaluate(olp, x, y, A @ x, olp.c + A.T @ y)
                 tx = torch.as_tensor(x, dtype=torch.float64, device=dev)
                 ty = torch.as_tensor(y, dtype=torch.float64, device=dev)
                 got_runs = []
@@ -73,10 +79,11 @@ def test_noalloc_evaluate_matches_evaluate_twice(native):
                 assert got_runs[0] == got_runs[1]  # deterministic, scratch reuse is clean
                 got = got_runs[0]
                 for k in ("pinf", "prow", "dinf", "op", "od", "gap"):
-                    if np.isinf(want[k]):
-                        assert got[k] == want[k], k
-                    else:
-                        assert got[k] == pytest.approx(want[k], rel=1e-9, abs=1e-9), (k, got[k], want[k])
+                    for w in (want, ref):
+                        if np.isinf(w[k]):
+                            assert got[k] == w[k], k
+                        else:
+                            assert got[k] == pytest.approx(w[k], rel=1e-9, abs=1e-9), (k, got[k], w[k])
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(native):
