@@ -3,43 +3,44 @@
 Workload (one step): the large sparse LP (m=200,000 rows, half equality half
 <=, n=500,000 box-bounded columns, ~5.2M nonzeros with Zipf(1.5) column
 degrees and |A_ij| log-uniform in [1e-3, 1e3]; seeded synthetic data), one
-solve call of ITERS accepted PDHG iterations with FP32 attempts and FP64
-refinement (FP64 anchors re-set at restarts, FP64 KKT checks every 64
-iterations), from a cold start on device-resident data.
+solve call of ITERS accepted PDHG iterations in FP64 -- the reference's
+arithmetic (FP64 attempts, FP64 KKT checks every 64 iterations, restarts,
+primal weight) -- from a cold start on device-resident data.
 
-Also reported (extra keys): time to 1e-8 relative KKT on the small random LP
-(m=2,000, n=5,000) for FP32+refine vs plain FP64 and the CPU oracle, where
-all of them converge; the large LP is not solved to 1e-8 by either
-precision in a bench-sized budget (see --tol-probe). With it,
-`crossover_from_fp32_refine`: the host crossover (igaos_pdhg_crossover) from
-the FP32+refine answer to an optimal vertex, wall time and pivots.
-`time_to_1e-8_multicommodity_lp`: the same comparison on the 1.08M x 2.87M
-multicommodity-flow LP. `batched_small_lps`:
-4,096 uneven small LPs solved to 1e-6 in one persistent launch vs
-sequential single-LP solves. `differentiable_layer`: forward and adjoint
-backward through 1,000 unrolled iterations of 256 ridge-regularised LPs.
-
-value: SpMV GB/s -- algorithmic bytes of every fused A^T y / A xbar attempt
-of the solve divided by the solve's CUDA-event device time (checks, restarts
-and host round trips included). Algorithmic bytes per attempt (s = 4 for
-FP32, 8 for FP64; int32 indices):
+value: SpMV GB/s of the FP64 attempts -- algorithmic bytes of every fused
+A^T y / A xbar attempt of the solve divided by the solve's CUDA-event device
+time (checks, restarts and host round trips included). Algorithmic bytes per
+attempt (s = 8 for FP64, 4 for FP32; int32 indices):
     2*nnz*(s+4) + 4*(m+n+2) + s*9*(m+n)
 (each matrix entry and index once per orientation, row/column pointers once,
 nine m- and nine n-vectors read or written once each: x, xavg, c, l, u, xbar
 and y, A x, yavg, rmin, rmax gathered/read; x', xavg', xbar, y', A x', yavg'
-written).
-roofline: the fused attempt's algorithmic bytes over its CUDA-event time
-against the measured HBM copy bandwidth; `roofline.l2` adds the bound that
-limits it on this LP, whose working set nearly fits L2: L1-miss sectors per
-attempt (committed ncu summary) per second against the device's random
-4-byte read rate of a 2 MB vector (igaos_pdhg_gather_rate, measured in the
-same run). The multicommodity extra reports `attempt_us` and
-`attempt_hbm_frac` for an LP that streams from HBM.
+written). The reference arm and cpu_baseline measure the same FP64 metric
+(the CPU oracle of the reference FP64 PDHG on the host cores), so the ratio
+of the two lines is at equal arithmetic.
+roofline: the FP64 attempt's algorithmic bytes over its CUDA-event time
+against the measured HBM copy bandwidth, with ncu DRAM traffic per attempt
+from the committed summary. `fp32_refine`: the same solve with FP32 attempts
+and FP64 refinement (GB/s, attempt time, its rooflines: HBM and L2's
+random-sector rate).
 e2e: the same metric through the C ABI with HOST buffers: igaos_pdhg_solve_csr
 (upload, device setup, solve, download, free) timed on the host.
-L2: flushed (512 MiB write) between steps. Reference arm and cpu_baseline:
-the CPU oracle of the reference FP64 PDHG (tests' checker) on the machine's host
-cores over a bounded sample of the same solve.
+L2: flushed (512 MiB write) between steps.
+
+Time-to-tolerance keys (relative KKT of the original LP, FP64 metrics):
+`time_to_tol_small_lp` (m 2,000, n 5,000): FP32 + refinement and FP64 to 1e-4
+and 1e-8 and the CPU oracle at 1e-8. `time_to_tol_multicommodity_lp` (m
+1,078,800, n 2,870,400): both precisions to 1e-4 and 1e-8, with attempt_us /
+attempt_hbm_frac (this LP streams from HBM). `time_to_tol_large_lp`: this
+workload to 1e-4 (FP32 + refinement with the opt-in Pock-Chambolle scaling;
+FP64 with the reference's scaling and with it), each within a stated budget,
+with the KKT reached. `vs_reference_gpu`: the reference's own GPU PDHG
+(cuSPARSE path, compiled from its sources into oracle/_ref, timed on this GPU
+in this process) beside this engine -- to 1e-4 and 1e-8 on the small LP, and
+over a fixed 4,992-iteration budget on the two large LPs (above 46,340 rows
+its dense dual repair, reached from iteration 5,000, overflows int32
+indices). Also `batched_small_lps` (4,096 uneven LPs to 1e-6 in one
+persistent launch vs sequential solves) and `differentiable_layer`.
 """
 from __future__ import annotations
 
@@ -259,6 +260,153 @@ def config_dict(lp, args):
             "parallelism": f"replicas x{args.gpus}"}
 
 
+def tol_entry(r, wall_s=None):
+    """Time-to-tolerance record of one engine solve (device-resident data:
+    `loop_s` is the solve loop's wall time, setup excluded; `wall_s`, when
+    given, a whole C-ABI call with host buffers)."""
+    d = {"status": r["status_name"], "loop_s": r["solve_time_ms"] / 1e3,
+         "device_s": r["device_time_ms"] / 1e3, "iterations": r["iterations"],
+         "objective": r["objective"], "pinf": r["pinf"], "dinf": r["dinf"],
+         "rel_gap": r["rel_gap"], "prow": r["prow"]}
+    if wall_s is not None:
+        d["wall_s"] = wall_s
+    return d
+
+
+def ref_gpu(lp, tol, time_limit, max_iterations=500000):
+    """The reference's own GPU PDHG (oracle/_ref, compiled from its sources)
+    on `lp`: loop_s is its own loop timer (setup excluded), wall_s the whole
+    call (handles, Ruiz, upload, power iteration, loop, download)."""
+    from oracle import oracle as O
+    r = O.ref_pdhg_solve(O.lp_from(lp), tolerance=tol, time_limit=time_limit,
+                         max_iterations=max_iterations)
+    return {"status": r["status_name"], "loop_s": r["loop_ms"] / 1e3, "wall_s": r["wall_ms"] / 1e3,
+            "iterations": r["iterations"], "objective": r["objective"], "pinf": r["pinf"],
+            "dinf": r["dinf"], "rel_gap": r["gap"], "message": r["message"]}
+
+
+def ref_gpu_ready():
+    try:
+        from oracle import oracle as O
+        return O.ref_pdhg_available()
+    except Exception:
+        return False
+
+
+def rel_diff(a, b):
+    return abs(a - b) / max(1.0, abs(b))
+
+
+def small_lp_probe(capi, G, local):
+    """Small random LP (m 2,000, n 5,000, seed 0): FP32 + refinement and FP64
+    to 1e-4 and 1e-8 (device-resident), and the CPU oracle at 1e-8."""
+    slp = G.config1(seed=0)
+    out = {"workload": f"small random LP m={slp.m} n={slp.n} nnz={slp.nnz} (seed 0)"}
+    x_last = None
+    with capi.Problem(slp, device=local) as P:
+        for prec in ("fp64", "fp32-refine"):
+            P.solve(precision=prec, tolerance=1e-6, time_limit=60.0)  # warm
+            for tol in (1e-4, 1e-8):
+                r = P.solve(precision=prec, tolerance=tol, time_limit=60.0)
+                out[f"{prec}@{tol:g}"] = tol_entry(r)
+                if prec == "fp32-refine" and tol == 1e-8:
+                    x_last = r["x"]
+    for tol in (1e-4, 1e-8):
+        a, b = out[f"fp64@{tol:g}"], out[f"fp32-refine@{tol:g}"]
+        if a["status"] == b["status"] == "near-optimal":
+            out[f"speedup_fp32_refine_vs_fp64@{tol:g}"] = a["loop_s"] / b["loop_s"]
+    try:  # host crossover from the FP32 + refinement answer (a probe)
+        t0 = time.perf_counter()
+        xv, _, _, xi = capi.crossover(slp, x_last)
+        out["crossover_from_fp32_refine"] = {
+            "status": xi["status"], "s": time.perf_counter() - t0, "pivots": xi["pivots"],
+            "objective": float(slp.c @ xv + slp.obj_const)}
+    except Exception as e:
+        out["crossover_from_fp32_refine"] = {"error": str(e)[:200]}
+    from oracle import oracle as O
+    rr = O.pdhg_solve(O.lp_from(slp), tolerance=1e-8, time_limit=120.0,
+                      threads=os.cpu_count() or 1)
+    out["cpu_oracle_fp64@1e-8"] = {"status": rr["status_name"], "s": rr["seconds"],
+                                   "iterations": rr["iterations"], "cores": os.cpu_count()}
+    return slp, out
+
+
+def c5_probe(capi, G, local):
+    """Multicommodity LP: both precisions to 1e-4 and 1e-8 (device-resident),
+    with the attempt time against the HBM roofline (this LP's working set
+    exceeds L2, so its attempts stream from HBM)."""
+    flp = G.config5(seed=0)
+    out = {"workload": f"multicommodity flow m={flp.m} n={flp.n} nnz={flp.nnz} (seed 0)"}
+    pk, pk_kind = peaks()
+    with capi.Problem(flp, device=local) as P:
+        for prec in ("fp32-refine", "fp64"):
+            cb = bytes_per_attempt(flp.m, flp.n, flp.nnz, 8 if prec == "fp64" else 4)
+            for tol in (1e-4, 1e-8):
+                r = P.solve(precision=prec, tolerance=tol, time_limit=240.0)
+                e = tol_entry(r)
+                us = 1e3 * r["attempt_time_ms"] / max(1, r["attempts"])
+                e.update(attempt_us=us, attempt_bytes=cb,
+                         attempt_hbm_frac=cb / (us * 1e-6) / 1e9 / pk, hbm_peak_kind=pk_kind)
+                out[f"{prec}@{tol:g}"] = e
+    for tol in (1e-4, 1e-8):
+        a, b = out[f"fp64@{tol:g}"], out[f"fp32-refine@{tol:g}"]
+        if a["status"] == b["status"] == "near-optimal":
+            out[f"speedup_fp32_refine_vs_fp64@{tol:g}"] = a["loop_s"] / b["loop_s"]
+            out[f"objective_rel_diff@{tol:g}"] = rel_diff(b["objective"], a["objective"])
+    return flp, out
+
+
+def c2_tol_probe(capi, lp, local, budget32, budget64):
+    """The large LP to 1e-4: FP32 + refinement with the opt-in Pock-Chambolle
+    scaling; FP64 with it and with the reference's Ruiz scaling alone; each
+    within its budget (seconds), reporting the KKT reached when it runs out."""
+    out = {"tolerance": 1e-4, "budget_s": {"fp32-refine": budget32, "fp64": budget64}}
+    with capi.Problem(lp, device=local, scaling="ruiz-pc") as P:
+        out["fp32-refine+pc"] = tol_entry(P.solve(precision="fp32-refine", tolerance=1e-4,
+                                                  time_limit=budget32))
+        out["fp64+pc"] = tol_entry(P.solve(precision="fp64", tolerance=1e-4, time_limit=budget64))
+    with capi.Problem(lp, device=local) as P:
+        out["fp64"] = tol_entry(P.solve(precision="fp64", tolerance=1e-4, time_limit=budget64))
+    return out
+
+
+def vs_reference_gpu(capi, local, slp, flp, lp):
+    """The reference's GPU PDHG beside this engine on the same GPU. Small LP:
+    both to 1e-4 and 1e-8 (loop time and whole-call wall time). Large LPs: a
+    fixed budget of 4,992 iterations (seconds per iteration, KKT reached)."""
+    out = {"engine": "reference src/pdhg/pdhg.cu (cuSPARSE/cuBLAS FP64), compiled from its "
+                     "sources, same GPU, same process"}
+    small = {}
+    for tol in (1e-4, 1e-8):
+        ref = ref_gpu(slp, tol, 120.0)
+        row = {"reference": ref}
+        for prec in ("fp64", "fp32-refine"):
+            t0 = time.perf_counter()
+            r = capi.solve_lp(slp, precision=prec, tolerance=tol, time_limit=120.0, device=local)
+            row[prec] = tol_entry(r, wall_s=time.perf_counter() - t0)
+            if ref["status"] == r["status_name"] == "near-optimal":
+                row[prec]["speedup_loop"] = ref["loop_s"] / row[prec]["loop_s"]
+                row[prec]["speedup_wall"] = ref["wall_s"] / row[prec]["wall_s"]
+                row[prec]["objective_rel_diff"] = rel_diff(r["objective"], ref["objective"])
+        small[f"s_to_{tol:g}"] = row
+    out["small_lp"] = small
+    for key, big in (("multicommodity_lp", flp), ("large_lp", lp)):
+        if big is None:
+            continue
+        ref = ref_gpu(big, 1e-12, 1e9, max_iterations=4992)
+        row = {"iterations": 4992, "reference": ref,
+               "reference_s_per_iteration": ref["loop_s"] / max(1, ref["iterations"])}
+        with capi.Problem(big, device=local) as P:
+            for prec in ("fp64", "fp32-refine"):
+                r = P.solve(precision=prec, tolerance=1e-12, time_limit=1e9, max_iterations=4992)
+                e = tol_entry(r)
+                e["s_per_iteration"] = e["loop_s"] / max(1, r["iterations"])
+                e["speedup_per_iteration"] = row["reference_s_per_iteration"] / e["s_per_iteration"]
+                row[prec] = e
+        out[key] = row
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -266,9 +414,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--iters", type=int, default=2048)
-    ap.add_argument("--precision", default="fp32-refine", choices=["fp32", "fp64", "fp32-refine"])
+    ap.add_argument("--precision", default="fp64", choices=["fp32", "fp64", "fp32-refine"],
+                    help="arithmetic of the headline steps (fp64: the reference's)")
     ap.add_argument("--no-small", action="store_true",
-                    help="skip the time-to-1e-8 comparison on the small LP")
+                    help="skip the time-to-tolerance comparison on the small LP")
     ap.add_argument("--cpu-iters", type=int, default=64)
     ap.add_argument("--scale", type=float, default=1.0, help="shrink the LP (testing only)")
     ap.add_argument("--no-e2e", action="store_true")
@@ -281,11 +430,15 @@ def main():
                     help="LPs in the batched workload (smaller for profiling)")
     ap.add_argument("--batch-sample", type=int, default=24,
                     help="sequential single-LP solves timed beside the batch (0: none)")
-    ap.add_argument("--no-c5", action="store_true", help="skip the multicommodity time-to-1e-8")
+    ap.add_argument("--no-c5", action="store_true", help="skip the multicommodity LP")
     ap.add_argument("--no-batch", action="store_true", help="skip the batched-LP comparison")
     ap.add_argument("--no-layer", action="store_true", help="skip the differentiable layer")
-    ap.add_argument("--tol-probe", type=float, default=0.0,
-                    help="also report time-to-tolerance probes within this many seconds")
+    ap.add_argument("--no-c2-tol", action="store_true", help="skip the large LP to 1e-4")
+    ap.add_argument("--no-ref-gpu", action="store_true",
+                    help="skip the reference GPU PDHG comparison")
+    ap.add_argument("--c2-budget", type=float, default=100.0,
+                    help="seconds for the FP32 + refinement solve of the large LP to 1e-4 "
+                         "(FP64 gets 0.6 of it)")
     args = ap.parse_args()
     args.warmup = max(3, args.warmup)
     ws, rank, local = dist()
@@ -327,23 +480,34 @@ def main():
         print(json.dumps(res), flush=True)
         return
     flush = torch.empty(512 << 20, dtype=torch.uint8, device="cuda")
-    opts = dict(precision=args.precision, tolerance=1e-12, time_limit=1e9,
-                max_iterations=args.iters, device=local)
-    bpa = bytes_per_attempt(lp.m, lp.n, lp.nnz, 8 if args.precision == "fp64" else 4)
+
+    def steps(P, prec, count, timed):
+        o = dict(precision=prec, tolerance=1e-12, time_limit=1e9, max_iterations=args.iters,
+                 device=local)
+        res = []
+        for _ in range(count):
+            if timed:
+                flush.fill_(1)
+                torch.cuda.synchronize()
+            res.append(P.solve(**o))
+        return res
+
+    alt = "fp32-refine" if args.precision == "fp64" else "fp64"
     with capi.Problem(lp, device=local) as P:
-        for _ in range(args.warmup):
-            P.solve(**opts)
+        steps(P, args.precision, args.warmup, False)
         clocks = Clocks(local)
         barrier(ws)
         torch.cuda.synchronize()
-        res = []
-        for _ in range(args.steps):
-            flush.fill_(1)
-            torch.cuda.synchronize()
-            res.append(P.solve(**opts))
+        res = steps(P, args.precision, args.steps, True)
         torch.cuda.synchronize()
         barrier(ws)
         ck = clocks.stop()
+        # the same steps in the other arithmetic (not part of `value`)
+        steps(P, alt, 1, False)
+        res_alt = steps(P, alt, min(3, args.steps), True)
+    s_main = 8 if args.precision == "fp64" else 4
+    bpa = bytes_per_attempt(lp.m, lp.n, lp.nnz, s_main)
+    bpa_alt = bytes_per_attempt(lp.m, lp.n, lp.nnz, 8 if alt == "fp64" else 4)
     dev_ms = sum(r["device_time_ms"] for r in res)
     att = sum(r["attempts"] for r in res)
     att_ms = sum(r["attempt_time_ms"] for r in res)
@@ -353,6 +517,8 @@ def main():
     # e2e through the C ABI with host buffers
     e2e = None
     if not args.no_e2e:
+        opts = dict(precision=args.precision, tolerance=1e-12, time_limit=1e9,
+                    max_iterations=args.iters, device=local)
         h2d = sum(np.asarray(a).nbytes for a in (lp.ap, lp.ai, lp.ax, lp.cp, lp.ci, lp.acx, lp.c,
                                                    lp.cl, lp.cu, lp.rmin, lp.rmax))
         d2h = 8 * (lp.m + lp.n)
@@ -368,106 +534,59 @@ def main():
         el = barrier_max(time.perf_counter() - t0, ws)
         e2e = {"value": ws * bpa * e_att / el / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d,
                "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * el / e_steps}
-    # time-to-tolerance probes (not part of `value`)
-    # Time to 1e-8 relative KKT, FP32 + FP64 refinement vs plain FP64 (the
-    # reference algorithm), on the small random LP (m=2,000, n=5,000,
-    # ~20k nnz) where both reach it; device-resident, CUDA-event time.
-    small = None
-    if not args.no_small and rank == 0:
-        slp = G.config1(seed=0)
-        small = {"workload": "small random LP m=2000 n=5000 nnz=19988 (seed 0), tol 1e-8"}
-        with capi.Problem(slp, device=local) as P:
-            for prec in ("fp64", "fp32-refine"):
-                P.solve(precision=prec, tolerance=1e-6, time_limit=60.0)  # warm
-                r = P.solve(precision=prec, tolerance=1e-8, time_limit=60.0)
-                small[prec] = {"status": r["status_name"], "s": r["device_time_ms"] / 1e3,
-                               "iterations": r["iterations"], "objective": r["objective"]}
-                x_last = r["x"]
-        if small["fp64"]["status"] == small["fp32-refine"]["status"] == "near-optimal":
-            small["speedup_fp32_refine_vs_fp64"] = small["fp64"]["s"] / small["fp32-refine"]["s"]
-        # host crossover from the FP32 + refinement answer to an optimal vertex
-        # (a probe: the line does not depend on it)
-        try:
-            t0 = time.perf_counter()
-            xv, _, _, xi = capi.crossover(slp, x_last)
-            small["crossover_from_fp32_refine"] = {
-                "status": xi["status"], "s": time.perf_counter() - t0, "pivots": xi["pivots"],
-                "host_threads": min(16, os.cpu_count() or 1),
-                "objective": float(slp.c @ xv + slp.obj_const)}
-        except Exception as e:
-            small["crossover_from_fp32_refine"] = {"error": str(e)[:200]}
-        from oracle import oracle as O
-        rr = O.pdhg_solve(O.lp_from(slp), tolerance=1e-8, time_limit=120.0,
-                          threads=os.cpu_count() or 1)
-        small["cpu_oracle_fp64"] = {"status": rr["status_name"], "s": rr["seconds"],
-                                    "iterations": rr["iterations"], "cores": os.cpu_count()}
-    # Time to 1e-8 on the multicommodity-flow LP (300 x 300 grid, 8
-    # commodities: m=1,078,800, n=2,870,400, nnz=8,611,200), where both
-    # precisions reach it within the bench's budget.
-    c5 = None
-    if not args.no_c5 and rank == 0:
-        flp = G.config5(seed=0)
-        c5 = {"workload": f"multicommodity flow m={flp.m} n={flp.n} nnz={flp.nnz} (seed 0), "
-                          "tol 1e-8, device-resident, CUDA-event time"}
-        with capi.Problem(flp, device=local) as P:
-            for prec in ("fp32-refine", "fp64"):
-                r = P.solve(precision=prec, tolerance=1e-8, time_limit=240.0)
-                # this LP's working set (~300 MB FP32) exceeds L2: its attempts
-                # stream from HBM, so the HBM roofline is the bound here
-                cb = bytes_per_attempt(flp.m, flp.n, flp.nnz, 8 if prec == "fp64" else 4)
-                us = 1e3 * r["attempt_time_ms"] / max(1, r["attempts"])
-                pk5, pk5_kind = peaks()
-                c5[prec] = {"status": r["status_name"], "s": r["device_time_ms"] / 1e3,
-                            "iterations": r["iterations"], "attempts": r["attempts"],
-                            "objective": r["objective"], "pinf": r["pinf"], "dinf": r["dinf"],
-                            "rel_gap": r["rel_gap"], "prow": r["prow"],
-                            "attempt_us": us, "attempt_bytes": cb,
-                            "attempt_hbm_frac": cb / (us * 1e-6) / 1e9 / pk5,
-                            "hbm_peak_kind": pk5_kind}
-        if c5["fp64"]["status"] == c5["fp32-refine"]["status"] == "near-optimal":
-            c5["speedup_fp32_refine_vs_fp64"] = c5["fp64"]["s"] / c5["fp32-refine"]["s"]
-            c5["objective_rel_diff"] = abs(c5["fp64"]["objective"] - c5["fp32-refine"]["objective"]) / \
-                max(1.0, abs(c5["fp64"]["objective"]))
+    slp = small = flp = c5 = c2tol = refg = None
+    if rank == 0 and not args.no_small:
+        slp, small = small_lp_probe(capi, G, local)
+    if rank == 0 and not args.no_c5:
+        flp, c5 = c5_probe(capi, G, local)
+    if rank == 0 and not args.no_c2_tol:
+        c2tol = c2_tol_probe(capi, lp, local, args.c2_budget, 0.6 * args.c2_budget)
+    if rank == 0 and not args.no_ref_gpu:
+        if ref_gpu_ready():
+            slp = slp or G.config1(seed=0)
+            refg = vs_reference_gpu(capi, local, slp, flp, lp if s == 1.0 else None)
+        else:
+            refg = {"unavailable": "reference GPU PDHG not built here (oracle/_ref needs the "
+                                   "reference sources or their staging in oracle/_ref/src)"}
     batch = None
     if not args.no_batch and rank == 0:
         batch = batch_probe(capi, G, sample=args.batch_sample, count=args.batch_count)
     layer = None
     if not args.no_layer and rank == 0:
         layer = layer_probe(torch, G)
-    probes = {}
-    if args.tol_probe > 0:
-        with capi.Problem(lp, device=local) as P:
-            for prec in ("fp32-refine", "fp64"):
-                for tol in (1e-4, 1e-8):
-                    r = P.solve(precision=prec, tolerance=tol, time_limit=args.tol_probe)
-                    probes[f"{prec}@{tol:g}"] = {
-                        "status": r["status_name"], "device_s": r["device_time_ms"] / 1e3,
-                        "iterations": r["iterations"], "pinf": r["pinf"], "dinf": r["dinf"],
-                        "rel_gap": r["rel_gap"]}
     if rank != 0:
         return
     pk, pk_kind = peaks()
     achieved = bpa * att / (att_ms / 1e3) / 1e9
-    # both FP32 modes run the same attempt kernels (refinement adds one
-    # m-vector read of the rounded anchor y)
     prec_key = "fp64" if args.precision == "fp64" else "fp32"
-    traffic = traffic_from_profile(f"fused_attempt_{prec_key}_{'c2' if s == 1.0 else 'scaled'}")
-    # The attempt's gathers are served by L2 (its working set nearly fits the
-    # 126 MB L2), so its second roofline is the random-sector rate of L2:
-    # L1-miss sectors per attempt (ncu, committed summary) against the
-    # device's measured rate for random 4-byte reads of a 2 MB vector.
+    alt_key = "fp64" if alt == "fp64" else "fp32"
+    suffix = "c2" if s == 1.0 else "scaled"
+    traffic = traffic_from_profile(f"fused_attempt_{prec_key}_{suffix}")
+    att_alt = sum(r["attempts"] for r in res_alt)
+    att_ms_alt = sum(r["attempt_time_ms"] for r in res_alt)
+    dev_ms_alt = sum(r["device_time_ms"] for r in res_alt)
+    ach_alt = bpa_alt * att_alt / (att_ms_alt / 1e3) / 1e9
+    # The FP32 attempt's working set (112 MB) nearly fits the 126 MB L2, so
+    # its gathers are served by L2: its second roofline is L2's random-sector
+    # rate (L1-miss sectors per attempt from the committed ncu summary against
+    # the device's measured rate for random 4-byte reads of a 2 MB vector).
     l2 = None
-    sectors = traffic_from_profile(f"fused_attempt_{prec_key}_c2_l1_miss_sectors") if s == 1.0 else None
     try:
         ceiling = capi.gather_rate(19)
     except Exception as ex:  # calibration is a report, not a gate
         ceiling = None
         print(f"gather-rate calibration failed: {ex}", file=sys.stderr)
+    sectors = traffic_from_profile("fused_attempt_fp32_c2_l1_miss_sectors") if s == 1.0 else None
     if ceiling:
-        l2 = {"bound": "l2 random sectors", "ceiling_sectors_per_s": ceiling,
-              "ceiling_probe": "random 4-byte reads of a 2 MB resident vector (igaos_pdhg_gather_rate)"}
+        fp32_rows = res if prec_key == "fp32" else res_alt
+        a32 = sum(r["attempts"] for r in fp32_rows)
+        ms32 = sum(r["attempt_time_ms"] for r in fp32_rows)
+        l2 = {"kernel": "FP32 attempt", "bound": "l2 random sectors",
+              "ceiling_sectors_per_s": ceiling,
+              "ceiling_probe": "random 4-byte reads of a 2 MB resident vector "
+                               "(igaos_pdhg_gather_rate)"}
         if sectors:
-            rate = sectors / (1e-3 * att_ms / att)
+            rate = sectors / (1e-3 * ms32 / a32)
             l2.update({"sectors_per_launch": sectors, "achieved_sectors_per_s": rate,
                        "frac": rate / ceiling})
     if args.no_cpu:
@@ -480,12 +599,12 @@ def main():
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f64" if args.precision == "fp64" else "f32", "data": "synthetic",
         "config": config_dict(lp, args),
-        "roofline": {"kernel": "fused PDHG attempt (k_primal: A^T y + primal step; k_dual: "
-                               "A xbar + dual step + step decision)",
+        "roofline": {"kernel": f"fused PDHG attempt, {prec_key.upper()} (k_primal: A^T y + "
+                               "primal step; k_dual: A xbar + dual step + step decision)",
                      "bound": "hbm", "achieved": achieved, "peak": pk, "peak_kind": pk_kind,
                      "unit": "GB/s", "frac": achieved / pk,
                      "bytes_per_launch": bpa, "launch_us": 1e3 * att_ms / att,
-                     "traffic": traffic, "l2": l2},
+                     "traffic": traffic},
         "cpu_baseline": {"value": cpu_v, "unit": "GB/s", "cores": os.cpu_count(),
                          "kind": "port",
                          "sample": f"{args.cpu_iters} iterations of the reference FP64 PDHG "
@@ -495,17 +614,28 @@ def main():
         "clocks": ck,
         "kkt_passes_per_s": ws * att / (dev_ms_max / 1e3),
         "iterations_per_step": res[-1]["iterations"], "attempts_per_step": res[-1]["attempts"],
+        alt.replace("-", "_"): {
+            "value": bpa_alt * att_alt / (dev_ms_alt / 1e3) / 1e9, "unit": "GB/s",
+            "ms_per_step": dev_ms_alt / len(res_alt),
+            "roofline": {"achieved": ach_alt, "peak": pk, "frac": ach_alt / pk,
+                         "bytes_per_launch": bpa_alt, "launch_us": 1e3 * att_ms_alt / att_alt,
+                         "traffic": traffic_from_profile(f"fused_attempt_{alt_key}_{suffix}"),
+                         "l2": l2 if alt_key == "fp32" else None}},
     }
+    if l2 and prec_key == "fp32":
+        line["roofline"]["l2"] = l2
     if small:
-        line["time_to_1e-8_small_lp"] = small
+        line["time_to_tol_small_lp"] = small
     if c5:
-        line["time_to_1e-8_multicommodity_lp"] = c5
+        line["time_to_tol_multicommodity_lp"] = c5
+    if c2tol:
+        line["time_to_tol_large_lp"] = c2tol
+    if refg:
+        line["vs_reference_gpu"] = refg
     if batch:
         line["batched_small_lps"] = batch
     if layer:
         line["differentiable_layer"] = layer
-    if probes:
-        line["time_to_tol"] = probes
     print(json.dumps(line), flush=True)
 
 

@@ -112,6 +112,58 @@ template <> struct Vec2<float> { using type = float2; };
 __device__ __forceinline__ double smax(double a, double b) { return (a < b) ? b : a; }
 __device__ __forceinline__ double smin(double a, double b) { return (b < a) ? b : a; }
 
+// FP64 comparisons on the integer pipe. This GPU's FP64 pipe does about 2
+// operations per clock per SM, and the FP64 attempt and KKT kernels are bound
+// by it; compare, min/max and sign tests of doubles are done instead on
+// order-preserving keys of the bit patterns (negative values with every bit
+// flipped, non-negative ones with the sign bit set), for operands that are not
+// NaN (the attempt kernels flag NaN/Inf dot products before any KKT pass).
+// dlt(a, b) = a < b; dmax / dmin = smax / smin (std::max / std::min order);
+// dabs = fabs; dfinite = isfinite; dgt0 = a > 0; dlt0 = a < 0.
+// IGX_INT_CLAMP=0 keeps the FP64 instructions in the attempt kernels.
+#ifndef IGX_INT_CLAMP
+#define IGX_INT_CLAMP 1
+#endif
+__device__ __forceinline__ unsigned long long order_key(double a) {
+    const long long b = __double_as_longlong(a);
+    return (unsigned long long)b ^ ((unsigned long long)(b >> 63) | 0x8000000000000000ULL);
+}
+__device__ __forceinline__ bool dlt(double a, double b) { return order_key(a) < order_key(b); }
+__device__ __forceinline__ double dmax(double a, double b) { return dlt(a, b) ? b : a; }
+__device__ __forceinline__ double dmin(double a, double b) { return dlt(b, a) ? b : a; }
+__device__ __forceinline__ double dabs(double a) {
+    return __longlong_as_double(__double_as_longlong(a) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool dfinite(double a) {
+    return (__double_as_longlong(a) & 0x7ff0000000000000LL) != 0x7ff0000000000000LL;
+}
+__device__ __forceinline__ bool dgt0(double a) { return __double_as_longlong(a) > 0; }
+__device__ __forceinline__ bool dlt0(double a) {
+    const long long b = __double_as_longlong(a);
+    return b < 0 && (b << 1) != 0;  // negative, not -0
+}
+// a < b and clamp(v, lo, hi) = min(max(v, lo), hi) (lo <= hi) in the
+// iterate's precision: FP32 on its own pipe, FP64 on the integer pipe (the
+// result is one of the three operands, bit for bit).
+__device__ __forceinline__ bool less(float a, float b) { return a < b; }
+__device__ __forceinline__ bool less(double a, double b) {
+#if IGX_INT_CLAMP
+    return dlt(a, b);
+#else
+    return a < b;
+#endif
+}
+__device__ __forceinline__ float clamp_val(float v, float lo, float hi) {
+    return fminf(fmaxf(v, lo), hi);
+}
+__device__ __forceinline__ double clamp_val(double v, double lo, double hi) {
+#if IGX_INT_CLAMP
+    return dlt(v, lo) ? lo : (dlt(hi, v) ? hi : v);
+#else
+    return fmin(fmax(v, lo), hi);
+#endif
+}
+
 // Row accumulator. FP64: a plain FMA chain. FP32: compensated dot product
 // (TwoProduct by fmaf + TwoSum, Ogita-Rump-Oishi "Dot2"): the running sum and
 // the exact rounding errors of every product and addition are kept apart and

@@ -273,6 +273,10 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     base_.rmax = vec(rmax, pr_);
     base_.cmax = 0.0;
     for (int j = 0; j < n; ++j) base_.cmax = std::max(base_.cmax, std::fabs(c[j]));
+    base_.lob = ar_.alloc<double>(n);
+    base_.hib = ar_.alloc<double>(n);
+    k_bands<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cl, base_.cu, base_.lob, base_.hib);
+    CU(cudaGetLastError());
     base_.sc = ar_.alloc<double>(n);
     base_.scl = ar_.alloc<double>(n);
     base_.scu = ar_.alloc<double>(n);
@@ -286,6 +290,7 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     dr_ = ar_.alloc<double>(m);
     dc_ = ar_.alloc<double>(n);
     idr_ = ar_.alloc<double>(m);
+    idc_ = ar_.alloc<double>(n);
     // control + scratch
     ctl_ = ar_.alloc<DevCtl>(1);
     met_ = ar_.alloc<DevMetrics>(2);
@@ -381,6 +386,7 @@ void Engine::setup_scaling() {
     k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cl, dc_, 0, base_.scl, base_.fcl);
     k_scale_vec<<<grid_for(n), kThreads, 0, st_>>>(n, base_.cu, dc_, 0, base_.scu, base_.fcu);
     k_recip<<<grid_for(m), kThreads, 0, st_>>>(m, dr_, idr_);
+    k_recip<<<grid_for(n), kThreads, 0, st_>>>(n, dc_, idc_);
     CU(cudaGetLastError());
     hp_dr_.resize(m);
     hp_dc_.resize(n);
@@ -620,6 +626,9 @@ void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* 
     ka.dr = dr_;
     ka.dc = dc_;
     ka.idr = idr_;
+    ka.idc = idc_;
+    ka.lob = v.lob;
+    ka.hib = v.hib;
     ka.c = v.c;
     ka.cl = v.cl;
     ka.cu = v.cu;
@@ -1046,7 +1055,7 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
                 last_rollback = k_done;
                 ++out.rollbacks;
                 if (o.verbosity > 1)
-                    std::fprintf(stderr, "[pdhg-gb300] rollback @k=%lld to the incumbent, eta %.6e\n",
+                    std::fprintf(stderr, "[pdhg-gb300] rollback @k=%lld to the incumbent, eta %.17g\n",
                                  k_done, h_ctl_->eta);
             }
             // restart + primal weight (src/pdhg/pdhg.cu:1001-1075)

@@ -62,6 +62,7 @@ std::vector<int> length_order(const int* ptr, int rows);
 // (FP64, for the KKT pass) and scaled units (FP64 and FP32, for iterating).
 struct Vecs {
     double *c, *cl, *cu, *rmin, *rmax;      // original
+    double *lob, *hib;                      // at-bound bands of cl, cu (k_bands)
     double *sc, *scl, *scu, *srmin, *srmax; // scaled FP64
     float *fc, *fcl, *fcu, *frmin, *frmax;  // scaled FP32
     double cmax;
@@ -164,6 +165,7 @@ class Engine {
     Sched sA_, sAT_;
     double *dr_, *dc_;
     double* idr_;  // 1 / dr, for the KKT kernels
+    double* idc_;  // 1 / dc, for the KKT kernels
     Vecs base_{};
     // device numbering: new index -> original (pr_, pc_) and inverses
     std::vector<int> pr_, pc_, ipr_, ipc_;

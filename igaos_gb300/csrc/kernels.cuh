@@ -91,7 +91,7 @@ struct PrimalEpi {
     }
     __device__ __forceinline__ void apply(int j, const Acc<T>& acc, const Pre& v) {
         const T g = v.c + acc.result();
-        const T xn = fmin(fmax(fma(-tau, g, v.x), v.lo), v.hi);
+        const T xn = clamp_val(fma(-tau, g, v.x), v.lo, v.hi);
         xn_out[j] = xn;
         const T xb = fma((T)2, xn, -v.x);
         xbar[j] = xb;
@@ -144,6 +144,16 @@ struct DualArgs {
 // FP64 anchor yhat; the dual projection must act on the full value, so the
 // clamp argument is (t + yhat)/sigma with t = dy + sigma A dxbar and the row
 // bounds shifted by the anchor's activity. yhat == nullptr: plain iterates.
+// sigma > 0, so u / sigma < lo exactly when u < sigma lo (up to the rounding
+// of the product at a tie): the step first compares u = t (+ yhat) with the
+// bounds times sigma. An out-of-range row gets the reference's value
+// (kern_dual, src/pdhg/pdhg.cu:49-61) without dividing, y' = fma(-sigma,
+// bound, t); only an in-range row divides, with the reference's own formula,
+// so its rounding residue -- which the line search sees through dy -- is the
+// reference's too. An FP64 division costs about ten FP64 instructions and
+// FP64's pipe bounds the FP64 attempt; equality rows never divide. (Giving
+// in-range rows an exact 0 instead froze the step size of a 1 x 1 LP: with
+// dy = 0 the line search sees no curvature.)
 template <typename T, class B = NoBcast>
 struct DualEpi {
     const T *rmin, *rmax, *yc, *axc, *ya, *yhat;
@@ -160,8 +170,11 @@ struct DualEpi {
     __device__ __forceinline__ void apply(int i, const Acc<T>& acc, const Pre& v) {
         const T ab = acc.result();
         const T t = fma(sigma, ab, v.y);
-        const T arg = yhat ? (t + v.yh) / sigma : t / sigma;
-        const T yn = fma(-sigma, fmin(fmax(arg, v.lo), v.hi), t);
+        const T u = yhat ? t + v.yh : t;
+        T yn;
+        if (less(u, sigma * v.lo)) yn = fma(-sigma, v.lo, t);
+        else if (less(sigma * v.hi, u)) yn = fma(-sigma, v.hi, t);
+        else yn = fma(-sigma, clamp_val(u / sigma, v.lo, v.hi), t);
         yn_out[i] = yn;
         bc(i, yn);
         const T dy = yn - v.y;
@@ -351,6 +364,22 @@ __global__ void k_pc_apply(int n, const double* __restrict__ sum, int mul, doubl
     }
 }
 
+// evaluate()'s at-bound bands per column (src/pdhg/pdhg.cu:206-212), the
+// same FP64 operations as the inline test: tol = 1e-9 (1 + |b|), b = cu if
+// finite else cl; lob = cl + tol, hib = cu - tol. A free column gives
+// inf - inf = NaN there, which the inline test's x <= NaN / x >= NaN never
+// passes; -inf / +inf keep that outcome for the integer-pipe compares.
+__global__ void k_bands(int n, const double* __restrict__ cl, const double* __restrict__ cu,
+                        double* __restrict__ lob, double* __restrict__ hib) {
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const double l = cl[j], u = cu[j];
+        const double tol = 1e-9 * (1.0 + fabs(isfinite(u) ? u : l));
+        const double lb = l + tol, hb = u - tol;
+        lob[j] = isnan(lb) ? -CUDART_INF : lb;
+        hib[j] = isnan(hb) ? CUDART_INF : hb;
+    }
+}
+
 __global__ void k_fill(int n, double v, double* __restrict__ out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
         out[i] = v;
@@ -508,6 +537,10 @@ struct KktArgs {
     const T* y[2];
     const double *dr, *dc;
     const double* idr;                        // 1 / dr (IEEE quotients)
+    const double* idc;                        // 1 / dc (IEEE quotients)
+    // evaluate()'s at-bound bands (src/pdhg/pdhg.cu:206-212), per column:
+    // lob = cl + 1e-9 (1 + |b|), hib = cu - 1e-9 (1 + |b|), b = finite cu else cl
+    const double *lob, *hib;
     const double *c, *cl, *cu, *rmin, *rmax;  // original units
     const T *slo, *shi;                       // scaled column bounds, iterate precision
     double cmax;
@@ -522,20 +555,20 @@ __global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_rows(KktArgs<T>
     const int v = blockIdx.y;
     const T* __restrict__ yv = a.y[v];
     double pv = 0.0, pa = 0.0, prow = 0.0, ymax = 0.0;
+    // comparisons on the integer pipe (dmax, dmin, ...; see device.cuh)
     auto f = [&](int i, const Acc<T>& acc) {
         const double Ax = acc.result_d() * a.dr[i];
         const double lo = a.rmin[i], hi = a.rmax[i];
-        const double vi = smax(lo - Ax, Ax - hi);
-        pv = smax(pv, vi);
-        pa = smax(pa, fabs(smin(smax(Ax, lo), hi)));
-        const double viol = smax(0.0, vi);
-        if (viol > 0.0) {  // viol / (1 + sc) is 0 otherwise: skip the FP64 division
-            double sc = fabs(Ax);
-            if (isfinite(lo)) sc = smax(sc, fabs(lo));
-            if (isfinite(hi)) sc = smax(sc, fabs(hi));
-            prow = smax(prow, viol / (1.0 + sc));
+        const double vi = dmax(lo - Ax, Ax - hi);
+        pv = dmax(pv, vi);
+        pa = dmax(pa, dabs(dmin(dmax(Ax, lo), hi)));
+        if (dgt0(vi)) {  // viol / (1 + sc) is 0 otherwise: skip the FP64 division
+            double sc = dabs(Ax);
+            if (dfinite(lo)) sc = dmax(sc, dabs(lo));
+            if (dfinite(hi)) sc = dmax(sc, dabs(hi));
+            prow = dmax(prow, vi / (1.0 + sc));
         }
-        ymax = smax(ymax, fabs((double)yv[i] * a.idr[i]));
+        ymax = dmax(ymax, dabs((double)yv[i] * a.idr[i]));
     };
     PlainEpi<decltype(f)> epi{f};
     warp_rows_all<T>(a.wsA, a.A, a.x[v], epi);
@@ -568,24 +601,22 @@ __global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_cols(KktArgs<T>
     const T* __restrict__ xv = a.x[v];
     const double dz = 1e-8 * (1.0 + a.cmax);
     double dv = 0.0, op = 0.0, od = 0.0, unb = 0.0;
+    // comparisons on the integer pipe, at-bound bands precomputed (k_bands);
+    // the reduced cost multiplies by 1/dc instead of dividing by dc
     auto f = [&](int j, const Acc<T>& acc) {
-        const double d = a.c[j] + 1.0 * acc.result_d() / a.dc[j];
+        const double d = a.c[j] + acc.result_d() * a.idc[j];
         const double x = unscale_x(xv[j], a.slo[j], a.shi[j], a.dc[j], a.cl[j], a.cu[j]);
         const double cl = a.cl[j], cu = a.cu[j];
-        const double bnd = fabs(isfinite(cu) ? cu : cl);
-        const double tol = 1e-9 * (1.0 + bnd);
-        double e;
-        if (x <= cl + tol && d > 0) e = 0.0;
-        else if (x >= cu - tol && d < 0) e = 0.0;
-        else e = fabs(d);
-        dv = smax(dv, e);
+        const bool pos = dgt0(d), neg = dlt0(d);
+        const bool excused = (pos && !dlt(a.lob[j], x)) || (neg && !dlt(x, a.hib[j]));
+        if (!excused) dv = dmax(dv, dabs(d));
         op += a.c[j] * x;
-        if (d >= 0) {
-            if (isfinite(cl)) od += d * cl;
-            else if (d > dz) unb = 1.0;
+        if (!neg) {  // d >= 0
+            if (dfinite(cl)) od += d * cl;
+            else if (dlt(dz, d)) unb = 1.0;
         } else {
-            if (isfinite(cu)) od += d * cu;
-            else if (-d > dz) unb = 1.0;
+            if (dfinite(cu)) od += d * cu;
+            else if (dlt(dz, -d)) unb = 1.0;
         }
     };
     PlainEpi<decltype(f)> epi{f};
@@ -634,11 +665,11 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rowdual(KktArgs<T> a, int m) {
     double od = 0.0, unb = 0.0;
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
         const double y = (double)yv[i] * a.idr[i];
-        if (y > yz) {
-            if (isfinite(a.rmax[i])) od -= y * a.rmax[i];
+        if (dlt(yz, y)) {
+            if (dfinite(a.rmax[i])) od -= y * a.rmax[i];
             else unb = 1.0;
-        } else if (y < -yz) {
-            if (isfinite(a.rmin[i])) od -= y * a.rmin[i];
+        } else if (dlt(y, -yz)) {
+            if (dfinite(a.rmin[i])) od -= y * a.rmin[i];
             else unb = 1.0;
         }
     }
