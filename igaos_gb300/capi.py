@@ -19,6 +19,7 @@ OK, ERR_INVALID, ERR_CUDA, ERR_NOMEM, ERR_NODEVICE, ERR_NUMERIC, ERR_TIMEOUT = r
 FP64, FP32_REFINE, FP32 = 0, 1, 2
 PRECISIONS = {"fp64": FP64, "fp32-refine": FP32_REFINE, "fp32": FP32}
 SCALINGS = {"ruiz": 0, "ruiz-pc": 1}
+SCHEDULES = {"fixed": 0, "autotune": 1}
 STATUS_NAMES = ["optimal", "near-optimal", "feasible", "infeasible", "unbounded",
                 "iteration-limit", "time-limit", "error"]
 
@@ -34,7 +35,7 @@ class Options(C.Structure):
         ("check_period", C.c_int), ("inner_tolerance", C.c_double),
         ("max_refinements", C.c_int), ("use_graphs", C.c_int), ("device", C.c_int),
         ("detect_infeasibility", C.c_int), ("pdhg_presolve", C.c_int), ("crossover", C.c_int),
-        ("scaling", C.c_int),
+        ("scaling", C.c_int), ("schedule", C.c_int),
     ]
 
 
@@ -47,7 +48,8 @@ class Result(C.Structure):
         ("refinements", C.c_int), ("solve_time_ms", C.c_double),
         ("setup_time_ms", C.c_double), ("device_time_ms", C.c_double),
         ("attempt_time_ms", C.c_double), ("launches", C.c_int64),
-        ("rollbacks", C.c_int64), ("message", C.c_char * 160),
+        ("rollbacks", C.c_int64), ("entries_a", C.c_int32), ("entries_at", C.c_int32),
+        ("message", C.c_char * 160),
     ]
 
     def as_dict(self):
@@ -313,6 +315,8 @@ def default_options(**kw) -> Options:
             v = PRECISIONS[v]
         if k == "scaling" and isinstance(v, str):
             v = SCALINGS[v]
+        if k == "schedule" and isinstance(v, str):
+            v = SCHEDULES[v]
         if not hasattr(o, k):
             raise TypeError(f"unknown option {k!r}")
         setattr(o, k, v)

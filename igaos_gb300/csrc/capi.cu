@@ -467,6 +467,8 @@ int igaos_pdhg_solve(igaos_pdhg_problem* p, const igaos_pdhg_options* opt,
     else igaos_pdhg_default_options(&o);
     if (!(o.tolerance > 0)) return fail(IGAOS_PDHG_ERR_INVALID, "tolerance must be positive");
     if (o.precision < 0 || o.precision > 2) return fail(IGAOS_PDHG_ERR_INVALID, "unknown precision");
+    if (o.schedule != IGAOS_PDHG_SCHEDULE_FIXED && o.schedule != IGAOS_PDHG_SCHEDULE_AUTOTUNE)
+        return fail(IGAOS_PDHG_ERR_INVALID, "unknown schedule");
     std::vector<double> xb, yb;  // the answer, when crossover needs it and the caller does not
     if (p->xo && !x) {
         xb.resize(p->orig.n);

@@ -55,14 +55,15 @@ std::vector<int> length_order(const int* ptr, int rows) {
     return ord;
 }
 
-void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<unsigned char>& wlg) {
+void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<unsigned char>& wlg,
+                 int entries) {
     wrow.assign(1, 0);
     wlg.clear();
     int r = 0;
     while (r < rows) {
         const int len = ptr[r + 1] - ptr[r];
         int lg = 0;
-        while (lg < 5 && (1 << lg) * kLaneEntries < len) ++lg;
+        while (lg < 5 && (1 << lg) * entries < len) ++lg;
         r = std::min(rows, r + (32 >> lg));
         wrow.push_back(r);
         wlg.push_back((unsigned char)lg);
@@ -116,11 +117,13 @@ static bool small_share(const int* ptr, int rows, std::vector<long long>& ent,
 // Launch width: enough CTAs for every warp item, capped at what stays
 // resident (6 CTAs of 256 threads per SM at <= 40 registers); the kernels
 // grid-stride over the items.
-static Sched upload_sched(Arena& ar, const int* ptr, int rows, int resident_ctas) {
+static Sched upload_sched(Arena& ar, const int* ptr, int rows, int resident_ctas,
+                          int entries = kLaneEntries) {
     std::vector<int> wr;
     std::vector<unsigned char> wl;
-    build_warps(ptr, rows, wr, wl);
+    build_warps(ptr, rows, wr, wl, entries);
     Sched s;
+    s.entries = entries;
     s.nwarps = (int)wl.size();
     s.ctas = std::max(1, std::min(resident_ctas, (s.nwarps + kWarps - 1) / kWarps));
     s.ctas64 = std::max(1, std::min(s.ctas, resident_ctas / kHotCtasPerSm * HotCtas<double>::value));
@@ -226,14 +229,22 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         int sms = 0;
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
         const int resident = std::max(1, sms) * kHotCtasPerSm;
-        sA_ = upload_sched(ar_, P.data(), m, resident);
+        for (int c = 0; c < 3; ++c) {
+            candA_[c] = upload_sched(ar_, P.data(), m, resident, kTuneEntries[c]);
+            if (kTuneEntries[c] == kLaneEntries) sA_ = candA_[c];
+            cap_ctas_A_ = std::max(cap_ctas_A_, candA_[c].ctas);
+        }
         std::vector<long long> ent_a, slot_a, ent_at, slot_at;
         bool fit = small_share(P.data(), m, ent_a, slot_a);
         permute_csr(n, cp, ci, acx, pc_, ipr_, P, I, V);
         CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(ci_, I.get(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(acx_, V.get(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
-        sAT_ = upload_sched(ar_, P.data(), n, resident);
+        for (int c = 0; c < 3; ++c) {
+            candAT_[c] = upload_sched(ar_, P.data(), n, resident, kTuneEntries[c]);
+            if (kTuneEntries[c] == kLaneEntries) sAT_ = candAT_[c];
+            cap_ctas_AT_ = std::max(cap_ctas_AT_, candAT_[c].ctas);
+        }
         fit = small_share(P.data(), n, ent_at, slot_at) && fit;
         // small LPs: the attempts of a chunk in one thread-block cluster with
         // the LP staged in its shared memory (cluster.cuh) when the largest
@@ -311,7 +322,7 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     fac_ = ar_.alloc<double>(2 * kFac);
     std::memset(h_ctl_, 0, sizeof(DevCtl));
     red_blocks_ = grid_for(std::max(m, n), kThreads, 152 * 4);
-    const int kkt_blocks = std::max(std::max(sA_.ctas, sAT_.ctas), red_blocks_);
+    const int kkt_blocks = std::max(std::max(cap_ctas_A_, cap_ctas_AT_), red_blocks_);
     kkt_part_ = ar_.alloc<double>((size_t)2 * kkt_blocks * 4);
     red_part_ = ar_.alloc<double>((size_t)2 * red_blocks_ + 8);
     scal_ = ar_.alloc<double>(16);
@@ -460,8 +471,8 @@ void Engine::ensure_work() {
     w.pesx = ar_.alloc<T>(n);
     w.yb = ar_.alloc<T>(m);
     w.pesy = ar_.alloc<T>(m);
-    w.part_p = ar_.alloc<double>(std::max(sAT_.ctas, kSmallCluster));
-    w.part_d = ar_.alloc<double>(2 * (size_t)std::max(sA_.ctas, kSmallCluster));
+    w.part_p = ar_.alloc<double>(std::max(cap_ctas_AT_, kSmallCluster));
+    w.part_d = ar_.alloc<double>(2 * (size_t)std::max(cap_ctas_A_, kSmallCluster));
     have = true;
 }
 
@@ -483,12 +494,10 @@ template <> struct VecSel<float> {
     static const float* yh(const Vecs& v) { return v.fyhat; }
 };
 
-// Enqueues `count` line-search attempts (2 launches each). With graphs the
-// sequence is captured once per (precision, count, vector set) and replayed.
+// Arguments of the two attempt kernels on the current schedules.
 template <typename T>
-void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
+void Engine::attempt_args(const Vecs& v, PrimalArgs<T>& pa, DualArgs<T>& da) {
     Work<T>& w = work<T>();
-    PrimalArgs<T> pa;
     pa.ws = sAT_.view();
     pa.AT = csrAT<T>();
     pa.y[0] = w.y[0];
@@ -503,7 +512,6 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     pa.xbar = w.xbar;
     pa.part = reinterpret_cast<Acc<T>*>(w.part_p);
     pa.ctl = ctl_;
-    DualArgs<T> da;
     da.ws = sA_.view();
     da.A = csrA<T>();
     da.xbar = w.xbar;
@@ -517,12 +525,22 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     da.part = reinterpret_cast<Acc<T>*>(w.part_d);
     da.part_primal = reinterpret_cast<const Acc<T>*>(w.part_p);
     const bool f64 = std::is_same<T, double>::value;
-    const int gp = f64 ? sAT_.ctas64 : sAT_.ctas, gd = f64 ? sA_.ctas64 : sA_.ctas;
-    da.n_primal = gp;
+    da.n_primal = f64 ? sAT_.ctas64 : sAT_.ctas;
     da.yhat = VecSel<T>::yh(v);
     da.fac = fac_;
     da.n_fac = kFac;
     da.ctl = ctl_;
+}
+
+// Enqueues `count` line-search attempts (2 launches each). With graphs the
+// sequence is captured once per (precision, count, vector set) and replayed.
+template <typename T>
+void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
+    PrimalArgs<T> pa;
+    DualArgs<T> da;
+    attempt_args<T>(v, pa, da);
+    const bool f64 = std::is_same<T, double>::value;
+    const int gp = f64 ? sAT_.ctas64 : sAT_.ctas, gd = f64 ? sA_.ctas64 : sA_.ctas;
     if (const int sb = small_bytes_[std::is_same<T, double>::value ? 1 : 0]) {
         // one cluster runs the whole chunk with the LP in shared memory
         ++launches_;
@@ -545,7 +563,7 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     }
     // key: precision, attempt count, vector set
     const GraphKey key{std::is_same<T, double>::value ? 1 : 2, count,
-                       (uintptr_t)VecSel<T>::c(v)};
+                       (uintptr_t)VecSel<T>::c(v), 3 * ia_ + iat_};
     auto it = graphs_.find(key);
     if (it == graphs_.end()) {
         cudaGraph_t g;
@@ -558,6 +576,84 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
         it = graphs_.emplace(key, ge).first;
     }
     CU(cudaGraphLaunch(it->second, st_));
+}
+
+void Engine::use_sched(int ia, int iat) {
+    ia_ = ia;
+    iat_ = iat;
+    sA_ = candA_[ia];
+    sAT_ = candAT_[iat];
+}
+
+// Autotuner (igaos_pdhg_options.schedule = IGAOS_PDHG_SCHEDULE_AUTOTUNE).
+// For each orientation the attempt kernel of precision T is timed on every
+// candidate warp schedule -- kTuneEntries entries per lane, which sets how
+// many lanes share a row of each length and how many rows a warp item holds
+// -- with CUDA events over kReps launches after a warming one, and the
+// fastest is kept for this problem and precision (later solves reuse it).
+// The probe runs on zero iterates under a control block that never stops;
+// the solve loop resets both afterwards. Small LPs that run on the
+// thread-block cluster path keep their staged layout.
+template <typename T>
+void Engine::tune() {
+    const int pi = std::is_same<T, double>::value ? 1 : 0;
+    if (choice_[pi][0] >= 0) return;
+    int def = 0;
+    for (int c = 0; c < 3; ++c)
+        if (kTuneEntries[c] == kLaneEntries) def = c;
+    if (small_bytes_[pi]) {
+        choice_[pi][0] = choice_[pi][1] = def;
+        return;
+    }
+    ensure_work<T>();
+    Work<T>& w = work<T>();
+    for (int s = 0; s < 2; ++s) {
+        CU(cudaMemsetAsync(w.x[s], 0, sizeof(T) * n, st_));
+        CU(cudaMemsetAsync(w.xavg[s], 0, sizeof(T) * n, st_));
+        CU(cudaMemsetAsync(w.y[s], 0, sizeof(T) * m, st_));
+        CU(cudaMemsetAsync(w.yavg[s], 0, sizeof(T) * m, st_));
+        CU(cudaMemsetAsync(w.axc[s], 0, sizeof(T) * m, st_));
+    }
+    CU(cudaMemsetAsync(w.xbar, 0, sizeof(T) * n, st_));
+    std::memset(h_ctl_, 0, sizeof(DevCtl));
+    h_ctl_->eta = eta0;
+    h_ctl_->omega = omega0;
+    h_ctl_->k = 1;
+    h_ctl_->k_stop = std::numeric_limits<long long>::max() / 2;
+    upload_ctl();
+    constexpr int kReps = 12;
+    cudaEvent_t e[3];
+    for (auto& ev : e) CU(cudaEventCreate(&ev));
+    const bool f64 = pi == 1;
+    for (int c = 0; c < 3; ++c) {
+        use_sched(c, c);
+        PrimalArgs<T> pa;
+        DualArgs<T> da;
+        attempt_args<T>(base_, pa, da);
+        const int gp = f64 ? sAT_.ctas64 : sAT_.ctas, gd = f64 ? sA_.ctas64 : sA_.ctas;
+        k_primal<T><<<gp, kThreads, 0, st_>>>(pa);
+        k_dual<T><<<gd, kThreads, 0, st_>>>(da);
+        CU(cudaEventRecord(e[0], st_));
+        for (int r = 0; r < kReps; ++r) k_primal<T><<<gp, kThreads, 0, st_>>>(pa);
+        CU(cudaEventRecord(e[1], st_));
+        for (int r = 0; r < kReps; ++r) k_dual<T><<<gd, kThreads, 0, st_>>>(da);
+        CU(cudaEventRecord(e[2], st_));
+        CU(cudaGetLastError());
+        CU(cudaEventSynchronize(e[2]));
+        float tp = 0.f, td = 0.f;
+        CU(cudaEventElapsedTime(&tp, e[0], e[1]));
+        CU(cudaEventElapsedTime(&td, e[1], e[2]));
+        tune_us_[pi][1][c] = 1e3f * tp / kReps;
+        tune_us_[pi][0][c] = 1e3f * td / kReps;
+        launches_ += 2 * (kReps + 1);
+    }
+    for (auto& ev : e) cudaEventDestroy(ev);
+    for (int o = 0; o < 2; ++o) {
+        int best = def;
+        for (int c = 0; c < 3; ++c)
+            if (tune_us_[pi][o][c] < tune_us_[pi][o][best]) best = c;
+        choice_[pi][o] = best;
+    }
 }
 
 void Engine::upload_ctl() {
@@ -1214,6 +1310,24 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     std::memset(&r, 0, sizeof(r));
     r.status = IGAOS_STATUS_ERROR;
     r.setup_time_ms = setup_ms;
+    // warp schedules: the fixed default, or the autotuner's choice for the
+    // attempt kernels' precision (timed once per handle and precision)
+    const int pi = o.precision == IGAOS_PDHG_FP64 ? 1 : 0;
+    int def = 0;
+    for (int c = 0; c < 3; ++c)
+        if (kTuneEntries[c] == kLaneEntries) def = c;
+    if (o.schedule == IGAOS_PDHG_SCHEDULE_AUTOTUNE) {
+        if (pi) tune<double>();
+        else tune<float>();
+        use_sched(choice_[pi][0], choice_[pi][1]);
+        if (o.verbosity > 0)
+            std::fprintf(stderr, "[pdhg-gb300] autotuned schedule (us per launch at 4/8/16 "
+                                 "entries per lane): A %.1f/%.1f/%.1f -> %d, A^T %.1f/%.1f/%.1f -> %d\n",
+                         tune_us_[pi][0][0], tune_us_[pi][0][1], tune_us_[pi][0][2], sA_.entries,
+                         tune_us_[pi][1][0], tune_us_[pi][1][1], tune_us_[pi][1][2], sAT_.entries);
+    } else {
+        use_sched(def, def);
+    }
     if (o.precision == IGAOS_PDHG_FP32_REFINE) {
         solve_refine(o, r, x, y);
         return;
@@ -1275,6 +1389,8 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     r.kkt_checks = out.checks;
     r.restarts = out.restarts;
     r.rollbacks = out.rollbacks;
+    r.entries_a = sA_.entries;
+    r.entries_at = sAT_.entries;
     r.kkt_passes = out.spmvs / 2;
     r.solve_time_ms = secs * 1000.0;
     if (out.numeric_failure) {
@@ -1594,6 +1710,8 @@ void Engine::solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, dou
     r.kkt_checks = out.checks;
     r.restarts = out.restarts;
     r.rollbacks = out.rollbacks;
+    r.entries_a = sA_.entries;
+    r.entries_at = sAT_.entries;
     r.kkt_passes = out.spmvs / 2;
     r.refinements = (int)out.anchors;
     if (out.numeric_failure) {

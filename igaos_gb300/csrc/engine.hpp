@@ -48,12 +48,18 @@ struct Sched {
     int nwarps = 0;
     int ctas = 0;  // kWarps warps per CTA
     int ctas64 = 0;  // launch width of the FP64 attempt kernels
+    int entries = 0; // entries per lane the schedule was built for
     WarpSched view() const { return WarpSched{row, lg, nwarps}; }
 };
 
 // Host-side warp schedule of a (length-sorted) CSR row pointer: consecutive
 // rows dealt to warps, G lanes per row from the first row's length.
-void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<unsigned char>& wlg);
+void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<unsigned char>& wlg,
+                 int entries = kLaneEntries);
+
+// Entries per lane of the schedules the autotuner chooses from (the first
+// value that is not the default is tried first; kLaneEntries is the default).
+constexpr int kTuneEntries[3] = {4, 8, 16};
 
 // Permutation sorting rows by decreasing length (stable): new -> old index.
 std::vector<int> length_order(const int* ptr, int rows);
@@ -86,12 +92,17 @@ struct Work {
     double *part_p, *part_d;
 };
 
+template <typename T> struct PrimalArgs;  // kernels.cuh
+template <typename T> struct DualArgs;
+
 struct GraphKey {
     int prec, count;
     uintptr_t vecs;
+    int sched;  // schedules in use (3 * index of A's + index of A^T's)
     bool operator<(const GraphKey& o) const {
         if (prec != o.prec) return prec < o.prec;
         if (count != o.count) return count < o.count;
+        if (sched != o.sched) return sched < o.sched;
         return vecs < o.vecs;
     }
 };
@@ -163,6 +174,16 @@ class Engine {
     double *ax_, *acx_;
     float *ax32_, *acx32_;
     Sched sA_, sAT_;
+    // warp schedules of A and A^T for every kTuneEntries value; sA_ / sAT_
+    // are one of them (kLaneEntries unless the autotuner chose otherwise)
+    Sched candA_[3], candAT_[3];
+    int cap_ctas_A_ = 0, cap_ctas_AT_ = 0;  // largest launch width of the candidates
+    int ia_ = 1, iat_ = 1;                  // candidates in use as sA_ / sAT_
+    int choice_[2][2] = {{-1, -1}, {-1, -1}};  // autotuned (A, A^T) per FP32 / FP64
+    float tune_us_[2][2][3] = {};           // per attempt-kernel launch, us
+    void use_sched(int ia, int iat);
+    template <typename T> void tune();
+    template <typename T> void attempt_args(const Vecs& v, PrimalArgs<T>& pa, DualArgs<T>& da);
     double *dr_, *dc_;
     double* idr_;  // 1 / dr, for the KKT kernels
     double* idc_;  // 1 / dc, for the KKT kernels

@@ -115,7 +115,24 @@ typedef struct igaos_pdhg_options {
      * scaling of PDLP (Applegate et al. 2021). Read by igaos_pdhg_create.
      * Added in ABI 4. */
     int scaling;
+    /* Warp schedule of the attempt kernels (how many lanes share a row of
+     * each length, and so how many rows a warp item holds):
+     * IGAOS_PDHG_SCHEDULE_FIXED (0, default): about 8 entries per lane.
+     * IGAOS_PDHG_SCHEDULE_AUTOTUNE (1): at the first solve of each precision
+     * on a handle, the A and A^T attempt kernels are timed on schedules of 4,
+     * 8 and 16 entries per lane (a dozen launches each) and the fastest is
+     * kept for that handle and precision; the result's entries_a /
+     * entries_at report the choice. The schedule changes the order of each
+     * row's sum, so results match the fixed schedule's to rounding, not bit
+     * for bit, and two handles may choose differently. Added in ABI 4. */
+    int schedule;
 } igaos_pdhg_options;
+
+/* Values of igaos_pdhg_options.schedule. */
+enum {
+    IGAOS_PDHG_SCHEDULE_FIXED = 0,
+    IGAOS_PDHG_SCHEDULE_AUTOTUNE = 1
+};
 
 /* Values of igaos_pdhg_options.scaling. */
 enum {
@@ -141,6 +158,8 @@ typedef struct igaos_pdhg_result {
     int64_t launches;         /* engine kernel launches during the solve */
     int64_t rollbacks;        /* restores of the incumbent after a blow-up
                                  (src/pdhg/pdhg.cu:965-988); added in ABI 4 */
+    int32_t entries_a;        /* entries per lane of the schedules used for A */
+    int32_t entries_at;       /* ... and for A^T (ABI 4; see options.schedule) */
     char message[160];
 } igaos_pdhg_result;
 

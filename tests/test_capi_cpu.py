@@ -40,6 +40,7 @@ def test_abi_version_and_defaults(native):
     assert o.pdhg_presolve == 0  # off: the reference engine ignores `presolve`
     assert o.crossover == 0
     assert o.scaling == capi.SCALINGS["ruiz"]  # the reference's Ruiz scaling alone
+    assert o.schedule == capi.SCHEDULES["fixed"]
     assert C.sizeof(o) == 88  # ABI 4 layout of igaos_pdhg_options
 
 
