@@ -61,7 +61,7 @@ class Result(C.Structure):
 
 class BatchResult(C.Structure):
     _fields_ = [
-        ("status", C.c_int), ("pad", C.c_int), ("objective", C.c_double),
+        ("status", C.c_int), ("finished_fp64", C.c_int), ("objective", C.c_double),
         ("pinf", C.c_double), ("dinf", C.c_double), ("rel_gap", C.c_double),
         ("prow", C.c_double), ("iterations", C.c_int64), ("attempts", C.c_int64),
         ("restarts", C.c_int64), ("kernel_time_ms", C.c_double), ("total_time_ms", C.c_double),

@@ -375,13 +375,16 @@ int igaos_pdhg_spmv(igaos_pdhg_problem* p, int transpose, int precision,
  * Per-instance outcome of igaos_pdhg_solve_batch. */
 typedef struct igaos_pdhg_batch_result {
     int status;              /* IGAOS_STATUS_* */
-    int pad;
+    int finished_fp64;       /* 1: the persistent launch left this instance at
+                                max_iterations and the single-LP engine
+                                finished it in FP64 (ABI 4; was padding) */
     double objective;        /* c^T x of the instance */
     double pinf, dinf, rel_gap, prow;
     int64_t iterations, attempts, restarts;
     double kernel_time_ms;   /* the whole batch's persistent kernel (same for all) */
     double total_time_ms;    /* the whole call: upload, kernel, download */
-    double instance_time_ms; /* this instance, from its CTA taking it to its answer */
+    double instance_time_ms; /* this instance, from its CTA taking it to its answer
+                                (plus its FP64 finish, if it had one) */
 } igaos_pdhg_batch_result;
 
 /* Solves `count` independent LPs of uneven sizes in one persistent kernel
@@ -394,7 +397,11 @@ typedef struct igaos_pdhg_batch_result {
  * FP32 iterates, termination metrics combined in FP64) to `tolerance` or
  * `max_iterations` on its own, with its own restarts and termination; the
  * reference has no batched path (its engine is one LP per call,
- * src/pdhg/pdhg.hpp:9). x (sum n) and y (sum m) may be NULL. */
+ * src/pdhg/pdhg.hpp:9). An instance the launch leaves at max_iterations
+ * (FP32 iterates can stall where FP64 ones do not) is then solved again,
+ * alone, by the single-LP engine in FP64 (the reference's arithmetic) under
+ * the same tolerance and iteration cap; its result says so (finished_fp64),
+ * and `iterations` counts both runs. x (sum n) and y (sum m) may be NULL. */
 int igaos_pdhg_solve_batch(int count, const int* m, const int* n,
                            const int* ap, const int* ai, const double* ax,
                            const double* c, const double* cl, const double* cu,
