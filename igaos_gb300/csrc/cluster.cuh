@@ -188,10 +188,12 @@ __global__ void __cluster_dims__(kSmallCluster, 1, 1) __launch_bounds__(kSmallTh
             v.tau = sctl.tau;
             v.sigma = sctl.sigma;
             v.w = sctl.w;
+            v.isigma = sctl.isigma;
         } else {
             v.tau = sctl.tau_f;
             v.sigma = sctl.sigma_f;
             v.w = sctl.w_f;
+            v.isigma = sctl.isigma_f;
         }
         for (int r = 0; r < nr; ++r) *cl.map_shared_rank(&sview, r) = v;
     };
@@ -278,7 +280,8 @@ __global__ void __cluster_dims__(kSmallCluster, 1, 1) __launch_bounds__(kSmallTh
         {
             DualEpi<T, ClusterBcast<T>> epi{da.rmin,    da.rmax, da.y[p],  da.axc[p], da.yavg[p],
                                             da.yhat,    da.y[q], da.axc[q], da.yavg[q], cv.sigma,
-                                            cv.w,       (T)0,    (T)0,     ClusterBcast<T>{sy[q], nr}};
+                                            cv.isigma,  cv.w,    (T)0,     (T)0,
+                                            ClusterBcast<T>{sy[q], nr}};
             for (int k = 0; k < snit[1][wi]; ++k) warp_item_staged<T>(sdesc[1][wi][k], st_a, sxbar, epi);
             T v[2] = {epi.dy2, epi.cross};
             block_sum_t<T, 2, kSmallWarps>(v, reinterpret_cast<T*>(smred));

@@ -83,7 +83,10 @@ struct DevCtl {
     // sigma = eta*omega (src/pdhg/pdhg.cu:756) and the averaging weight
     // w = 2/(hn+2) (:795), in FP64 and rounded to FP32.
     double tau, sigma, w;
-    float tau_f, sigma_f, w_f, pad_f;
+    float tau_f, sigma_f, w_f, isigma_f;
+    // correctly rounded 1/sigma in each precision (the dual step's quotient,
+    // see DualEpi in kernels.cuh)
+    double isigma;
 };
 
 __host__ __device__ inline void ctl_derive(DevCtl* c) {
@@ -93,6 +96,8 @@ __host__ __device__ inline void ctl_derive(DevCtl* c) {
     c->tau_f = (float)c->tau;
     c->sigma_f = (float)c->sigma;
     c->w_f = (float)c->w;
+    c->isigma = 1.0 / c->sigma;
+    c->isigma_f = 1.0f / c->sigma_f;
 }
 
 // FP64 KKT metrics of one candidate (see k_kkt_* in kernels.cuh).

@@ -36,17 +36,19 @@ __global__ void k_unscale_cols(int n, const TI* __restrict__ xs, const TI* __res
 template <typename T>
 struct CtlView {
     int parity, stop;
-    T tau, sigma, w;
+    T tau, sigma, w, isigma;
 };
 template <typename T>
 __device__ __forceinline__ CtlView<T> read_ctl(const DevCtl* c);
 template <>
 __device__ __forceinline__ CtlView<double> read_ctl<double>(const DevCtl* c) {
-    return CtlView<double>{c->parity, *(volatile const int*)&c->stop, c->tau, c->sigma, c->w};
+    return CtlView<double>{c->parity, *(volatile const int*)&c->stop, c->tau, c->sigma, c->w,
+                           c->isigma};
 }
 template <>
 __device__ __forceinline__ CtlView<float> read_ctl<float>(const DevCtl* c) {
-    return CtlView<float>{c->parity, *(volatile const int*)&c->stop, c->tau_f, c->sigma_f, c->w_f};
+    return CtlView<float>{c->parity, *(volatile const int*)&c->stop, c->tau_f, c->sigma_f, c->w_f,
+                          c->isigma_f};
 }
 
 template <typename T>
@@ -144,21 +146,24 @@ struct DualArgs {
 // FP64 anchor yhat; the dual projection must act on the full value, so the
 // clamp argument is (t + yhat)/sigma with t = dy + sigma A dxbar and the row
 // bounds shifted by the anchor's activity. yhat == nullptr: plain iterates.
-// sigma > 0, so u / sigma < lo exactly when u < sigma lo (up to the rounding
-// of the product at a tie): the step first compares u = t (+ yhat) with the
-// bounds times sigma. An out-of-range row gets the reference's value
-// (kern_dual, src/pdhg/pdhg.cu:49-61) without dividing, y' = fma(-sigma,
-// bound, t); only an in-range row divides, with the reference's own formula,
-// so its rounding residue -- which the line search sees through dy -- is the
-// reference's too. An FP64 division costs about ten FP64 instructions and
-// FP64's pipe bounds the FP64 attempt; equality rows never divide. (Giving
-// in-range rows an exact 0 instead froze the step size of a 1 x 1 LP: with
-// dy = 0 the line search sees no curvature.)
+// The quotient u / sigma (u = t, or t + yhat) is formed from the correctly
+// rounded reciprocal 1/sigma of the step decision by one remainder
+// correction (Markstein): q0 = u (1/sigma), r = fma(-sigma, q0, u),
+// q = fma(r, 1/sigma, q0). q is the correctly rounded quotient except in
+// rare cases (where it is one ulp off); an IEEE FP64 division costs about
+// ten FP64 instructions, and FP64's pipe (2 per clock per SM on this GPU)
+// bounds the FP64 attempt. The rest is the reference's formula (kern_dual,
+// src/pdhg/pdhg.cu:49-61), y' = fma(-sigma, clamp(q, lo, hi), t), so an
+// in-range row keeps the reference's rounding residue, which the line search
+// sees through dy. (An oracle run with this quotient took the same
+// iterations to the same objective, bit for bit, on the 14 golden LPs, six
+// Netlib LPs and a 1 x 1 LP; giving in-range rows an exact 0 instead froze
+// the 1 x 1 LP's step size: with dy = 0 the line search sees no curvature.)
 template <typename T, class B = NoBcast>
 struct DualEpi {
     const T *rmin, *rmax, *yc, *axc, *ya, *yhat;
     T *yn_out, *axc_out, *ya_out;
-    T sigma, w, dy2, cross;
+    T sigma, isigma, w, dy2, cross;
     B bc{};
     struct Pre {
         T lo, hi, y, ax, ya, yh;
@@ -171,10 +176,9 @@ struct DualEpi {
         const T ab = acc.result();
         const T t = fma(sigma, ab, v.y);
         const T u = yhat ? t + v.yh : t;
-        T yn;
-        if (less(u, sigma * v.lo)) yn = fma(-sigma, v.lo, t);
-        else if (less(sigma * v.hi, u)) yn = fma(-sigma, v.hi, t);
-        else yn = fma(-sigma, clamp_val(u / sigma, v.lo, v.hi), t);
+        const T q0 = u * isigma;
+        const T q = fma(fma(-sigma, q0, u), isigma, q0);
+        const T yn = fma(-sigma, clamp_val(q, v.lo, v.hi), t);
         yn_out[i] = yn;
         bc(i, yn);
         const T dy = yn - v.y;
@@ -244,7 +248,7 @@ __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_dual(DualArgs<T
     if (cv.stop) return;
     const int p = cv.parity, q = p ^ 1;
     DualEpi<T> epi{a.rmin, a.rmax, a.y[p], a.axc[p], a.yavg[p], a.yhat, a.y[q], a.axc[q], a.yavg[q],
-                   cv.sigma, cv.w, (T)0, (T)0};
+                   cv.sigma, cv.isigma, cv.w, (T)0, (T)0};
     warp_rows_all<T>(a.ws, a.A, a.xbar, epi);
     T v[2] = {epi.dy2, epi.cross};
     block_sum_t<T, 2>(v, reinterpret_cast<T*>(smred));
