@@ -59,7 +59,35 @@ struct Csr {
     const int* __restrict__ idx;
     const T* __restrict__ val;
     int rows;
+    // 1: values and indices are read with an L2 evict-first policy, so that a
+    // matrix streamed once per product does not push the iterate vectors
+    // (reused by the next launch) out of L2 (LPs whose attempt working set
+    // exceeds L2); 0: plain read-only loads
+    int stream = 0;
 };
+
+// Read-only loads with an L2 evict-first cache policy (PTX createpolicy +
+// ld.global.nc.L2::cache_hint).
+__device__ __forceinline__ unsigned long long l2_evict_first() {
+    unsigned long long p;
+    asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+__device__ __forceinline__ float ld_first(const float* a, unsigned long long pol) {
+    float v;
+    asm("ld.global.nc.L2::cache_hint.f32 %0, [%1], %2;" : "=f"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ double ld_first(const double* a, unsigned long long pol) {
+    double v;
+    asm("ld.global.nc.L2::cache_hint.f64 %0, [%1], %2;" : "=d"(v) : "l"(a), "l"(pol));
+    return v;
+}
+__device__ __forceinline__ int ld_first(const int* a, unsigned long long pol) {
+    int v;
+    asm("ld.global.nc.L2::cache_hint.s32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
 
 // Device control block of the iteration loop (one per solve). Written by the
 // last CTA of each dual-side launch; read by every CTA at launch start.
@@ -403,12 +431,23 @@ __device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
         for (int p = b + gl; p < e; p += kLaneBatch * G) {
             T a[kLaneBatch];
             int j[kLaneBatch];
+            if (A.stream) {  // uniform branch: one policy per batch
+                const unsigned long long pol = l2_evict_first();
 #pragma unroll
-            for (int u = 0; u < kLaneBatch; ++u) {
-                const int q = p + u * G;
-                const bool ok = q < e;
-                a[u] = ok ? __ldg(A.val + q) : T(0);
-                j[u] = ok ? __ldg(A.idx + q) : 0;
+                for (int u = 0; u < kLaneBatch; ++u) {
+                    const int q = p + u * G;
+                    const bool ok = q < e;
+                    a[u] = ok ? ld_first(A.val + q, pol) : T(0);
+                    j[u] = ok ? ld_first(A.idx + q, pol) : 0;
+                }
+            } else {
+#pragma unroll
+                for (int u = 0; u < kLaneBatch; ++u) {
+                    const int q = p + u * G;
+                    const bool ok = q < e;
+                    a[u] = ok ? __ldg(A.val + q) : T(0);
+                    j[u] = ok ? __ldg(A.idx + q) : 0;
+                }
             }
             T xv[kLaneBatch];
 #pragma unroll

@@ -334,6 +334,19 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     tmp_m_ = ar_.alloc<double>(m);
     tmp_m2_ = ar_.alloc<double>(m);
 
+    // matrices streamed with an L2 evict-first policy when the attempt's
+    // working set (matrix in both orientations, pointers, nine vectors per
+    // side) exceeds L2; IGAOS_PDHG_L2_STREAM=0/1 overrides (measurement)
+    {
+        int l2 = 0;
+        CU(cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, device_));
+        for (int k = 0; k < 2; ++k) {
+            const long long s = k ? 8 : 4;
+            const long long ws = 2 * nnz * (s + 4) + 4LL * (m + n + 2) + 9 * s * (m + n);
+            stream_[k] = ws > (long long)l2 ? 1 : 0;
+        }
+        if (const char* e = std::getenv("IGAOS_PDHG_L2_STREAM")) stream_[0] = stream_[1] = std::atoi(e) ? 1 : 0;
+    }
     setup_scaling();
     power_iteration();
     // eta0, omega0 (src/pdhg/pdhg.cu:642-663), from the scaled cost and
@@ -411,10 +424,10 @@ void Engine::setup_scaling() {
     CU(cudaStreamSynchronize(st_));
 }
 
-template <> Csr<double> Engine::csrA<double>() const { return Csr<double>{ap_, ai_, ax_, m}; }
-template <> Csr<double> Engine::csrAT<double>() const { return Csr<double>{cp_, ci_, acx_, n}; }
-template <> Csr<float> Engine::csrA<float>() const { return Csr<float>{ap_, ai_, ax32_, m}; }
-template <> Csr<float> Engine::csrAT<float>() const { return Csr<float>{cp_, ci_, acx32_, n}; }
+template <> Csr<double> Engine::csrA<double>() const { return Csr<double>{ap_, ai_, ax_, m, stream_[1]}; }
+template <> Csr<double> Engine::csrAT<double>() const { return Csr<double>{cp_, ci_, acx_, n, stream_[1]}; }
+template <> Csr<float> Engine::csrA<float>() const { return Csr<float>{ap_, ai_, ax32_, m, stream_[0]}; }
+template <> Csr<float> Engine::csrAT<float>() const { return Csr<float>{cp_, ci_, acx32_, n, stream_[0]}; }
 
 template <typename T>
 void Engine::spmv_dev(bool transpose, const T* x, T* y) {

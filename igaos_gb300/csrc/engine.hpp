@@ -277,6 +277,9 @@ class Engine {
     double elapsed() const;
     void setup_scaling();
     int scaling_ = IGAOS_PDHG_SCALING_RUIZ;  // igaos_pdhg_options.scaling
+    // FP32 / FP64 products stream the matrix with an L2 evict-first policy
+    // (Csr::stream): set when that precision's attempt working set exceeds L2
+    int stream_[2] = {0, 0};
     void power_iteration();
     void solve_refine(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x, double* y);
 };

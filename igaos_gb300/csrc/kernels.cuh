@@ -554,7 +554,7 @@ struct KktArgs {
 };
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_rows(KktArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_kkt_rows(KktArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const int v = blockIdx.y;
     const T* __restrict__ yv = a.y[v];
@@ -599,7 +599,7 @@ __global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_rows(KktArgs<T>
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, kHotCtasPerSm) k_kkt_cols(KktArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_kkt_cols(KktArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const int v = blockIdx.y;
     const T* __restrict__ xv = a.x[v];
