@@ -275,7 +275,7 @@ __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_dual(DualArgs<T
 // ------------------------------------------------------------- plain SpMV
 // y = A x (Spmv::mv, src/pdhg/pdhg.cu:143-157).
 template <typename T, typename TO>
-__global__ void __launch_bounds__(kThreads, kHotCtasPerSm)
+__global__ void __launch_bounds__(kThreads, HotCtas<T>::value)
     k_spmv(WarpSched ws, Csr<T> A, const T* __restrict__ x, TO* __restrict__ y) {
     auto f = [&](int r, const Acc<T>& acc) { y[r] = (TO)acc.result_d(); };
     PlainEpi<decltype(f)> epi{f};
