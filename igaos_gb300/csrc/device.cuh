@@ -67,7 +67,11 @@ struct Csr {
 };
 
 // Read-only loads with an L2 evict-first cache policy (PTX createpolicy +
-// ld.global.nc.L2::cache_hint).
+// ld.global.nc.L2::cache_hint). IGX_L2_STREAM=0 compiles the products
+// without the option.
+#ifndef IGX_L2_STREAM
+#define IGX_L2_STREAM 1
+#endif
 __device__ __forceinline__ unsigned long long l2_evict_first() {
     unsigned long long p;
     asm("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
@@ -383,16 +387,11 @@ __device__ __forceinline__ bool last_cta(unsigned int* ticket) {
 // ------------------------------------------------------ warp row schedule
 // Rows are processed by warps. The host permutes the LP so that rows (and
 // columns) appear in decreasing nonzero count, then deals consecutive rows to
-// warps. Two layouts of the same idea:
-// * the products' items (warp_item below): 32 consecutive rows per item,
-//   G lanes per row (G = 1..32 from the item's first, longest row, about
-//   kLaneEntries entries per lane), the item's rows taken 32/G at a time in
-//   G passes, so the per-row step after the sums runs once with all 32 lanes
-//   busy (an FP64 step issued with 32/G active lanes occupies this GPU's
-//   narrow FP64 pipe as long as a full one);
-// * setup passes (Ruiz, Pock-Chambolle) and the cluster path: 32/G rows per
-//   item, one pass.
-// No shared memory and no block-wide barrier on the hot path.
+// warps: a warp owns 32/G consecutive rows of similar length with G lanes per
+// row (G = 1..32, about kLaneEntries entries per lane). No shared memory and no
+// block-wide barrier on the hot path. (Items of 32 rows taken in G passes, so
+// that the per-row step runs with all lanes busy, left 4x fewer items than
+// resident warps on the 200k x 500k LP and doubled its attempt time.)
 struct WarpSched {
     const int* row;           // nwarps + 1 row boundaries
     const unsigned char* lg;  // log2(G) of each warp
@@ -411,67 +410,61 @@ struct PlainEpi {
     __device__ __forceinline__ void apply(int r, const A& acc, const NoPre&) { f(r, acc); }
 };
 
-// One warp item (32-row layout): every row of item `w` of A times x. Lane i
-// loads its epilogue vector entries for the item's i-th row first
-// (epi.load); then, pass by pass, each G-lane group walks one row's entries
-// in predicated batches of kLaneBatch per lane (all value and index loads of
-// a batch, then its gathers in flight), the group's shuffle reduction leaves
-// the sum in the group, and lane i collects it when its row is in the pass;
-// finally lane i applies the row step (epi.apply) to row i, so consecutive
-// lanes touch consecutive vector entries.
+// One warp item: every row of item `w` of A times x. The epilogue's vector
+// entries for the lane's row are loaded first (epi.load), then the row's
+// entries in predicated batches of kLaneBatch per lane (all value and index
+// loads of a batch, then its gathers in flight), the G-lane shuffle
+// reduction, and the row step (epi.apply) from lane i for the item's i-th
+// row, so consecutive lanes touch consecutive vector entries.
 template <typename T, class E>
 __device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
                                           const T* __restrict__ x, int w, E& epi) {
     const int lane = threadIdx.x & 31;
     const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
     const int lg = __ldg(ws.lg + w);
-    const int G = 1 << lg, per = 32 >> lg;  // lanes per row, rows per pass
+    const int G = 1 << lg;
     const int g = lane >> lg, gl = lane & (G - 1);
+    const int r = r0 + g;
     const int er = r0 + lane;
-    const bool has_epi = er < r1;
+    const bool has_epi = lane < (32 >> lg) && er < r1;
     typename E::Pre pre{};
     if (has_epi) pre = epi.load(er);
-    Acc<T> mine;
-    for (int k = 0; k < G; ++k) {  // pass k: rows r0 + k per ... + per - 1
-        const int r = r0 + k * per + g;
-        Acc<T> acc;
-        if (r < r1) {
-            const int b = __ldg(A.ptr + r), e = __ldg(A.ptr + r + 1);
-            for (int p = b + gl; p < e; p += kLaneBatch * G) {
-                T a[kLaneBatch];
-                int j[kLaneBatch];
-                if (A.stream) {  // uniform branch: one policy per batch
-                    const unsigned long long pol = l2_evict_first();
+    Acc<T> acc;
+    if (r < r1) {
+        const int b = __ldg(A.ptr + r), e = __ldg(A.ptr + r + 1);
+        for (int p = b + gl; p < e; p += kLaneBatch * G) {
+            T a[kLaneBatch];
+            int j[kLaneBatch];
+#if IGX_L2_STREAM
+            if (A.stream) {  // uniform branch: one policy per batch
+                const unsigned long long pol = l2_evict_first();
 #pragma unroll
-                    for (int u = 0; u < kLaneBatch; ++u) {
-                        const int q = p + u * G;
-                        const bool ok = q < e;
-                        a[u] = ok ? ld_first(A.val + q, pol) : T(0);
-                        j[u] = ok ? ld_first(A.idx + q, pol) : 0;
-                    }
-                } else {
-#pragma unroll
-                    for (int u = 0; u < kLaneBatch; ++u) {
-                        const int q = p + u * G;
-                        const bool ok = q < e;
-                        a[u] = ok ? __ldg(A.val + q) : T(0);
-                        j[u] = ok ? __ldg(A.idx + q) : 0;
-                    }
+                for (int u = 0; u < kLaneBatch; ++u) {
+                    const int q = p + u * G;
+                    const bool ok = q < e;
+                    a[u] = ok ? ld_first(A.val + q, pol) : T(0);
+                    j[u] = ok ? ld_first(A.idx + q, pol) : 0;
                 }
-                T xv[kLaneBatch];
+            } else
+#endif
+            {
 #pragma unroll
-                for (int u = 0; u < kLaneBatch; ++u) xv[u] = __ldg(x + j[u]);
-#pragma unroll
-                for (int u = 0; u < kLaneBatch; ++u) acc.add(a[u], xv[u]);  // masked: 0 * x[0] adds 0
+                for (int u = 0; u < kLaneBatch; ++u) {
+                    const int q = p + u * G;
+                    const bool ok = q < e;
+                    a[u] = ok ? __ldg(A.val + q) : T(0);
+                    j[u] = ok ? __ldg(A.idx + q) : 0;
+                }
             }
+            T xv[kLaneBatch];
+#pragma unroll
+            for (int u = 0; u < kLaneBatch; ++u) xv[u] = __ldg(x + j[u]);
+#pragma unroll
+            for (int u = 0; u < kLaneBatch; ++u) acc.add(a[u], xv[u]);  // masked: 0 * x[0] adds 0
         }
-        for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(0xffffffffu, o, G);
-        // lane k per + i takes row r0 + k per + i, whose sum its G-lane
-        // group (from lane i G) holds
-        const Acc<T> t = acc.shfl_from(0xffffffffu, ((lane - k * per) << lg) & 31);
-        if ((lane >> (5 - lg)) == k) mine = t;
-        if ((k + 1) * per >= r1 - r0) break;  // uniform: the item's rows are done
     }
+    for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(0xffffffffu, o, G);
+    const Acc<T> mine = acc.shfl_from(0xffffffffu, (lane << lg) & 31);
     if (has_epi) epi.apply(er, mine, pre);
 }
 

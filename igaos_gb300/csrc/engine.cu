@@ -56,7 +56,7 @@ std::vector<int> length_order(const int* ptr, int rows) {
 }
 
 void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<unsigned char>& wlg,
-                 int entries, bool full) {
+                 int entries) {
     wrow.assign(1, 0);
     wlg.clear();
     int r = 0;
@@ -64,7 +64,7 @@ void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<u
         const int len = ptr[r + 1] - ptr[r];
         int lg = 0;
         while (lg < 5 && (1 << lg) * entries < len) ++lg;
-        r = std::min(rows, r + (full ? 32 : (32 >> lg)));
+        r = std::min(rows, r + (32 >> lg));
         wrow.push_back(r);
         wlg.push_back((unsigned char)lg);
     }
@@ -118,10 +118,10 @@ static bool small_share(const int* ptr, int rows, std::vector<long long>& ent,
 // resident (6 CTAs of 256 threads per SM at <= 40 registers); the kernels
 // grid-stride over the items.
 static Sched upload_sched(Arena& ar, const int* ptr, int rows, int resident_ctas,
-                          int entries, bool full) {
+                          int entries) {
     std::vector<int> wr;
     std::vector<unsigned char> wl;
-    build_warps(ptr, rows, wr, wl, entries, full);
+    build_warps(ptr, rows, wr, wl, entries);
     Sched s;
     s.entries = entries;
     s.nwarps = (int)wl.size();
@@ -229,13 +229,9 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         int sms = 0;
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
         const int resident = std::max(1, sms) * kHotCtasPerSm;
-        // IGAOS_PDHG_ITEM_LAYOUT=onepass: the products use the one-pass
-        // layout too (measurement)
-        const char* lay = std::getenv("IGAOS_PDHG_ITEM_LAYOUT");
-        const bool full = !(lay && std::strcmp(lay, "onepass") == 0);
-        sRA_ = upload_sched(ar_, P.data(), m, resident, kLaneEntries, false);
+        sRA_ = upload_sched(ar_, P.data(), m, resident, kLaneEntries);
         for (int c = 0; c < 3; ++c) {
-            candA_[c] = upload_sched(ar_, P.data(), m, resident, kTuneEntries[c], full);
+            candA_[c] = upload_sched(ar_, P.data(), m, resident, kTuneEntries[c]);
             if (kTuneEntries[c] == kLaneEntries) sA_ = candA_[c];
             cap_ctas_A_ = std::max(cap_ctas_A_, candA_[c].ctas);
         }
@@ -245,9 +241,9 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(ci_, I.get(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(acx_, V.get(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
-        sRAT_ = upload_sched(ar_, P.data(), n, resident, kLaneEntries, false);
+        sRAT_ = upload_sched(ar_, P.data(), n, resident, kLaneEntries);
         for (int c = 0; c < 3; ++c) {
-            candAT_[c] = upload_sched(ar_, P.data(), n, resident, kTuneEntries[c], full);
+            candAT_[c] = upload_sched(ar_, P.data(), n, resident, kTuneEntries[c]);
             if (kTuneEntries[c] == kLaneEntries) sAT_ = candAT_[c];
             cap_ctas_AT_ = std::max(cap_ctas_AT_, candAT_[c].ctas);
         }
@@ -562,7 +558,7 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     const int gp = f64 ? sAT_.ctas64 : sAT_.ctas, gd = f64 ? sA_.ctas64 : sA_.ctas;
     if (const int sb = small_bytes_[std::is_same<T, double>::value ? 1 : 0]) {
         // one cluster runs the whole chunk with the LP in shared memory (it
-        // stages the one-pass layout)
+        // stages the default schedule)
         pa.ws = sRAT_.view();
         da.ws = sRA_.view();
         ++launches_;

@@ -54,10 +54,8 @@ struct Sched {
 
 // Host-side warp schedule of a (length-sorted) CSR row pointer: consecutive
 // rows dealt to warps, G lanes per row from the first row's length.
-// full: items of 32 rows taken in G passes (the products' layout); else
-// 32/G rows per item (setup passes and the cluster path)
 void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<unsigned char>& wlg,
-                 int entries = kLaneEntries, bool full = false);
+                 int entries = kLaneEntries);
 
 // Entries per lane of the schedules the autotuner chooses from (the first
 // value that is not the default is tried first; kLaneEntries is the default).
@@ -176,7 +174,7 @@ class Engine {
     double *ax_, *acx_;
     float *ax32_, *acx32_;
     Sched sA_, sAT_;
-    Sched sRA_, sRAT_;  // one-pass layout (setup passes, cluster path)
+    Sched sRA_, sRAT_;  // default schedules (setup passes, cluster path)
     // warp schedules of A and A^T for every kTuneEntries value; sA_ / sAT_
     // are one of them (kLaneEntries unless the autotuner chose otherwise)
     Sched candA_[3], candAT_[3];
