@@ -230,7 +230,7 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device_));
         const int resident = std::max(1, sms) * kHotCtasPerSm;
         sRA_ = upload_sched(ar_, P.data(), m, resident, kLaneEntries);
-        for (int c = 0; c < 3; ++c) {
+        for (int c = 0; c < kTuneCount; ++c) {
             candA_[c] = upload_sched(ar_, P.data(), m, resident, kTuneEntries[c]);
             if (kTuneEntries[c] == kLaneEntries) sA_ = candA_[c];
             cap_ctas_A_ = std::max(cap_ctas_A_, candA_[c].ctas);
@@ -242,7 +242,7 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         CU(cudaMemcpy(ci_, I.get(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
         CU(cudaMemcpy(acx_, V.get(), sizeof(double) * nnz, cudaMemcpyHostToDevice));
         sRAT_ = upload_sched(ar_, P.data(), n, resident, kLaneEntries);
-        for (int c = 0; c < 3; ++c) {
+        for (int c = 0; c < kTuneCount; ++c) {
             candAT_[c] = upload_sched(ar_, P.data(), n, resident, kTuneEntries[c]);
             if (kTuneEntries[c] == kLaneEntries) sAT_ = candAT_[c];
             cap_ctas_AT_ = std::max(cap_ctas_AT_, candAT_[c].ctas);
@@ -581,7 +581,7 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     }
     // key: precision, attempt count, vector set
     const GraphKey key{std::is_same<T, double>::value ? 1 : 2, count,
-                       (uintptr_t)VecSel<T>::c(v), 3 * ia_ + iat_};
+                       (uintptr_t)VecSel<T>::c(v), kTuneCount * ia_ + iat_};
     auto it = graphs_.find(key);
     if (it == graphs_.end()) {
         cudaGraph_t g;
@@ -617,7 +617,7 @@ void Engine::tune() {
     const int pi = std::is_same<T, double>::value ? 1 : 0;
     if (choice_[pi][0] >= 0) return;
     int def = 0;
-    for (int c = 0; c < 3; ++c)
+    for (int c = 0; c < kTuneCount; ++c)
         if (kTuneEntries[c] == kLaneEntries) def = c;
     if (small_bytes_[pi]) {
         choice_[pi][0] = choice_[pi][1] = def;
@@ -643,7 +643,7 @@ void Engine::tune() {
     cudaEvent_t e[3];
     for (auto& ev : e) CU(cudaEventCreate(&ev));
     const bool f64 = pi == 1;
-    for (int c = 0; c < 3; ++c) {
+    for (int c = 0; c < kTuneCount; ++c) {
         use_sched(c, c);
         PrimalArgs<T> pa;
         DualArgs<T> da;
@@ -668,7 +668,7 @@ void Engine::tune() {
     for (auto& ev : e) cudaEventDestroy(ev);
     for (int o = 0; o < 2; ++o) {
         int best = def;
-        for (int c = 0; c < 3; ++c)
+        for (int c = 0; c < kTuneCount; ++c)
             if (tune_us_[pi][o][c] < tune_us_[pi][o][best]) best = c;
         choice_[pi][o] = best;
     }
@@ -1332,17 +1332,19 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
     // attempt kernels' precision (timed once per handle and precision)
     const int pi = o.precision == IGAOS_PDHG_FP64 ? 1 : 0;
     int def = 0;
-    for (int c = 0; c < 3; ++c)
+    for (int c = 0; c < kTuneCount; ++c)
         if (kTuneEntries[c] == kLaneEntries) def = c;
     if (o.schedule == IGAOS_PDHG_SCHEDULE_AUTOTUNE) {
         if (pi) tune<double>();
         else tune<float>();
         use_sched(choice_[pi][0], choice_[pi][1]);
         if (o.verbosity > 0)
-            std::fprintf(stderr, "[pdhg-gb300] autotuned schedule (us per launch at 4/8/16 "
-                                 "entries per lane): A %.1f/%.1f/%.1f -> %d, A^T %.1f/%.1f/%.1f -> %d\n",
-                         tune_us_[pi][0][0], tune_us_[pi][0][1], tune_us_[pi][0][2], sA_.entries,
-                         tune_us_[pi][1][0], tune_us_[pi][1][1], tune_us_[pi][1][2], sAT_.entries);
+            std::fprintf(stderr, "[pdhg-gb300] autotuned schedule (us per launch at 2/4/8/16 "
+                                 "entries per lane): A %.1f/%.1f/%.1f/%.1f -> %d, A^T "
+                                 "%.1f/%.1f/%.1f/%.1f -> %d\n",
+                         tune_us_[pi][0][0], tune_us_[pi][0][1], tune_us_[pi][0][2],
+                         tune_us_[pi][0][3], sA_.entries, tune_us_[pi][1][0], tune_us_[pi][1][1],
+                         tune_us_[pi][1][2], tune_us_[pi][1][3], sAT_.entries);
     } else {
         use_sched(def, def);
     }

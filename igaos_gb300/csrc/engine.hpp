@@ -59,7 +59,8 @@ void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<u
 
 // Entries per lane of the schedules the autotuner chooses from (the first
 // value that is not the default is tried first; kLaneEntries is the default).
-constexpr int kTuneEntries[3] = {4, 8, 16};
+constexpr int kTuneCount = 4;
+constexpr int kTuneEntries[kTuneCount] = {2, 4, 8, 16};
 
 // Permutation sorting rows by decreasing length (stable): new -> old index.
 std::vector<int> length_order(const int* ptr, int rows);
@@ -98,7 +99,7 @@ template <typename T> struct DualArgs;
 struct GraphKey {
     int prec, count;
     uintptr_t vecs;
-    int sched;  // schedules in use (3 * index of A's + index of A^T's)
+    int sched;  // schedules in use (kTuneCount * index of A's + index of A^T's)
     bool operator<(const GraphKey& o) const {
         if (prec != o.prec) return prec < o.prec;
         if (count != o.count) return count < o.count;
@@ -177,11 +178,11 @@ class Engine {
     Sched sRA_, sRAT_;  // default schedules (setup passes, cluster path)
     // warp schedules of A and A^T for every kTuneEntries value; sA_ / sAT_
     // are one of them (kLaneEntries unless the autotuner chose otherwise)
-    Sched candA_[3], candAT_[3];
+    Sched candA_[kTuneCount], candAT_[kTuneCount];
     int cap_ctas_A_ = 0, cap_ctas_AT_ = 0;  // largest launch width of the candidates
-    int ia_ = 1, iat_ = 1;                  // candidates in use as sA_ / sAT_
+    int ia_ = 2, iat_ = 2;                  // candidates in use as sA_ / sAT_
     int choice_[2][2] = {{-1, -1}, {-1, -1}};  // autotuned (A, A^T) per FP32 / FP64
-    float tune_us_[2][2][3] = {};           // per attempt-kernel launch, us
+    float tune_us_[2][2][kTuneCount] = {};  // per attempt-kernel launch, us
     void use_sched(int ia, int iat);
     template <typename T> void tune();
     template <typename T> void attempt_args(const Vecs& v, PrimalArgs<T>& pa, DualArgs<T>& da);
