@@ -256,6 +256,7 @@ def config_dict(lp, args):
                         "degrees, |A_ij| log-uniform [1e-3,1e3], box [0,10]); one solve of "
                         f"{args.iters} PDHG iterations per step",
             "m": lp.m, "n": lp.n, "nnz": lp.nnz, "precision": args.precision,
+            "schedule": args.schedule,
             "iters_per_step": args.iters, "l2": "flushed between steps (512 MiB write)",
             "parallelism": f"replicas x{args.gpus}"}
 
@@ -436,6 +437,8 @@ def main():
     ap.add_argument("--no-c2-tol", action="store_true", help="skip the large LP to 1e-4")
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="skip the reference GPU PDHG comparison")
+    ap.add_argument("--schedule", default="fixed", choices=["fixed", "autotune"],
+                    help="warp schedule of the headline steps and the attempts-c5 probe")
     ap.add_argument("--c2-budget", type=float, default=100.0,
                     help="seconds for the FP32 + refinement solve of the large LP to 1e-4 "
                          "(FP64 gets 0.6 of it)")
@@ -463,7 +466,7 @@ def main():
         cb = bytes_per_attempt(flp.m, flp.n, flp.nnz, 8 if args.precision == "fp64" else 4)
         with capi.Problem(flp, device=local) as P:
             o = dict(precision=args.precision, tolerance=1e-12, time_limit=1e9,
-                     max_iterations=args.iters)
+                     max_iterations=args.iters, schedule=args.schedule)
             P.solve(**o)
             r = P.solve(**o)
         us = 1e3 * r["attempt_time_ms"] / max(1, r["attempts"])
@@ -471,6 +474,7 @@ def main():
         print(json.dumps({"workload": f"multicommodity flow m={flp.m} n={flp.n} nnz={flp.nnz}",
                           "precision": args.precision, "iterations": r["iterations"],
                           "attempts": r["attempts"], "attempt_us": us, "attempt_bytes": cb,
+                          "entries_per_lane": [r["entries_a"], r["entries_at"]],
                           "attempt_hbm_frac": cb / (us * 1e-6) / 1e9 / pk,
                           "hbm_peak_kind": pk_kind}), flush=True)
         return
@@ -483,7 +487,7 @@ def main():
 
     def steps(P, prec, count, timed):
         o = dict(precision=prec, tolerance=1e-12, time_limit=1e9, max_iterations=args.iters,
-                 device=local)
+                 device=local, schedule=args.schedule)
         res = []
         for _ in range(count):
             if timed:

@@ -61,8 +61,9 @@ struct Csr {
     int rows;
     // 1: values and indices are read with an L2 evict-first policy, so that a
     // matrix streamed once per product does not push the iterate vectors
-    // (reused by the next launch) out of L2 (LPs whose attempt working set
-    // exceeds L2); 0: plain read-only loads
+    // (reused by the next launch) out of L2 (FP32 products of LPs whose
+    // attempt working set exceeds L2; multicommodity LP: 72.5 -> 70.1 us per
+    // attempt); 0: plain read-only loads
     int stream = 0;
 };
 
@@ -436,7 +437,9 @@ __device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
             T a[kLaneBatch];
             int j[kLaneBatch];
 #if IGX_L2_STREAM
-            if (A.stream) {  // uniform branch: one policy per batch
+            // FP32 products only: in the FP64 ones the branch alone cost 3-5 %
+            // and streaming gained nothing (they are FP64-pipe bound)
+            if (sizeof(T) == 4 && A.stream) {  // uniform branch: one policy per batch
                 const unsigned long long pol = l2_evict_first();
 #pragma unroll
                 for (int u = 0; u < kLaneBatch; ++u) {
