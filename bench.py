@@ -437,8 +437,9 @@ def main():
     ap.add_argument("--no-c2-tol", action="store_true", help="skip the large LP to 1e-4")
     ap.add_argument("--no-ref-gpu", action="store_true",
                     help="skip the reference GPU PDHG comparison")
-    ap.add_argument("--schedule", default="fixed", choices=["fixed", "autotune"],
-                    help="warp schedule of the headline steps and the attempts-c5 probe")
+    ap.add_argument("--schedule", default="autotune", choices=["fixed", "autotune"],
+                    help="warp schedule of the headline steps and the attempts-c5 probe "
+                         "(autotune: timed once per handle and precision, in the warm-up)")
     ap.add_argument("--c2-budget", type=float, default=100.0,
                     help="seconds for the FP32 + refinement solve of the large LP to 1e-4 "
                          "(FP64 gets 0.6 of it)")
@@ -618,6 +619,7 @@ def main():
         "clocks": ck,
         "kkt_passes_per_s": ws * att / (dev_ms_max / 1e3),
         "iterations_per_step": res[-1]["iterations"], "attempts_per_step": res[-1]["attempts"],
+        "entries_per_lane": {"A": res[-1]["entries_a"], "A^T": res[-1]["entries_at"]},
         alt.replace("-", "_"): {
             "value": bpa_alt * att_alt / (dev_ms_alt / 1e3) / 1e9, "unit": "GB/s",
             "ms_per_step": dev_ms_alt / len(res_alt),
