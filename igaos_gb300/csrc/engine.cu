@@ -1339,12 +1339,13 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
         else tune<float>();
         use_sched(choice_[pi][0], choice_[pi][1]);
         if (o.verbosity > 0)
-            std::fprintf(stderr, "[pdhg-gb300] autotuned schedule (us per launch at 2/4/8/16 "
-                                 "entries per lane): A %.1f/%.1f/%.1f/%.1f -> %d, A^T "
-                                 "%.1f/%.1f/%.1f/%.1f -> %d\n",
+            std::fprintf(stderr, "[pdhg-gb300] autotuned schedule (us per launch at 2/4/8/16/32 "
+                                 "entries per lane): A %.1f/%.1f/%.1f/%.1f/%.1f -> %d, A^T "
+                                 "%.1f/%.1f/%.1f/%.1f/%.1f -> %d\n",
                          tune_us_[pi][0][0], tune_us_[pi][0][1], tune_us_[pi][0][2],
-                         tune_us_[pi][0][3], sA_.entries, tune_us_[pi][1][0], tune_us_[pi][1][1],
-                         tune_us_[pi][1][2], tune_us_[pi][1][3], sAT_.entries);
+                         tune_us_[pi][0][3], tune_us_[pi][0][4], sA_.entries, tune_us_[pi][1][0],
+                         tune_us_[pi][1][1], tune_us_[pi][1][2], tune_us_[pi][1][3],
+                         tune_us_[pi][1][4], sAT_.entries);
     } else {
         use_sched(def, def);
     }

@@ -59,8 +59,8 @@ void build_warps(const int* ptr, int rows, std::vector<int>& wrow, std::vector<u
 
 // Entries per lane of the schedules the autotuner chooses from (the first
 // value that is not the default is tried first; kLaneEntries is the default).
-constexpr int kTuneCount = 4;
-constexpr int kTuneEntries[kTuneCount] = {2, 4, 8, 16};
+constexpr int kTuneCount = 5;
+constexpr int kTuneEntries[kTuneCount] = {2, 4, 8, 16, 32};
 
 // Permutation sorting rows by decreasing length (stable): new -> old index.
 std::vector<int> length_order(const int* ptr, int rows);
@@ -180,7 +180,7 @@ class Engine {
     // are one of them (kLaneEntries unless the autotuner chose otherwise)
     Sched candA_[kTuneCount], candAT_[kTuneCount];
     int cap_ctas_A_ = 0, cap_ctas_AT_ = 0;  // largest launch width of the candidates
-    int ia_ = 2, iat_ = 2;                  // candidates in use as sA_ / sAT_
+    int ia_ = 2, iat_ = 2;                  // candidates in use as sA_ / sAT_ (8 entries)
     int choice_[2][2] = {{-1, -1}, {-1, -1}};  // autotuned (A, A^T) per FP32 / FP64
     float tune_us_[2][2][kTuneCount] = {};  // per attempt-kernel launch, us
     void use_sched(int ia, int iat);
