@@ -205,6 +205,12 @@ def batch_probe(capi, G, sample=24, count=4096, warm=True):
         "status": st, "kernel_ms": kms, "call_s": wall,
         "lps_per_s": len(lps) / wall, "lps_per_s_kernel": len(lps) / (kms / 1e3),
         "iterations_median": float(np.median([r["iterations"] for r in out])),
+        "iterations_p99_max": [float(np.percentile([r["iterations"] for r in out], 99)),
+                               float(max(r["iterations"] for r in out))],
+        "instances_over": {str(k): int(sum(r["iterations"] > k for r in out))
+                           for k in (20000, 50000, 100000)},
+        "finished_fp64": int(sum(r.get("finished_fp64", 0) for r in out)),
+        "instance_ms_max": float(max(r["instance_time_ms"] for r in out)),
     }
     if sample > 0:
         idx = np.random.default_rng(0).choice(len(lps), min(sample, len(lps)), replace=False)
