@@ -623,7 +623,11 @@ def main():
         "e2e": e2e,
         "gpu_launches": launches,
         "clocks": ck,
-        "kkt_passes_per_s": ws * att / (dev_ms_max / 1e3),
+        "attempts_per_s": ws * att / (dev_ms_max / 1e3),
+        # device time outside the fused attempts (KKT checks, restarts, the
+        # step's setup) per 64-iteration check
+        "check_us": 1e3 * (sum(r["device_time_ms"] for r in res) - att_ms)
+                    / max(1, sum(r["iterations"] // 64 for r in res)),
         "iterations_per_step": res[-1]["iterations"], "attempts_per_step": res[-1]["attempts"],
         "entries_per_lane": {"A": res[-1]["entries_a"], "A^T": res[-1]["entries_at"]},
         alt.replace("-", "_"): {

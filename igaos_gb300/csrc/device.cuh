@@ -411,25 +411,18 @@ struct PlainEpi {
     __device__ __forceinline__ void apply(int r, const A& acc, const NoPre&) { f(r, acc); }
 };
 
-// One warp item: every row of item `w` of A times x. The epilogue's vector
-// entries for the lane's row are loaded first (epi.load), then the row's
-// entries in predicated batches of kLaneBatch per lane (all value and index
-// loads of a batch, then its gathers in flight), the G-lane shuffle
-// reduction, and the row step (epi.apply) from lane i for the item's i-th
-// row, so consecutive lanes touch consecutive vector entries.
-template <typename T, class E>
-__device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
-                                          const T* __restrict__ x, int w, E& epi) {
+// The row sums of one warp item: rows [r0, r1) of A times x with 2^lg
+// lanes per row, the row's entries in predicated batches of kLaneBatch per
+// lane (all value and index loads of a batch, then its gathers in flight),
+// the G-lane shuffle reduction, and the sum of the item's i-th row handed to
+// lane i, so consecutive lanes touch consecutive vector entries.
+template <typename T>
+__device__ __forceinline__ Acc<T> item_sums(const Csr<T>& A, const T* __restrict__ x, int r0,
+                                            int r1, int lg) {
     const int lane = threadIdx.x & 31;
-    const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
-    const int lg = __ldg(ws.lg + w);
     const int G = 1 << lg;
     const int g = lane >> lg, gl = lane & (G - 1);
     const int r = r0 + g;
-    const int er = r0 + lane;
-    const bool has_epi = lane < (32 >> lg) && er < r1;
-    typename E::Pre pre{};
-    if (has_epi) pre = epi.load(er);
     Acc<T> acc;
     if (r < r1) {
         const int b = __ldg(A.ptr + r), e = __ldg(A.ptr + r + 1);
@@ -467,7 +460,23 @@ __device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
         }
     }
     for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(0xffffffffu, o, G);
-    const Acc<T> mine = acc.shfl_from(0xffffffffu, (lane << lg) & 31);
+    return acc.shfl_from(0xffffffffu, (lane << lg) & 31);
+}
+
+// One warp item with its row steps in place: the epilogue's vector entries
+// for the lane's row are loaded first (epi.load), then the row sums, then
+// the row step (epi.apply) on the 32/G lanes that hold a row.
+template <typename T, class E>
+__device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
+                                          const T* __restrict__ x, int w, E& epi) {
+    const int lane = threadIdx.x & 31;
+    const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
+    const int lg = __ldg(ws.lg + w);
+    const int er = r0 + lane;
+    const bool has_epi = lane < (32 >> lg) && er < r1;
+    typename E::Pre pre{};
+    if (has_epi) pre = epi.load(er);
+    const Acc<T> mine = item_sums<T>(A, x, r0, r1, lg);
     if (has_epi) epi.apply(er, mine, pre);
 }
 
@@ -480,6 +489,70 @@ __device__ __forceinline__ void warp_rows_all(const WarpSched& ws, const Csr<T>&
     for (int w = blockIdx.x * kWarps + (threadIdx.x >> 5); w < ws.nwarps; w += stride)
         warp_item<T>(ws, A, x, w, epi);
 }
+
+// The same items with deferred row steps: each warp parks its items' row
+// sums (row index and sum) in shared memory and runs the row steps 32 rows
+// at a time, on all 32 lanes. An item with G lanes per row holds only 32/G
+// rows, and on GB300 an FP64 instruction issued with partial lanes occupies
+// the narrow FP64 pipe as long as a full one; deferred, the FP64 row steps
+// cost 1/G of the issues. The products, their order and every row's
+// arithmetic are unchanged; only which lane runs a row's step, and when,
+// differ. `park` holds kWarps * 64 entries.
+template <typename T>
+struct Parked {
+    int row;
+    Acc<T> sum;
+};
+
+template <typename T, class E>
+__device__ __forceinline__ void warp_rows_deferred(const WarpSched& ws, const Csr<T>& A,
+                                                   const T* __restrict__ x, E& epi,
+                                                   Parked<T>* park) {
+    const int lane = threadIdx.x & 31;
+    Parked<T>* wp = park + (threadIdx.x >> 5) * 64;
+    int cnt = 0;  // parked rows (< 32 between items; < 64 after one)
+    const int stride = gridDim.x * kWarps;
+    for (int w = blockIdx.x * kWarps + (threadIdx.x >> 5); w < ws.nwarps; w += stride) {
+        const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
+        const int lg = __ldg(ws.lg + w);
+        const int nr = min(32 >> lg, r1 - r0);
+        const Acc<T> mine = item_sums<T>(A, x, r0, r1, lg);
+        if (lane < nr) {
+            wp[cnt + lane].row = r0 + lane;
+            wp[cnt + lane].sum = mine;
+        }
+        cnt += nr;
+        __syncwarp();
+        if (cnt >= 32) {
+            const Parked<T> mine_p = wp[lane];
+            const bool carry = lane < cnt - 32;
+            Parked<T> rest;
+            if (carry) rest = wp[32 + lane];
+            __syncwarp();
+            if (carry) wp[lane] = rest;
+            cnt -= 32;
+            __syncwarp();
+            const typename E::Pre pre = epi.load(mine_p.row);
+            epi.apply(mine_p.row, mine_p.sum, pre);
+        }
+    }
+    if (lane < cnt) {
+        const Parked<T> mine_p = wp[lane];
+        const typename E::Pre pre = epi.load(mine_p.row);
+        epi.apply(mine_p.row, mine_p.sum, pre);
+    }
+}
+
+// Deferred row steps per iterate precision (compile switches for A/B
+// builds): FP64 row steps are bound by the FP64 pipe's issue slots.
+#ifndef IGX_DEFER_F64
+#define IGX_DEFER_F64 0
+#endif
+#ifndef IGX_DEFER_F32
+#define IGX_DEFER_F32 0
+#endif
+template <typename T> struct DeferSteps { static constexpr bool value = IGX_DEFER_F32 != 0; };
+template <> struct DeferSteps<double> { static constexpr bool value = IGX_DEFER_F64 != 0; };
 
 
 }  // namespace igx

@@ -325,7 +325,9 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     std::memset(h_ctl_, 0, sizeof(DevCtl));
     red_blocks_ = grid_for(std::max(m, n), kThreads, 152 * 4);
     const int kkt_blocks = std::max(std::max(cap_ctas_A_, cap_ctas_AT_), red_blocks_);
-    kkt_part_ = ar_.alloc<double>((size_t)2 * kkt_blocks * 4);
+    kkt_part_ = ar_.alloc<double>((size_t)2 * kkt_blocks * 8);
+    kkt_ax_ = ar_.alloc<double>((size_t)2 * m);
+    kkt_aty_ = ar_.alloc<double>((size_t)2 * n);
     red_part_ = ar_.alloc<double>((size_t)2 * red_blocks_ + 8);
     scal_ = ar_.alloc<double>(16);
     ticket_ = ar_.alloc<unsigned int>(4);
@@ -729,14 +731,14 @@ void Engine::run_until_stop(const Vecs& v, bool graphs, LoopOut& out) {
 template <typename T>
 void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* y1, int ncand) {
     KktArgs<T> ka;
-    ka.wsA = sA_.view();
-    ka.wsAT = sAT_.view();
-    ka.A = csrA<T>();
-    ka.AT = csrAT<T>();
     ka.x[0] = x0;
     ka.y[0] = y0;
     ka.x[1] = x1;
     ka.y[1] = y1;
+    ka.ax[0] = kkt_ax_;
+    ka.ax[1] = kkt_ax_ + m;
+    ka.aty[0] = kkt_aty_;
+    ka.aty[1] = kkt_aty_ + n;
     ka.dr = dr_;
     ka.dc = dc_;
     ka.idr = idr_;
@@ -754,10 +756,13 @@ void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* 
     ka.part = kkt_part_;
     ka.out = met_;
     ka.ticket = ticket_ + 2;
-    launches_ += 3;
-    k_kkt_rows<T><<<dim3(sA_.ctas, ncand), kThreads, 0, st_>>>(ka);
-    k_kkt_cols<T><<<dim3(sAT_.ctas, ncand), kThreads, 0, st_>>>(ka);
-    k_kkt_rowdual<T><<<dim3(red_blocks_, ncand), kThreads, 0, st_>>>(ka, m);
+    launches_ += 4;
+    k_kkt_prod<T><<<dim3(sA_.ctas, ncand), kThreads, 0, st_>>>(sA_.view(), csrA<T>(), x0, x1,
+                                                              kkt_ax_, kkt_ax_ + m);
+    k_kkt_prod<T><<<dim3(sAT_.ctas, ncand), kThreads, 0, st_>>>(sAT_.view(), csrAT<T>(), y0, y1,
+                                                               kkt_aty_, kkt_aty_ + n);
+    k_kkt_rows<T><<<dim3(red_blocks_, ncand), kThreads, 0, st_>>>(ka, m);
+    k_kkt_cols<T><<<dim3(red_blocks_, ncand), kThreads, 0, st_>>>(ka, n, m);
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(h_met_, met_, ncand * sizeof(DevMetrics), cudaMemcpyDeviceToHost, st_));
     CU(cudaStreamSynchronize(st_));

@@ -204,6 +204,8 @@ class Engine {
     DevMetrics* met_ = nullptr;    // device [2]
     DevMetrics* h_met_ = nullptr;  // pinned mirror [2]
     double* kkt_part_ = nullptr;
+    double* kkt_ax_ = nullptr;     // device [2m]: A~ x~ of the KKT candidates
+    double* kkt_aty_ = nullptr;    // device [2n]: A~^T y~ of the KKT candidates
     double* red_part_ = nullptr;
     double* scal_ = nullptr;       // device scalars
     double* h_scal_ = nullptr;     // pinned

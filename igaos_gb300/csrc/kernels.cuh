@@ -104,6 +104,19 @@ struct PrimalEpi {
     }
 };
 
+// The attempt kernels' traversal: row steps in place, or deferred to full
+// warps (DeferSteps: FP64 by default).
+template <typename T, class E>
+__device__ __forceinline__ void rows_with_steps(const WarpSched& ws, const Csr<T>& M,
+                                                const T* __restrict__ v, E& epi) {
+    if constexpr (DeferSteps<T>::value) {
+        __shared__ __align__(16) unsigned char park[kWarps * 64 * sizeof(Parked<T>)];
+        warp_rows_deferred<T>(ws, M, v, epi, reinterpret_cast<Parked<T>*>(park));
+    } else {
+        warp_rows_all<T>(ws, M, v, epi);
+    }
+}
+
 template <typename T>
 __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_primal(PrimalArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
@@ -112,7 +125,7 @@ __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_primal(PrimalAr
     const int p = cv.parity, q = p ^ 1;
     PrimalEpi<T> epi{a.c, a.lo, a.hi, a.x[p], a.xavg[p], a.x[q], a.xavg[q], a.xbar,
                      cv.tau, cv.w, (T)0};
-    warp_rows_all<T>(a.ws, a.AT, a.y[p], epi);
+    rows_with_steps<T>(a.ws, a.AT, a.y[p], epi);
     const T dx2 = epi.dx2;
     T v[1] = {dx2};
     block_sum_t<T, 1>(v, reinterpret_cast<T*>(smred));
@@ -249,7 +262,7 @@ __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_dual(DualArgs<T
     const int p = cv.parity, q = p ^ 1;
     DualEpi<T> epi{a.rmin, a.rmax, a.y[p], a.axc[p], a.yavg[p], a.yhat, a.y[q], a.axc[q], a.yavg[q],
                    cv.sigma, cv.isigma, cv.w, (T)0, (T)0};
-    warp_rows_all<T>(a.ws, a.A, a.xbar, epi);
+    rows_with_steps<T>(a.ws, a.A, a.xbar, epi);
     T v[2] = {epi.dy2, epi.cross};
     block_sum_t<T, 2>(v, reinterpret_cast<T*>(smred));
     if (threadIdx.x == 0) {
@@ -527,18 +540,24 @@ __global__ void k_convert(int n, const TI* __restrict__ in, TO* __restrict__ out
 // --------------------------------------------------------------- KKT pass
 // FP64 metrics of candidate pairs (x~, y~) in ORIGINAL units, one fused
 // device pass replacing metrics_of + evaluate (src/pdhg/pdhg.cu:698-733,
-// 173-254). Candidate v = blockIdx.y. Three launches:
-//   rows  : A x -> pinf numerator/normaliser, prow, max |y|
-//   cols  : A^T y -> reduced costs d, dinf, c^T x, column part of the bound
-//   rowdual: row part of the Lagrangian bound (needs max |y| for its noise
-//            threshold) and the final metrics.
+// 173-254). Candidate v = blockIdx.y. Four launches:
+//   prod (A)  : A~ x~ over the warp schedule, stored in FP64 (scaled units)
+//   prod (A^T): A~^T y~, likewise
+//   rows      : one thread per row: pinf numerator/normaliser, prow, max |y|
+//   cols      : one thread per column: reduced costs d, dinf, c^T x, the
+//               column part of the Lagrangian bound; then one thread per row
+//               for its row part (needs max |y| for its noise threshold) and
+//               the final metrics.
+// The metrics run with every lane of a warp busy: inside the warp schedule
+// only 32/G lanes hold a row, and an FP64 instruction issued with partial
+// lanes occupies GB300's narrow FP64 pipe as long as a full one.
 
 template <typename T>
 struct KktArgs {
-    WarpSched wsA, wsAT;
-    Csr<T> A, AT;
     const T* x[2];
     const T* y[2];
+    const double* ax[2];                      // A~ x~ per candidate (scaled units)
+    const double* aty[2];                     // A~^T y~ per candidate (scaled units)
     const double *dr, *dc;
     const double* idr;                        // 1 / dr (IEEE quotients)
     const double* idc;                        // 1 / dc (IEEE quotients)
@@ -548,34 +567,47 @@ struct KktArgs {
     const double *c, *cl, *cu, *rmin, *rmax;  // original units
     const T *slo, *shi;                       // scaled column bounds, iterate precision
     double cmax;
-    double* part;   // >= 2 * max(tiles) * 4 doubles
+    double* part;   // >= 2 * blocks * 8 doubles
     DevMetrics* out;
     unsigned int* ticket;
 };
 
+// Products of both candidates: out[v] = M v_in[v] in FP64 (the same warp
+// traversal and accumulator as every other product of the engine).
 template <typename T>
-__global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_kkt_rows(KktArgs<T> a) {
+__global__ void __launch_bounds__(kThreads, HotCtas<T>::value)
+    k_kkt_prod(WarpSched ws, Csr<T> M, const T* in0, const T* in1, double* out0, double* out1) {
+    const T* __restrict__ in = blockIdx.y ? in1 : in0;
+    double* __restrict__ out = blockIdx.y ? out1 : out0;
+    auto f = [&](int r, const Acc<T>& acc) { out[r] = acc.result_d(); };
+    PlainEpi<decltype(f)> epi{f};
+    warp_rows_all<T>(ws, M, in, epi);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a, int m) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const int v = blockIdx.y;
     const T* __restrict__ yv = a.y[v];
+    const double* __restrict__ axv = a.ax[v];
     double pv = 0.0, pa = 0.0, prow = 0.0, ymax = 0.0;
     // comparisons on the integer pipe (dmax, dmin, ...; see device.cuh)
-    auto f = [&](int i, const Acc<T>& acc) {
-        const double Ax = acc.result_d() * a.dr[i];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const double Ax = axv[i] * a.dr[i];
         const double lo = a.rmin[i], hi = a.rmax[i];
         const double vi = dmax(lo - Ax, Ax - hi);
         pv = dmax(pv, vi);
         pa = dmax(pa, dabs(dmin(dmax(Ax, lo), hi)));
-        if (dgt0(vi)) {  // viol / (1 + sc) is 0 otherwise: skip the FP64 division
+        // vi / (1 + sc) <= vi: the FP64 division only when vi beats this
+        // thread's running maximum (with prow = 0 that is vi > 0)
+        if (dlt(prow, vi)) {
             double sc = dabs(Ax);
             if (dfinite(lo)) sc = dmax(sc, dabs(lo));
             if (dfinite(hi)) sc = dmax(sc, dabs(hi));
             prow = dmax(prow, vi / (1.0 + sc));
         }
         ymax = dmax(ymax, dabs((double)yv[i] * a.idr[i]));
-    };
-    PlainEpi<decltype(f)> epi{f};
-    warp_rows_all<T>(a.wsA, a.A, a.x[v], epi);
+    }
     double r[4] = {pv, pa, prow, ymax};
     block_max<4>(r, smred);
     const int nt = gridDim.x;
@@ -599,16 +631,17 @@ __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_kkt_rows(KktArg
 }
 
 template <typename T>
-__global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_kkt_cols(KktArgs<T> a) {
+__global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a, int n, int m) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const int v = blockIdx.y;
     const T* __restrict__ xv = a.x[v];
+    const double* __restrict__ atyv = a.aty[v];
     const double dz = 1e-8 * (1.0 + a.cmax);
     double dv = 0.0, op = 0.0, od = 0.0, unb = 0.0;
     // comparisons on the integer pipe, at-bound bands precomputed (k_bands);
     // the reduced cost multiplies by 1/dc instead of dividing by dc
-    auto f = [&](int j, const Acc<T>& acc) {
-        const double d = a.c[j] + acc.result_d() * a.idc[j];
+    for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+        const double d = a.c[j] + atyv[j] * a.idc[j];
         const double x = unscale_x(xv[j], a.slo[j], a.shi[j], a.dc[j], a.cl[j], a.cu[j]);
         const double cl = a.cl[j], cu = a.cu[j];
         const bool pos = dgt0(d), neg = dlt0(d);
@@ -622,33 +655,47 @@ __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_kkt_cols(KktArg
             if (dfinite(cu)) od += d * cu;
             else if (dlt(dz, -d)) unb = 1.0;
         }
-    };
-    PlainEpi<decltype(f)> epi{f};
-    warp_rows_all<T>(a.wsAT, a.AT, a.y[v], epi);
-    double mx[2] = {dv, unb};
-    block_max<2>(mx, smred);
-    double sm2[2] = {op, od};
-    block_sum<2>(sm2, smred);
+    }
+    // row part of the Lagrangian bound (src/pdhg/pdhg.cu:232-242)
+    const T* __restrict__ yv = a.y[v];
+    const double yz = 1e-8 * (1.0 + a.out[v].ymax);
+    double odr = 0.0, unbr = 0.0;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
+        const double y = (double)yv[i] * a.idr[i];
+        if (dlt(yz, y)) {
+            if (dfinite(a.rmax[i])) odr -= y * a.rmax[i];
+            else unbr = 1.0;
+        } else if (dlt(y, -yz)) {
+            if (dfinite(a.rmin[i])) odr -= y * a.rmin[i];
+            else unbr = 1.0;
+        }
+    }
+    double mx[4] = {dv, unb, unbr, 0.0};
+    block_max<4>(mx, smred);
+    double sm3[4] = {op, od, odr, 0.0};
+    block_sum<4>(sm3, smred);
     const int nt = gridDim.x;
     if (threadIdx.x == 0) {
-        double* P = a.part + (v * nt + blockIdx.x) * 4;
+        double* P = a.part + (v * nt + blockIdx.x) * 8;
         P[0] = mx[0];
         P[1] = mx[1];
-        P[2] = sm2[0];
-        P[3] = sm2[1];
+        P[2] = mx[2];
+        P[3] = sm3[0];
+        P[4] = sm3[1];
+        P[5] = sm3[2];
     }
     if (!last_cta(a.ticket)) return;
     for (int cv = 0; cv < (int)gridDim.y; ++cv) {
-        double tm[2] = {0.0, 0.0}, ts[2] = {0.0, 0.0};
+        double tm[4] = {0.0, 0.0, 0.0, 0.0}, ts[4] = {0.0, 0.0, 0.0, 0.0};
         for (int b = threadIdx.x; b < nt; b += kThreads) {
-            const double* P = a.part + (cv * nt + b) * 4;
-            tm[0] = smax(tm[0], P[0]);
-            tm[1] = smax(tm[1], P[1]);
-            ts[0] += P[2];
-            ts[1] += P[3];
+            const double* P = a.part + (cv * nt + b) * 8;
+            for (int q = 0; q < 3; ++q) {
+                tm[q] = smax(tm[q], P[q]);
+                ts[q] += P[3 + q];
+            }
         }
-        block_max<2>(tm, smred);
-        block_sum<2>(ts, smred);
+        block_max<4>(tm, smred);
+        block_sum<4>(ts, smred);
         if (threadIdx.x == 0) {
             DevMetrics& o = a.out[cv];
             o.dv = tm[0];
@@ -656,49 +703,8 @@ __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_kkt_cols(KktArg
             o.unb_col = tm[1] > 0.0;
             o.op = ts[0];
             o.od_col = ts[1];
-        }
-    }
-}
-
-template <typename T>
-__global__ void __launch_bounds__(kThreads) k_kkt_rowdual(KktArgs<T> a, int m) {
-    __shared__ double red[kWarps * 4];
-    const int v = blockIdx.y;
-    const T* __restrict__ yv = a.y[v];
-    const double yz = 1e-8 * (1.0 + a.out[v].ymax);
-    double od = 0.0, unb = 0.0;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < m; i += gridDim.x * blockDim.x) {
-        const double y = (double)yv[i] * a.idr[i];
-        if (dlt(yz, y)) {
-            if (dfinite(a.rmax[i])) od -= y * a.rmax[i];
-            else unb = 1.0;
-        } else if (dlt(y, -yz)) {
-            if (dfinite(a.rmin[i])) od -= y * a.rmin[i];
-            else unb = 1.0;
-        }
-    }
-    double s[1] = {od};
-    block_sum<1>(s, red);
-    double u[1] = {unb};
-    block_max<1>(u, red);
-    const int nb = gridDim.x;
-    if (threadIdx.x == 0) {
-        a.part[(v * nb + blockIdx.x) * 2] = s[0];
-        a.part[(v * nb + blockIdx.x) * 2 + 1] = u[0];
-    }
-    if (!last_cta(a.ticket)) return;
-    for (int cv = 0; cv < (int)gridDim.y; ++cv) {
-        double t[1] = {0.0}, w[1] = {0.0};
-        for (int b = threadIdx.x; b < nb; b += kThreads) {
-            t[0] += a.part[(cv * nb + b) * 2];
-            w[0] = smax(w[0], a.part[(cv * nb + b) * 2 + 1]);
-        }
-        block_sum<1>(t, red);
-        block_max<1>(w, red);
-        if (threadIdx.x == 0) {
-            DevMetrics& o = a.out[cv];
-            o.od_row = t[0];
-            o.unb_row = w[0] > 0.0;
+            o.od_row = ts[2];
+            o.unb_row = tm[2] > 0.0;
             const bool bounded = !o.unb_col && !o.unb_row;
             o.od = bounded ? o.od_col + o.od_row : -CUDART_INF;
             o.gap = bounded ? smax(0.0, o.op - o.od) / (1.0 + fabs(o.op)) : CUDART_INF;

@@ -41,6 +41,16 @@ def checksum(lp) -> dict:
                 rmax_fin=float(np.sum(lp.rmax[np.isfinite(lp.rmax)])))
 
 
+def same_checksum(lp, want: dict) -> bool:
+    """Sizes exactly, sums to 1e-12 relative: numpy's summation order (and
+    so the last bits of a float sum) differs between x86 and Arm builds."""
+    got = checksum(lp)
+    if any(got[k] != want[k] for k in ("m", "n", "nnz")):
+        return False
+    return all(abs(got[k] - want[k]) <= 1e-12 * max(1.0, abs(want[k]))
+               for k in ("ax_sum", "c_sum", "rmax_fin"))
+
+
 # ------------------------------------------------------------ LP catalogue
 # name -> (generator name, kwargs); every generator is seeded and pure.
 CATALOGUE = {}

@@ -6,6 +6,9 @@ persistent launch, each with its own restarts and termination.
   1e-6 relative KKT (FP32 iterates).
 * C3-shaped instances (m log-uniform, n = 2.5 m, Bernoulli pattern, box
   [0,5]) agree with the single-LP engine (FP64, 1e-8).
+* A spread of the 4,096-LP set itself (16 ranks of m, the 8 largest
+  instances up to m = 2,000, and the slowest instance) reaches scipy-HiGHS
+  optima (tests/golden/make_c3_golden.py) within 1e-5 at 1e-6.
 * Per-instance results do not depend on the batch's composition or order
   (CTAs never share an instance) and repeat bit for bit.
 """
@@ -60,6 +63,26 @@ def test_batch_matches_single_lp_engine(native):
         single = capi.solve_lp(lp, tolerance=1e-8, time_limit=60.0)
         assert single["status_name"] == "near-optimal"
         assert rel(r["objective"], single["objective"]) <= 2e-5
+
+
+def test_batch_full_size_range_reaches_highs_optimum(native):
+    import sys
+    sys.path.insert(0, os.path.join(HERE, "golden"))
+    from make_golden import same_checksum
+    from igaos_gb300 import capi
+    gold = json.load(open(os.path.join(HERE, "golden", "c3_objectives.json")))
+    lps = G.config3(**gold["kwargs"])
+    idx = sorted(gold["instances"], key=int)
+    batch = [lps[int(i)] for i in idx]
+    assert max(lp.m for lp in batch) >= 1990
+    for i, lp in zip(idx, batch):
+        assert same_checksum(lp, gold["instances"][i]["checksum"]), "generator drift"
+    out = capi.solve_batch(batch, tolerance=1e-6)
+    for i, r in zip(idx, out):
+        want = gold["instances"][i]["highs_ds_objective"]
+        assert r["status_name"] == "near-optimal", (i, r["status_name"])
+        assert max(r["pinf"], r["dinf"], r["rel_gap"], r["prow"]) <= 1e-6, i
+        assert rel(r["objective"], want) <= 1e-5, (i, r["objective"], want)
 
 
 def test_batch_order_independent_and_deterministic(native):
