@@ -31,8 +31,9 @@ Time-to-tolerance keys (relative KKT of the original LP, FP64 metrics):
 `time_to_tol_small_lp` (m 2,000, n 5,000): FP32 + refinement and FP64 to 1e-4
 and 1e-8 and the CPU oracle at 1e-8. `time_to_tol_multicommodity_lp` (m
 1,078,800, n 2,870,400): both precisions to 1e-4 and 1e-8, with attempt_us /
-attempt_hbm_frac (this LP streams from HBM). `time_to_tol_large_lp`: this
-workload to 1e-4 (FP32 + refinement with the opt-in Pock-Chambolle scaling;
+attempt_hbm_frac (this LP streams from HBM) and the distance of the 1e-8
+objectives to scipy-HiGHS's optimum (tests/golden/mcf_objectives.json).
+`time_to_tol_large_lp`: this workload to 1e-4 (FP32 + refinement with the opt-in Pock-Chambolle scaling;
 FP64 with the reference's scaling and with it), each within a stated budget,
 with the KKT reached. `vs_reference_gpu`: the reference's own GPU PDHG
 (cuSPARSE path, compiled from its sources into oracle/_ref, timed on this GPU
@@ -360,6 +361,15 @@ def c5_probe(capi, G, local):
         if a["status"] == b["status"] == "near-optimal":
             out[f"speedup_fp32_refine_vs_fp64@{tol:g}"] = a["loop_s"] / b["loop_s"]
             out[f"objective_rel_diff@{tol:g}"] = rel_diff(b["objective"], a["objective"])
+    # the independent optimum (scipy HiGHS interior point, committed fixture)
+    try:
+        gold = json.load(open(os.path.join(ROOT, "tests", "golden", "mcf_objectives.json")))
+        ref = gold["mcf300x8-s0"]["highs_ipm_objective"]
+        out["highs_ipm_objective"] = ref
+        for k in ("fp32-refine@1e-08", "fp64@1e-08"):
+            out[f"{k}_rel_diff_vs_highs"] = rel_diff(out[k]["objective"], ref)
+    except (OSError, KeyError, ValueError):
+        pass
     return flp, out
 
 

@@ -121,6 +121,7 @@ def lib():
         L.igaos_pdhg_get_transpose.argtypes = [C.c_void_p, _ip, _ip, _dp]
         L.igaos_pdhg_iterate.argtypes = [C.c_void_p, C.c_int, C.c_int64, _dp, _dp, _dp, _dp, _dp, _dp]
         L.igaos_pdhg_evaluate.argtypes = [C.c_void_p, _dp, _dp, _dp]
+        L.igaos_pdhg_set_start.argtypes = [C.c_void_p, _dp, _dp]
         L.igaos_pdhg_spmv.argtypes = [C.c_void_p, C.c_int, C.c_int, _dp, _dp]
         L.igaos_pdhg_gather_rate.argtypes = [C.c_int, C.c_int, _dp]
         L.igaos_pdhg_ray_certificate.argtypes = [C.c_int, C.c_int] + [_dp] * 11 + [C.POINTER(C.c_int)]
@@ -403,6 +404,16 @@ class Problem:
         st.update(eta=s6[0], omega=s6[1], k=int(s6[2]), hn=int(s6[3]), attempts=int(s6[4]),
                   parity=int(s6[5]))
         return st
+
+    def set_start(self, x0=None, y0=None):
+        """Start point (original units) of the following solves on this
+        handle; no arguments clear it (igaos_pdhg_set_start)."""
+        if x0 is None and y0 is None:
+            _check(lib().igaos_pdhg_set_start(self.h, None, None))
+            return
+        self._x0 = np.ascontiguousarray(x0, np.float64)
+        self._y0 = np.ascontiguousarray(y0, np.float64)
+        _check(lib().igaos_pdhg_set_start(self.h, _d(self._x0), _d(self._y0)))
 
     def evaluate(self, x, y):
         x = np.ascontiguousarray(x, np.float64)

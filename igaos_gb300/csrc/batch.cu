@@ -14,11 +14,23 @@
 // from the original FP64 values, so the termination metrics -- evaluated in
 // FP64 on anchor + delta -- reach FP64-level accuracy. Incumbent/rollback and
 // dual repair are not part of this path.
+//
+// FP32 iterates can stall where FP64 ones do not (one instance of a 4,096-LP
+// set needs 255,872 FP32 + refinement iterations against 54,336 in FP64),
+// and the launch lasts as long as its slowest instance. So the first
+// `handoff_max` instances still running at `handoff_at` iterations stop
+// there (a device counter bounds how many), and, with those the launch left
+// at max_iterations, the host finishes them in FP64 with the single-LP engine,
+// several at once on their own streams and threads.
 #include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <numeric>
+#include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -39,7 +51,7 @@ struct BatchDesc {
 };
 
 struct BatchOut {
-    int status, pad;
+    int status, handed;  // handed: stopped at handoff_at for the FP64 finish
     double objective, pinf, dinf, gap, prow;
     long long iterations, attempts, restarts;
     long long ns;  // device time of the instance (global timer)
@@ -72,6 +84,9 @@ struct BatchArgs {
     const float* fac;
     double tol;
     long long maxit;
+    long long handoff_at;        // iterations after which an instance may be handed off
+    unsigned int* handoff_count; // instances that asked (device counter)
+    int handoff_max;             // at most this many are handed off
     int check;
     double* x_out;
     double* y_out;
@@ -466,6 +481,7 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
     __shared__ double s_epoch_kkt, s_prev_cand, s_omega, s_eta;
     __shared__ long long s_k, s_hn, s_epoch_start, s_attempts, s_restarts;
     __shared__ int s_retries, s_have_pe, s_done, s_status, s_use_avg, s_restart, s_avg_better;
+    __shared__ int s_asked, s_handed;
     __shared__ BMetrics s_last;
     if (t == 0) {
         s_eta = s_eta0;
@@ -482,6 +498,8 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
         s_done = 0;
         s_status = IGAOS_STATUS_ITERATION_LIMIT;
         s_use_avg = 0;
+        s_asked = 0;
+        s_handed = 0;
         sh.parity = 0;
         s_last.pinf = s_last.dinf = CUDART_INF;
         s_last.gap = CUDART_INF;
@@ -592,6 +610,10 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
                     s_status = IGAOS_STATUS_NEAR_OPTIMAL;
                 } else if (k >= maxit) {
                     s_done = 1;
+                } else if (k >= a.handoff_at && !s_asked &&
+                           (s_asked = 1, atomicAdd(a.handoff_count, 1u) < (unsigned)a.handoff_max)) {
+                    s_done = 1;  // left for the FP64 finish
+                    s_handed = 1;
                 } else {
                     const double cand = fmin(ec, ea);
                     if (s_epoch_kkt < 0.0) {
@@ -674,7 +696,7 @@ __device__ void solve_one(const BatchArgs& a, BatchShared& sh, const BatchDesc& 
     if (t == 0) {
         BatchOut o;
         o.status = s_status;
-        o.pad = 0;
+        o.handed = s_handed;
         o.objective = s_last.op;
         o.pinf = s_last.pinf;
         o.dinf = s_last.dinf;
@@ -836,9 +858,22 @@ extern "C" int igaos_pdhg_solve_batch(int count, const int* m, const int* n, con
         A.tol = o.tolerance;
         // per-instance iteration cap (the kernel has no wall clock)
         A.maxit = (long long)std::max<int64_t>(1, o.max_iterations);
+        // hand-off: 100,000 iterations and 16 instances unless overridden
+        // (IGAOS_PDHG_BATCH_HANDOFF=iterations, 0 = never;
+        // IGAOS_PDHG_BATCH_HANDOFF_MAX=instances)
+        {
+            const char* e = std::getenv("IGAOS_PDHG_BATCH_HANDOFF");
+            const long long h = e && *e ? std::atoll(e) : 100000;
+            A.handoff_at = h > 0 ? h : A.maxit;
+            const char* em = std::getenv("IGAOS_PDHG_BATCH_HANDOFF_MAX");
+            A.handoff_max = em && *em ? std::max(0, std::atoi(em)) : 16;
+        }
+        A.handoff_count = ar.alloc<unsigned int>(1);
+        CU(cudaMemsetAsync(A.handoff_count, 0, sizeof(unsigned int), st));
         A.check = o.check_period > 0 ? o.check_period : 64;
-        A.x_out = x ? ar.alloc<double>(cols) : nullptr;
-        A.y_out = y ? ar.alloc<double>(rows) : nullptr;
+        // every instance's answer (the FP64 finish starts from it)
+        A.x_out = ar.alloc<double>(cols);
+        A.y_out = ar.alloc<double>(rows);
         A.out = ar.alloc<BatchOut>(count);
         int sms = 0, dev = 0, per_sm = 0;
         CU(cudaGetDevice(&dev));
@@ -854,40 +889,92 @@ extern "C" int igaos_pdhg_solve_batch(int count, const int* m, const int* n, con
         CU(cudaEventRecord(e1, st));
         std::vector<BatchOut> out(count);
         CU(cudaMemcpyAsync(out.data(), A.out, sizeof(BatchOut) * count, cudaMemcpyDeviceToHost, st));
-        if (x) CU(cudaMemcpyAsync(x, A.x_out, sizeof(double) * cols, cudaMemcpyDeviceToHost, st));
-        if (y) CU(cudaMemcpyAsync(y, A.y_out, sizeof(double) * rows, cudaMemcpyDeviceToHost, st));
+        std::vector<double> xk, yk;  // the launch's answers when the caller wants none
+        if (!x) {
+            xk.resize(cols);
+            x = xk.data();
+        }
+        if (!y) {
+            yk.resize(rows);
+            y = yk.data();
+        }
+        CU(cudaMemcpyAsync(x, A.x_out, sizeof(double) * cols, cudaMemcpyDeviceToHost, st));
+        CU(cudaMemcpyAsync(y, A.y_out, sizeof(double) * rows, cudaMemcpyDeviceToHost, st));
         CU(cudaStreamSynchronize(st));
         float kms = 0.f;
         CU(cudaEventElapsedTime(&kms, e0, e1));
         cudaEventDestroy(e0);
         cudaEventDestroy(e1);
-        // Instances the launch left at the cap: FP32 iterates can stall where
-        // FP64 ones do not (one instance of the 4,096-LP set needs 255,872
-        // FP32 + refinement iterations against 54,336 in FP64), so each is
-        // solved again, alone, by the single-LP engine in FP64 through the
-        // public entry point, with the same tolerance and cap.
+        // Instances the launch handed off or left at the cap are solved again,
+        // alone, by the single-LP engine in FP64 through the public entry
+        // points, from the launch's answer (igaos_pdhg_set_start), with the
+        // same tolerance and cap; up to 8 at once, each on its own host
+        // thread, engine and stream.
         std::vector<igaos_pdhg_result> fin(count);
         std::vector<char> redo(count, 0);
         std::vector<double> fin_ms(count, 0.0);
-        for (int b = 0; b < count; ++b) {
-            const BatchDesc& d = desc[b];
-            if (out[b].status != IGAOS_STATUS_ITERATION_LIMIT || d.m <= 0 || d.n <= 0) continue;
-            igaos_pdhg_options o64 = o;
-            o64.precision = IGAOS_PDHG_FP64;
-            o64.time_limit_s = 1e9;  // the cap binds, as in the launch
-            o64.pdhg_presolve = 0;
-            o64.crossover = 0;
-            const auto t1 = std::chrono::steady_clock::now();
-            const int rc = igaos_pdhg_solve_csr(
-                d.m, d.n, d.nnz, ap + d.ap_off, ai + d.nz_off, ax + d.nz_off, nullptr, nullptr,
-                nullptr, c + d.col_off, cl + d.col_off, cu + d.col_off, rmin + d.row_off,
-                rmax + d.row_off, 0.0, &o64, &fin[b], x ? x + d.col_off : nullptr,
-                y ? y + d.row_off : nullptr);
-            if (rc != IGAOS_PDHG_OK) return rc;  // error state already set
-            fin_ms[b] = std::chrono::duration<double, std::milli>(
-                            std::chrono::steady_clock::now() - t1).count();
-            redo[b] = 1;
+        std::vector<int> todo;
+        for (int b = 0; b < count; ++b)
+            if (out[b].status == IGAOS_STATUS_ITERATION_LIMIT && desc[b].m > 0 && desc[b].n > 0)
+                todo.push_back(b);
+        std::vector<int> fin_rc(count, IGAOS_PDHG_OK);
+        std::vector<std::string> fin_msg(count);
+        std::atomic<size_t> next{0};
+        auto finish = [&]() {
+            CU(cudaSetDevice(dev));
+            for (size_t t; (t = next.fetch_add(1)) < todo.size();) {
+                const int b = todo[t];
+                const BatchDesc& d = desc[b];
+                igaos_pdhg_options o64 = o;
+                o64.precision = IGAOS_PDHG_FP64;
+                o64.time_limit_s = 1e9;  // the cap binds, as in the launch
+                o64.pdhg_presolve = 0;
+                o64.crossover = 0;
+                const auto t1 = std::chrono::steady_clock::now();
+                igaos_pdhg_problem* P = nullptr;
+                int rc = igaos_pdhg_create(&P, d.m, d.n, d.nnz, ap + d.ap_off, ai + d.nz_off,
+                                           ax + d.nz_off, nullptr, nullptr, nullptr, c + d.col_off,
+                                           cl + d.col_off, cu + d.col_off, rmin + d.row_off,
+                                           rmax + d.row_off, 0.0, &o64);
+                if (rc == IGAOS_PDHG_OK)
+                    rc = igaos_pdhg_set_start(P, x + d.col_off, y + d.row_off);
+                if (rc == IGAOS_PDHG_OK)
+                    rc = igaos_pdhg_solve(P, &o64, &fin[b], x + d.col_off, y + d.row_off);
+                igaos_pdhg_destroy(P);
+                fin_rc[b] = rc;
+                if (fin_rc[b] != IGAOS_PDHG_OK) {
+                    char msg[512];
+                    igaos_pdhg_last_error(msg, sizeof(msg));
+                    fin_msg[b] = msg;
+                }
+                fin_ms[b] = std::chrono::duration<double, std::milli>(
+                                std::chrono::steady_clock::now() - t1).count();
+                redo[b] = 1;
+            }
+        };
+        int nthreads = 8;
+        if (const char* e = std::getenv("IGAOS_PDHG_BATCH_FINISH_THREADS"))
+            nthreads = std::max(1, std::atoi(e));
+        nthreads = (int)std::min<size_t>((size_t)nthreads, todo.size());
+        if (nthreads == 1) {
+            finish();
+        } else if (nthreads > 1) {
+            std::vector<std::thread> pool;
+            std::vector<std::exception_ptr> errs(nthreads);
+            for (int i = 0; i < nthreads; ++i)
+                pool.emplace_back([&, i] {
+                    try {
+                        finish();
+                    } catch (...) {
+                        errs[i] = std::current_exception();
+                    }
+                });
+            for (auto& th : pool) th.join();
+            for (auto& e : errs)
+                if (e) std::rethrow_exception(e);
         }
+        for (int b : todo)
+            if (fin_rc[b] != IGAOS_PDHG_OK) return igx_set_error(fin_rc[b], fin_msg[b].c_str());
         const double wall = std::chrono::duration<double, std::milli>(
                                 std::chrono::steady_clock::now() - t_start).count();
         for (int b = 0; b < count; ++b) {

@@ -560,6 +560,14 @@ int igaos_pdhg_iterate(igaos_pdhg_problem* p, int precision, int64_t iters, doub
     return guarded([&] { p->eng->iterate(precision, iters, x, y, xavg, yavg, axcur, state6); });
 }
 
+int igaos_pdhg_set_start(igaos_pdhg_problem* p, const double* x0, const double* y0) {
+    if (p && p->pre)
+        return fail(IGAOS_PDHG_ERR_INVALID, "a start point is not available on a presolved handle");
+    if (!p || !p->eng) return fail(IGAOS_PDHG_ERR_INVALID, "problem handle is NULL");
+    if (!x0 != !y0) return fail(IGAOS_PDHG_ERR_INVALID, "x0 and y0 are both given or both NULL");
+    return guarded([&] { p->eng->set_start(x0, y0); });
+}
+
 int igaos_pdhg_evaluate(igaos_pdhg_problem* p, const double* x, const double* y, double* out6) {
     if (p && p->pre) return fail(IGAOS_PDHG_ERR_INVALID, kPresolvedInspect);
     if (!p || !p->eng || !x || !y || !out6) return fail(IGAOS_PDHG_ERR_INVALID, "NULL argument");

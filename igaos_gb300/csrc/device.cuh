@@ -340,6 +340,31 @@ __device__ __forceinline__ void block_max(double (&v)[NV], double* sh) {
     __syncthreads();
 }
 
+// block_max on the integer pipe (order-preserving keys): the same maxima,
+// without the FP64 compares that otherwise dominate a short streaming pass
+// on this GPU's narrow FP64 pipe (a positive NaN wins, as the largest key).
+template <int NV, int NW = kWarps>
+__device__ __forceinline__ void block_dmax(double (&v)[NV], double* sh) {
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+#pragma unroll
+    for (int q = 0; q < NV; ++q)
+        for (int o = 16; o > 0; o >>= 1) v[q] = dmax(v[q], __shfl_xor_sync(0xffffffffu, v[q], o));
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < NV; ++q) sh[w * NV + q] = v[q];
+    __syncthreads();
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int q = 0; q < NV; ++q) {
+            double s = sh[q];
+            for (int k = 1; k < NW; ++k) s = dmax(s, sh[k * NV + q]);
+            v[q] = s;
+        }
+    }
+    __syncthreads();
+}
+
 // Block-wide fixed-order merge of NV compensated accumulators; result in
 // thread 0. `sh` needs kWarps * NV entries.
 template <typename T, int NV, int NW = kWarps>
@@ -411,56 +436,71 @@ struct PlainEpi {
     __device__ __forceinline__ void apply(int r, const A& acc, const NoPre&) { f(r, acc); }
 };
 
-// The row sums of one warp item: rows [r0, r1) of A times x with 2^lg
-// lanes per row, the row's entries in predicated batches of kLaneBatch per
-// lane (all value and index loads of a batch, then its gathers in flight),
-// the G-lane shuffle reduction, and the sum of the item's i-th row handed to
-// lane i, so consecutive lanes touch consecutive vector entries.
+// The row sums of one warp item with 2^lg lanes per row: the lane's row
+// has entries [b, e) (empty for lanes without a row), taken in predicated
+// batches of kLaneBatch per lane (all value and index loads of a batch, then
+// its gathers in flight); then the G-lane shuffle reduction, and the sum of
+// the item's i-th row handed to lane i, so consecutive lanes touch
+// consecutive vector entries.
+template <typename T>
+__device__ __forceinline__ Acc<T> lane_products(const Csr<T>& A, const T* __restrict__ x, int b,
+                                                int e, int lg) {
+    const int G = 1 << lg;
+    const int gl = (threadIdx.x & 31) & (G - 1);
+    Acc<T> acc;
+    for (int p = b + gl; p < e; p += kLaneBatch * G) {
+        T a[kLaneBatch];
+        int j[kLaneBatch];
+#if IGX_L2_STREAM
+        // FP32 products only: in the FP64 ones the branch alone cost 3-5 %
+        // and streaming gained nothing (they are FP64-pipe bound)
+        if (sizeof(T) == 4 && A.stream) {  // uniform branch: one policy per batch
+            const unsigned long long pol = l2_evict_first();
+#pragma unroll
+            for (int u = 0; u < kLaneBatch; ++u) {
+                const int q = p + u * G;
+                const bool ok = q < e;
+                a[u] = ok ? ld_first(A.val + q, pol) : T(0);
+                j[u] = ok ? ld_first(A.idx + q, pol) : 0;
+            }
+        } else
+#endif
+        {
+#pragma unroll
+            for (int u = 0; u < kLaneBatch; ++u) {
+                const int q = p + u * G;
+                const bool ok = q < e;
+                a[u] = ok ? __ldg(A.val + q) : T(0);
+                j[u] = ok ? __ldg(A.idx + q) : 0;
+            }
+        }
+        T xv[kLaneBatch];
+#pragma unroll
+        for (int u = 0; u < kLaneBatch; ++u) xv[u] = __ldg(x + j[u]);
+#pragma unroll
+        for (int u = 0; u < kLaneBatch; ++u) acc.add(a[u], xv[u]);  // masked: 0 * x[0] adds 0
+    }
+    return acc;
+}
+
+template <typename T>
+__device__ __forceinline__ Acc<T> reduce_rows(Acc<T> acc, int lg) {
+    const int G = 1 << lg;
+    for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(0xffffffffu, o, G);
+    return acc.shfl_from(0xffffffffu, ((threadIdx.x & 31) << lg) & 31);
+}
+
+// The row sums of the item holding rows [r0, r1).
 template <typename T>
 __device__ __forceinline__ Acc<T> item_sums(const Csr<T>& A, const T* __restrict__ x, int r0,
                                             int r1, int lg) {
-    const int lane = threadIdx.x & 31;
-    const int G = 1 << lg;
-    const int g = lane >> lg, gl = lane & (G - 1);
-    const int r = r0 + g;
-    Acc<T> acc;
+    const int r = r0 + ((threadIdx.x & 31) >> lg);
+    int b = 0, e = 0;
     if (r < r1) {
-        const int b = __ldg(A.ptr + r), e = __ldg(A.ptr + r + 1);
-        for (int p = b + gl; p < e; p += kLaneBatch * G) {
-            T a[kLaneBatch];
-            int j[kLaneBatch];
-#if IGX_L2_STREAM
-            // FP32 products only: in the FP64 ones the branch alone cost 3-5 %
-            // and streaming gained nothing (they are FP64-pipe bound)
-            if (sizeof(T) == 4 && A.stream) {  // uniform branch: one policy per batch
-                const unsigned long long pol = l2_evict_first();
-#pragma unroll
-                for (int u = 0; u < kLaneBatch; ++u) {
-                    const int q = p + u * G;
-                    const bool ok = q < e;
-                    a[u] = ok ? ld_first(A.val + q, pol) : T(0);
-                    j[u] = ok ? ld_first(A.idx + q, pol) : 0;
-                }
-            } else
-#endif
-            {
-#pragma unroll
-                for (int u = 0; u < kLaneBatch; ++u) {
-                    const int q = p + u * G;
-                    const bool ok = q < e;
-                    a[u] = ok ? __ldg(A.val + q) : T(0);
-                    j[u] = ok ? __ldg(A.idx + q) : 0;
-                }
-            }
-            T xv[kLaneBatch];
-#pragma unroll
-            for (int u = 0; u < kLaneBatch; ++u) xv[u] = __ldg(x + j[u]);
-#pragma unroll
-            for (int u = 0; u < kLaneBatch; ++u) acc.add(a[u], xv[u]);  // masked: 0 * x[0] adds 0
-        }
+        b = __ldg(A.ptr + r);
+        e = __ldg(A.ptr + r + 1);
     }
-    for (int o = G >> 1; o > 0; o >>= 1) acc.shfl_xor(0xffffffffu, o, G);
-    return acc.shfl_from(0xffffffffu, (lane << lg) & 31);
+    return reduce_rows<T>(lane_products<T>(A, x, b, e, lg), lg);
 }
 
 // One warp item with its row steps in place: the epilogue's vector entries
@@ -482,77 +522,65 @@ __device__ __forceinline__ void warp_item(const WarpSched& ws, const Csr<T>& A,
 
 // All warp items of the schedule, grid-stride over the launched warps
 // (CTAs are sized to stay resident, so per-CTA costs are paid once).
+#ifndef IGX_ITEM_PREFETCH
+#define IGX_ITEM_PREFETCH 0
+#endif
 template <typename T, class E>
 __device__ __forceinline__ void warp_rows_all(const WarpSched& ws, const Csr<T>& A,
                                               const T* __restrict__ x, E& epi) {
     const int stride = gridDim.x * kWarps;
+#if IGX_ITEM_PREFETCH
+    // software-pipelined: the next item's schedule entries are loaded when
+    // this item starts, and its row pointers between this item's products
+    // and its reduction, so each item starts with [b, e) in registers
+    const int lane = threadIdx.x & 31;
+    int w = blockIdx.x * kWarps + (threadIdx.x >> 5);
+    if (w >= ws.nwarps) return;
+    int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1), lg = __ldg(ws.lg + w);
+    int b = 0, e = 0;
+    {
+        const int r = r0 + (lane >> lg);
+        if (r < r1) {
+            b = __ldg(A.ptr + r);
+            e = __ldg(A.ptr + r + 1);
+        }
+    }
+    for (;;) {
+        const int wn = w + stride;
+        const bool more = wn < ws.nwarps;
+        int n0 = 0, n1 = 0, nlg = 0;
+        if (more) {
+            n0 = __ldg(ws.row + wn);
+            n1 = __ldg(ws.row + wn + 1);
+            nlg = __ldg(ws.lg + wn);
+        }
+        const int er = r0 + lane;
+        const bool has_epi = lane < (32 >> lg) && er < r1;
+        typename E::Pre pre{};
+        if (has_epi) pre = epi.load(er);
+        const Acc<T> acc = lane_products<T>(A, x, b, e, lg);
+        int nb = 0, ne = 0;
+        if (more) {
+            const int nr = n0 + (lane >> nlg);
+            if (nr < n1) {
+                nb = __ldg(A.ptr + nr);
+                ne = __ldg(A.ptr + nr + 1);
+            }
+        }
+        const Acc<T> mine = reduce_rows<T>(acc, lg);
+        if (has_epi) epi.apply(er, mine, pre);
+        if (!more) break;
+        w = wn;
+        r0 = n0;
+        r1 = n1;
+        lg = nlg;
+        b = nb;
+        e = ne;
+    }
+#else
     for (int w = blockIdx.x * kWarps + (threadIdx.x >> 5); w < ws.nwarps; w += stride)
         warp_item<T>(ws, A, x, w, epi);
-}
-
-// The same items with deferred row steps: each warp parks its items' row
-// sums (row index and sum) in shared memory and runs the row steps 32 rows
-// at a time, on all 32 lanes. An item with G lanes per row holds only 32/G
-// rows, and on GB300 an FP64 instruction issued with partial lanes occupies
-// the narrow FP64 pipe as long as a full one; deferred, the FP64 row steps
-// cost 1/G of the issues. The products, their order and every row's
-// arithmetic are unchanged; only which lane runs a row's step, and when,
-// differ. `park` holds kWarps * 64 entries.
-template <typename T>
-struct Parked {
-    int row;
-    Acc<T> sum;
-};
-
-template <typename T, class E>
-__device__ __forceinline__ void warp_rows_deferred(const WarpSched& ws, const Csr<T>& A,
-                                                   const T* __restrict__ x, E& epi,
-                                                   Parked<T>* park) {
-    const int lane = threadIdx.x & 31;
-    Parked<T>* wp = park + (threadIdx.x >> 5) * 64;
-    int cnt = 0;  // parked rows (< 32 between items; < 64 after one)
-    const int stride = gridDim.x * kWarps;
-    for (int w = blockIdx.x * kWarps + (threadIdx.x >> 5); w < ws.nwarps; w += stride) {
-        const int r0 = __ldg(ws.row + w), r1 = __ldg(ws.row + w + 1);
-        const int lg = __ldg(ws.lg + w);
-        const int nr = min(32 >> lg, r1 - r0);
-        const Acc<T> mine = item_sums<T>(A, x, r0, r1, lg);
-        if (lane < nr) {
-            wp[cnt + lane].row = r0 + lane;
-            wp[cnt + lane].sum = mine;
-        }
-        cnt += nr;
-        __syncwarp();
-        if (cnt >= 32) {
-            const Parked<T> mine_p = wp[lane];
-            const bool carry = lane < cnt - 32;
-            Parked<T> rest;
-            if (carry) rest = wp[32 + lane];
-            __syncwarp();
-            if (carry) wp[lane] = rest;
-            cnt -= 32;
-            __syncwarp();
-            const typename E::Pre pre = epi.load(mine_p.row);
-            epi.apply(mine_p.row, mine_p.sum, pre);
-        }
-    }
-    if (lane < cnt) {
-        const Parked<T> mine_p = wp[lane];
-        const typename E::Pre pre = epi.load(mine_p.row);
-        epi.apply(mine_p.row, mine_p.sum, pre);
-    }
-}
-
-// Deferred row steps per iterate precision (compile switches for A/B
-// builds): FP64 row steps are bound by the FP64 pipe's issue slots.
-#ifndef IGX_DEFER_F64
-#define IGX_DEFER_F64 0
 #endif
-#ifndef IGX_DEFER_F32
-#define IGX_DEFER_F32 0
-#endif
-template <typename T> struct DeferSteps { static constexpr bool value = IGX_DEFER_F32 != 0; };
-template <> struct DeferSteps<double> { static constexpr bool value = IGX_DEFER_F64 != 0; };
-
+}
 
 }  // namespace igx

@@ -761,8 +761,9 @@ void Engine::kkt(const Vecs& v, const T* x0, const T* y0, const T* x1, const T* 
                                                               kkt_ax_, kkt_ax_ + m);
     k_kkt_prod<T><<<dim3(sAT_.ctas, ncand), kThreads, 0, st_>>>(sAT_.view(), csrAT<T>(), y0, y1,
                                                                kkt_aty_, kkt_aty_ + n);
-    k_kkt_rows<T><<<dim3(red_blocks_, ncand), kThreads, 0, st_>>>(ka, m);
-    k_kkt_cols<T><<<dim3(red_blocks_, ncand), kThreads, 0, st_>>>(ka, n, m);
+    // about four rows (columns) per thread, at most 2 CTAs per SM per candidate
+    k_kkt_rows<T><<<dim3(grid_for(m, 4 * kThreads, 152 * 2), ncand), kThreads, 0, st_>>>(ka, m);
+    k_kkt_cols<T><<<dim3(grid_for(n, 4 * kThreads, 152 * 2), ncand), kThreads, 0, st_>>>(ka, n, m);
     CU(cudaGetLastError());
     CU(cudaMemcpyAsync(h_met_, met_, ncand * sizeof(DevMetrics), cudaMemcpyDeviceToHost, st_));
     CU(cudaStreamSynchronize(st_));
@@ -1013,17 +1014,7 @@ int Engine::ray_check(bool anch, int p, LoopOut& out) {
     CU(cudaMemcpyAsync(dy.data(), tmp_m_, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
     CU(cudaMemcpyAsync(aty.data(), tmp_n2_, sizeof(double) * n, cudaMemcpyDeviceToHost, st_));
     CU(cudaMemcpyAsync(ax.data(), tmp_m2_, sizeof(double) * m, cudaMemcpyDeviceToHost, st_));
-    if (h_c_.empty()) {
-        auto get = [&](const double* d, int len, std::vector<double>& h) {
-            h.resize(len);
-            CU(cudaMemcpyAsync(h.data(), d, sizeof(double) * len, cudaMemcpyDeviceToHost, st_));
-        };
-        get(base_.c, n, h_c_);
-        get(base_.cl, n, h_cl_);
-        get(base_.cu, n, h_cu_);
-        get(base_.rmin, m, h_rmin_);
-        get(base_.rmax, m, h_rmax_);
-    }
+    fetch_host_data();
     CU(cudaStreamSynchronize(st_));
     // original units: x = dc x~, y = y~ / dr, A^T y = (A~^T y~) / dc, A x = dr (A~ x~)
     for (int i = 0; i < m; ++i) {
@@ -1062,11 +1053,26 @@ LoopOut Engine::loop(const Vecs& v, const LoopOpts& o) {
     CU(cudaMemsetAsync(w.axc[0], 0, mb, st_));
     // anchored FP32 iterations (FP32 + FP64 refinement): start at anchor 0
     const bool anch = v.fyhat != nullptr;
-    if (anch) {
-        CU(cudaMemsetAsync(anc_.xh, 0, sizeof(double) * n, st_));
-        CU(cudaMemsetAsync(anc_.yh, 0, sizeof(double) * m, st_));
+    const bool warm = !start_x_.empty();
+    if (anch) {  // the first anchor: the start point, else 0
+        if (warm) {
+            CU(cudaMemcpyAsync(anc_.xh, start_x_.data(), sizeof(double) * n, cudaMemcpyHostToDevice, st_));
+            CU(cudaMemcpyAsync(anc_.yh, start_y_.data(), sizeof(double) * m, cudaMemcpyHostToDevice, st_));
+        } else {
+            CU(cudaMemsetAsync(anc_.xh, 0, sizeof(double) * n, st_));
+            CU(cudaMemsetAsync(anc_.yh, 0, sizeof(double) * m, st_));
+        }
         anchor_data();
         out.spmvs += 2;
+    } else if (warm) {  // x = xavg = x0, y = yavg = y0, A x committed
+        std::vector<T> sx(start_x_.begin(), start_x_.end()), sy(start_y_.begin(), start_y_.end());
+        CU(cudaMemcpyAsync(w.x[0], sx.data(), nb, cudaMemcpyHostToDevice, st_));
+        CU(cudaMemcpyAsync(w.xavg[0], sx.data(), nb, cudaMemcpyHostToDevice, st_));
+        CU(cudaMemcpyAsync(w.y[0], sy.data(), mb, cudaMemcpyHostToDevice, st_));
+        CU(cudaMemcpyAsync(w.yavg[0], sy.data(), mb, cudaMemcpyHostToDevice, st_));
+        spmv_dev<T>(false, w.x[0], w.axc[0]);
+        CU(cudaStreamSynchronize(st_));  // the host vectors go out of scope
+        out.spmvs += 1;
     }
     std::memset(h_ctl_, 0, sizeof(DevCtl));
     h_ctl_->eta = o.eta_init;
@@ -1555,6 +1561,41 @@ void Engine::iterate(int precision, long long iters, double* x, double* y, doubl
     };
     if (precision == IGAOS_PDHG_FP64) run(double());
     else run(float());
+}
+
+// Host copies of c, cl, cu, rmin, rmax (original units, device order), once.
+void Engine::fetch_host_data() {
+    if (!h_c_.empty()) return;
+    auto get = [&](const double* d, int len, std::vector<double>& h) {
+        h.resize(len);
+        CU(cudaMemcpyAsync(h.data(), d, sizeof(double) * len, cudaMemcpyDeviceToHost, st_));
+    };
+    get(base_.c, n, h_c_);
+    get(base_.cl, n, h_cl_);
+    get(base_.cu, n, h_cu_);
+    get(base_.rmin, m, h_rmin_);
+    get(base_.rmax, m, h_rmax_);
+}
+
+void Engine::set_start(const double* x0, const double* y0) {
+    if (!x0 || !y0) {
+        start_x_.clear();
+        start_y_.clear();
+        return;
+    }
+    fetch_host_data();
+    CU(cudaStreamSynchronize(st_));
+    // x~ = clamp(x, cl, cu) / dc, y~ = y dr; non-finite entries start at 0
+    start_x_.assign(n, 0.0);
+    start_y_.assign(m, 0.0);
+    for (int j = 0; j < n; ++j) {
+        const double v = std::min(std::max(x0[pc_[j]], h_cl_[j]), h_cu_[j]) / hp_dc_[j];
+        start_x_[j] = std::isfinite(v) ? v : 0.0;
+    }
+    for (int i = 0; i < m; ++i) {
+        const double v = y0[pr_[i]] * hp_dr_[i];
+        start_y_[i] = std::isfinite(v) ? v : 0.0;
+    }
 }
 
 void Engine::evaluate(const double* x, const double* y, double* out6) {

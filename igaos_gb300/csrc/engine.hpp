@@ -159,6 +159,10 @@ class Engine {
     void iterate(int precision, long long iters, double* x, double* y, double* xavg,
                  double* yavg, double* axc, double* st6);
     void evaluate(const double* x, const double* y, double* out6);
+    // start point of the following solves (original units, caller's
+    // numbering; NULLs clear it)
+    void set_start(const double* x0, const double* y0);
+    void fetch_host_data();
     void spmv(int transpose, int precision, const double* x, double* y);
     // matrix-free dual repair on the device (any m): original units, caller's
     // numbering; certified when pinf, prow and a finite gap are <= tol.
@@ -193,6 +197,7 @@ class Engine {
     // device numbering: new index -> original (pr_, pc_) and inverses
     std::vector<int> pr_, pc_, ipr_, ipc_;
     std::vector<double> hp_dr_, hp_dc_;  // scaling in device numbering
+    std::vector<double> start_x_, start_y_;  // scaled start point, device numbering (or empty)
     void to_dev_order(const double* in, double* out, bool rows) const;
     void to_user_order(const double* in, double* out, bool rows) const;
     // workspace

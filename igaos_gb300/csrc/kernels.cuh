@@ -104,19 +104,6 @@ struct PrimalEpi {
     }
 };
 
-// The attempt kernels' traversal: row steps in place, or deferred to full
-// warps (DeferSteps: FP64 by default).
-template <typename T, class E>
-__device__ __forceinline__ void rows_with_steps(const WarpSched& ws, const Csr<T>& M,
-                                                const T* __restrict__ v, E& epi) {
-    if constexpr (DeferSteps<T>::value) {
-        __shared__ __align__(16) unsigned char park[kWarps * 64 * sizeof(Parked<T>)];
-        warp_rows_deferred<T>(ws, M, v, epi, reinterpret_cast<Parked<T>*>(park));
-    } else {
-        warp_rows_all<T>(ws, M, v, epi);
-    }
-}
-
 template <typename T>
 __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_primal(PrimalArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
@@ -125,7 +112,7 @@ __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_primal(PrimalAr
     const int p = cv.parity, q = p ^ 1;
     PrimalEpi<T> epi{a.c, a.lo, a.hi, a.x[p], a.xavg[p], a.x[q], a.xavg[q], a.xbar,
                      cv.tau, cv.w, (T)0};
-    rows_with_steps<T>(a.ws, a.AT, a.y[p], epi);
+    warp_rows_all<T>(a.ws, a.AT, a.y[p], epi);
     const T dx2 = epi.dx2;
     T v[1] = {dx2};
     block_sum_t<T, 1>(v, reinterpret_cast<T*>(smred));
@@ -262,7 +249,7 @@ __global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_dual(DualArgs<T
     const int p = cv.parity, q = p ^ 1;
     DualEpi<T> epi{a.rmin, a.rmax, a.y[p], a.axc[p], a.yavg[p], a.yhat, a.y[q], a.axc[q], a.yavg[q],
                    cv.sigma, cv.isigma, cv.w, (T)0, (T)0};
-    rows_with_steps<T>(a.ws, a.A, a.xbar, epi);
+    warp_rows_all<T>(a.ws, a.A, a.xbar, epi);
     T v[2] = {epi.dy2, epi.cross};
     block_sum_t<T, 2>(v, reinterpret_cast<T*>(smred));
     if (threadIdx.x == 0) {
@@ -548,9 +535,12 @@ __global__ void k_convert(int n, const TI* __restrict__ in, TO* __restrict__ out
 //               column part of the Lagrangian bound; then one thread per row
 //               for its row part (needs max |y| for its noise threshold) and
 //               the final metrics.
-// The metrics run with every lane of a warp busy: inside the warp schedule
+// The metrics run with every lane of a warp busy (inside the warp schedule
 // only 32/G lanes hold a row, and an FP64 instruction issued with partial
-// lanes occupies GB300's narrow FP64 pipe as long as a full one.
+// lanes occupies GB300's narrow FP64 pipe as long as a full one), several
+// rows or columns per thread, and their maxima reduce on the integer pipe:
+// with a row per thread, the FP64 compares of the block reductions cost
+// more of that pipe than the metrics themselves.
 
 template <typename T>
 struct KktArgs {
@@ -609,7 +599,7 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a, int m) {
         ymax = dmax(ymax, dabs((double)yv[i] * a.idr[i]));
     }
     double r[4] = {pv, pa, prow, ymax};
-    block_max<4>(r, smred);
+    block_dmax<4>(r, smred);
     const int nt = gridDim.x;
     if (threadIdx.x == 0)
         for (int q = 0; q < 4; ++q) a.part[(v * nt + blockIdx.x) * 4 + q] = r[q];
@@ -617,8 +607,8 @@ __global__ void __launch_bounds__(kThreads) k_kkt_rows(KktArgs<T> a, int m) {
     for (int cv = 0; cv < (int)gridDim.y; ++cv) {
         double t[4] = {0.0, 0.0, 0.0, 0.0};
         for (int b = threadIdx.x; b < nt; b += kThreads)
-            for (int q = 0; q < 4; ++q) t[q] = smax(t[q], a.part[(cv * nt + b) * 4 + q]);
-        block_max<4>(t, smred);
+            for (int q = 0; q < 4; ++q) t[q] = dmax(t[q], a.part[(cv * nt + b) * 4 + q]);
+        block_dmax<4>(t, smred);
         if (threadIdx.x == 0) {
             DevMetrics& o = a.out[cv];
             o.pv = t[0];
@@ -671,7 +661,7 @@ __global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a, int n, int 
         }
     }
     double mx[4] = {dv, unb, unbr, 0.0};
-    block_max<4>(mx, smred);
+    block_dmax<4>(mx, smred);
     double sm3[4] = {op, od, odr, 0.0};
     block_sum<4>(sm3, smred);
     const int nt = gridDim.x;
@@ -690,11 +680,11 @@ __global__ void __launch_bounds__(kThreads) k_kkt_cols(KktArgs<T> a, int n, int 
         for (int b = threadIdx.x; b < nt; b += kThreads) {
             const double* P = a.part + (cv * nt + b) * 8;
             for (int q = 0; q < 3; ++q) {
-                tm[q] = smax(tm[q], P[q]);
+                tm[q] = dmax(tm[q], P[q]);
                 ts[q] += P[3 + q];
             }
         }
-        block_max<4>(tm, smred);
+        block_dmax<4>(tm, smred);
         block_sum<4>(ts, smred);
         if (threadIdx.x == 0) {
             DevMetrics& o = a.out[cv];

@@ -358,6 +358,14 @@ int igaos_pdhg_dual_repair_device(igaos_pdhg_problem* p, const double* x, const 
                                   double col_tol, double tol, double* y, int* certified,
                                   double* metrics6);
 
+/* Start point of the following solves on this handle (until replaced; two
+ * NULLs clear it): x0 (n) and y0 (m) in ORIGINAL units, the caller's
+ * numbering. The iterates start there instead of at zero (x0 projected onto
+ * the column bounds; the reference starts at zero, src/pdhg/pdhg.cu:576-580);
+ * FP32 + refinement takes it as its first anchor. Step size and primal
+ * weight start as usual. Not available on a presolved handle. */
+int igaos_pdhg_set_start(igaos_pdhg_problem* p, const double* x0, const double* y0);
+
 /* FP64 KKT metrics of (x, y) given in ORIGINAL units, evaluated on the
  * device (the fused pass replacing src/pdhg/pdhg.cu:173-254 + :698-733).
  * out6 = {pinf, dinf, gap, op, od, prow}. */
@@ -375,9 +383,10 @@ int igaos_pdhg_spmv(igaos_pdhg_problem* p, int transpose, int precision,
  * Per-instance outcome of igaos_pdhg_solve_batch. */
 typedef struct igaos_pdhg_batch_result {
     int status;              /* IGAOS_STATUS_* */
-    int finished_fp64;       /* 1: the persistent launch left this instance at
-                                max_iterations and the single-LP engine
-                                finished it in FP64 (ABI 4; was padding) */
+    int finished_fp64;       /* 1: the persistent launch handed this instance off
+                                or left it at max_iterations, and the
+                                single-LP engine finished it in FP64 (ABI 4;
+                                was padding) */
     double objective;        /* c^T x of the instance */
     double pinf, dinf, rel_gap, prow;
     int64_t iterations, attempts, restarts;
@@ -397,11 +406,15 @@ typedef struct igaos_pdhg_batch_result {
  * FP32 iterates, termination metrics combined in FP64) to `tolerance` or
  * `max_iterations` on its own, with its own restarts and termination; the
  * reference has no batched path (its engine is one LP per call,
- * src/pdhg/pdhg.hpp:9). An instance the launch leaves at max_iterations
- * (FP32 iterates can stall where FP64 ones do not) is then solved again,
- * alone, by the single-LP engine in FP64 (the reference's arithmetic) under
- * the same tolerance and iteration cap; its result says so (finished_fp64),
- * and `iterations` counts both runs. x (sum n) and y (sum m) may be NULL. */
+ * src/pdhg/pdhg.hpp:9). FP32 iterates can stall where FP64 ones do not:
+ * the first 16 instances still running at 100,000 iterations stop there
+ * (environment IGAOS_PDHG_BATCH_HANDOFF / _MAX change both numbers; 0
+ * iterations turns the hand-off off), and those, with any instance the
+ * launch leaves at max_iterations, are solved again by the single-LP engine
+ * in FP64 (the reference's arithmetic) under the same tolerance and
+ * iteration cap, up to 8 at once on their own streams. Their results say so
+ * (finished_fp64), and `iterations` counts both runs. x (sum n) and y
+ * (sum m) may be NULL. */
 int igaos_pdhg_solve_batch(int count, const int* m, const int* n,
                            const int* ap, const int* ai, const double* ax,
                            const double* c, const double* cl, const double* cu,

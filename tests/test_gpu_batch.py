@@ -65,6 +65,33 @@ def test_batch_matches_single_lp_engine(native):
         assert rel(r["objective"], single["objective"]) <= 2e-5
 
 
+def test_handoff_is_bounded_and_finishes_in_fp64(native, monkeypatch):
+    """With the hand-off at 1,000 iterations and at most 3 instances, exactly
+    3 of the instances still running at 1,000 iterations stop there and are
+    finished in FP64 (each to the tolerance, with more than 1,000 iterations
+    counted); the rest run to the tolerance in the launch, as without a
+    hand-off, bit for bit."""
+    from igaos_gb300 import capi
+    lps = c3_like(24, 11)
+    monkeypatch.setenv("IGAOS_PDHG_BATCH_HANDOFF", "0")
+    base = capi.solve_batch(lps, tolerance=1e-6, max_iterations=400000)
+    assert all(r["finished_fp64"] == 0 for r in base)
+    slow = [i for i, r in enumerate(base) if r["iterations"] > 1000]
+    assert len(slow) > 3
+    monkeypatch.setenv("IGAOS_PDHG_BATCH_HANDOFF", "1000")
+    monkeypatch.setenv("IGAOS_PDHG_BATCH_HANDOFF_MAX", "3")
+    out = capi.solve_batch(lps, tolerance=1e-6, max_iterations=400000)
+    handed = [i for i, r in enumerate(out) if r["finished_fp64"]]
+    assert len(handed) == 3 and set(handed) <= set(slow), handed
+    for i, (a, r) in enumerate(zip(base, out)):
+        assert r["status_name"] == "near-optimal", (i, r["status_name"])
+        if i in handed:
+            assert r["iterations"] > 1000
+            assert rel(r["objective"], a["objective"]) <= 2e-5
+        else:
+            assert r["iterations"] == a["iterations"] and r["objective"] == a["objective"]
+
+
 def test_batch_full_size_range_reaches_highs_optimum(native):
     import sys
     sys.path.insert(0, os.path.join(HERE, "golden"))
@@ -116,10 +143,10 @@ def test_batch_iteration_cap_and_validation(native):
 def test_instance_left_at_the_cap_is_finished_in_fp64(native):
     """Instance 1018 of the 4,096-LP set (m 1,747, n 4,368, 1 % density)
     needs ~256k FP32 + refinement iterations but far fewer in FP64. Under a
-    cap of 120,000 the persistent launch leaves it at the cap; the single-LP
-    engine then solves it in FP64 within the same cap, and the batch result
-    reports that finish and the FP64 engine's optimum. A batch whose instances all
-    converge in the launch has no such finish."""
+    cap of 120,000 the persistent launch hands it off at 100,000 iterations;
+    the single-LP engine then solves it in FP64 within the same cap, and the
+    batch result reports that finish and the FP64 engine's optimum. A batch
+    whose instances all converge early in the launch has no such finish."""
     from igaos_gb300 import capi
     lp = G.config3(seed=0, count=4096)[1018]
     assert (lp.m, lp.n) == (1747, 4368)
