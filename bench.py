@@ -33,9 +33,9 @@ and 1e-8 and the CPU oracle at 1e-8. `time_to_tol_multicommodity_lp` (m
 1,078,800, n 2,870,400): both precisions to 1e-4 and 1e-8, with attempt_us /
 attempt_hbm_frac (this LP streams from HBM) and the distance of the 1e-8
 objectives to scipy-HiGHS's optimum (tests/golden/mcf_objectives.json).
-`time_to_tol_large_lp`: this workload to 1e-4 (FP32 + refinement with the opt-in Pock-Chambolle scaling;
-FP64 with the reference's scaling and with it), each within a stated budget,
-with the KKT reached. `vs_reference_gpu`: the reference's own GPU PDHG
+`time_to_tol_large_lp`: this workload to 1e-4 (FP32 + refinement with the
+opt-in Pock-Chambolle scaling; FP64 with the reference's scaling and with
+it), each within a stated budget, with the KKT reached. `vs_reference_gpu`: the reference's own GPU PDHG
 (cuSPARSE path, compiled from its sources into oracle/_ref, timed on this GPU
 in this process) beside this engine -- to 1e-4 and 1e-8 on the small LP, and
 over a fixed 4,992-iteration budget on the two large LPs (above 46,340 rows
@@ -539,7 +539,7 @@ def main():
     e2e = None
     if not args.no_e2e:
         opts = dict(precision=args.precision, tolerance=1e-12, time_limit=1e9,
-                    max_iterations=args.iters, device=local)
+                    max_iterations=args.iters, device=local, schedule=args.schedule)
         h2d = sum(np.asarray(a).nbytes for a in (lp.ap, lp.ai, lp.ax, lp.cp, lp.ci, lp.acx, lp.c,
                                                    lp.cl, lp.cu, lp.rmin, lp.rmax))
         d2h = 8 * (lp.m + lp.n)
@@ -548,13 +548,21 @@ def main():
         barrier(ws)
         t0 = time.perf_counter()
         e_att = 0
+        setup_ms = solve_ms = 0.0
         for _ in range(e_steps):
             r = capi.solve_lp(lp, **opts)
             e_att += r["attempts"]
+            setup_ms += r["setup_time_ms"]
+            solve_ms += r["solve_time_ms"]
         torch.cuda.synchronize()
         el = barrier_max(time.perf_counter() - t0, ws)
+        # where a step's wall time goes: upload + device setup (ordering,
+        # scaling, power iteration), the solve (autotuning included when
+        # selected), the rest (host validation, download, teardown)
         e2e = {"value": ws * bpa * e_att / el / 1e9, "unit": "GB/s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * el / e_steps}
+               "d2h_bytes_per_step": d2h, "ms_per_step": 1e3 * el / e_steps,
+               "setup_ms": setup_ms / e_steps, "solve_ms": solve_ms / e_steps,
+               "schedule": args.schedule}
     slp = small = flp = c5 = c2tol = refg = None
     if rank == 0 and not args.no_small:
         slp, small = small_lp_probe(capi, G, local)

@@ -185,6 +185,11 @@ static std::vector<int> inverse(const std::vector<int>& p) {
     return q;
 }
 
+// IGX_PAD4=0 compiles out the padded FP32 copy of A (16-byte loads).
+#ifndef IGX_PAD4
+#define IGX_PAD4 1
+#endif
+
 static int grid_for(long long n, int per_block = kThreads, int cap = 152 * 16) {
     long long g = (n + per_block - 1) / per_block;
     if (g < 1) g = 1;
@@ -237,6 +242,22 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         }
         std::vector<long long> ent_a, slot_a, ent_at, slot_at;
         bool fit = small_share(P.data(), m, ent_a, slot_a);
+        // FP32 copy of A with every row padded to a multiple of 4 entries
+        // (16-byte aligned rows, pads: value 0 and the row's first index) for
+        // 16-byte vector loads (lane_products); built below when the LP runs
+        // on the grid-wide kernels and the pads add at most nnz / 8 entries
+        std::vector<int> P4(m + 1), I4;
+        P4[0] = 0;
+        for (int r = 0; r < m; ++r) P4[r + 1] = P4[r] + ((P[r + 1] - P[r] + 3) & ~3);
+        const long long nnz4 = P4[m];
+        if (IGX_PAD4 && nnz4 - nnz <= nnz / 8) {
+            I4.assign((size_t)nnz4, 0);
+            for (int r = 0; r < m; ++r) {
+                const int len = P[r + 1] - P[r];
+                for (int k = 0; k < P4[r + 1] - P4[r]; ++k)
+                    I4[(size_t)P4[r] + k] = I[(size_t)P[r] + (k < len ? k : 0)];
+            }
+        }
         permute_csr(n, cp, ci, acx, pc_, ipr_, P, I, V);
         CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(ci_, I.get(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
@@ -269,6 +290,15 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
                 if (worst <= kSmallSmemMax && cluster_fits(k == 1, (int)worst))
                     small_bytes_[k] = (int)worst;
             }
+        }
+        // the cluster path stages A by its unpadded row pointers: no padded
+        // copy for LPs it runs
+        if (!I4.empty() && small_bytes_[0] == 0) {
+            ap4_ = ar_.alloc<int>(m + 1);
+            ai4_ = ar_.alloc<int>((size_t)nnz4);
+            ax4_ = ar_.alloc<float>((size_t)nnz4);
+            CU(cudaMemcpy(ap4_, P4.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(ai4_, I4.data(), sizeof(int) * nnz4, cudaMemcpyHostToDevice));
         }
     }
     // vectors
@@ -407,6 +437,7 @@ void Engine::setup_scaling() {
     k_fix_scale<<<grid_for(m), kThreads, 0, st_>>>(m, dr_);
     k_fix_scale<<<grid_for(n), kThreads, 0, st_>>>(n, dc_);
     k_scale_matrix<<<gr_full, kThreads, 0, st_>>>(m, ap_, ai_, ax_, ax32_, dr_, dc_, 1);
+    if (ax4_) k_pad4<<<grid_for(m), kThreads, 0, st_>>>(m, ap_, ax32_, ap4_, ax4_);
     k_scale_matrix<<<gc_full, kThreads, 0, st_>>>(n, cp_, ci_, acx_, acx32_, dr_, dc_, 0);
     k_scale_vec<<<grid_for(m), kThreads, 0, st_>>>(m, base_.rmin, dr_, 0, base_.srmin, base_.frmin);
     k_scale_vec<<<grid_for(m), kThreads, 0, st_>>>(m, base_.rmax, dr_, 0, base_.srmax, base_.frmax);
@@ -430,7 +461,9 @@ void Engine::setup_scaling() {
 
 template <> Csr<double> Engine::csrA<double>() const { return Csr<double>{ap_, ai_, ax_, m, stream_[1]}; }
 template <> Csr<double> Engine::csrAT<double>() const { return Csr<double>{cp_, ci_, acx_, n, stream_[1]}; }
-template <> Csr<float> Engine::csrA<float>() const { return Csr<float>{ap_, ai_, ax32_, m, stream_[0]}; }
+template <> Csr<float> Engine::csrA<float>() const {
+    return ax4_ ? Csr<float>{ap4_, ai4_, ax4_, m, stream_[0], 1} : Csr<float>{ap_, ai_, ax32_, m, stream_[0]};
+}
 template <> Csr<float> Engine::csrAT<float>() const { return Csr<float>{cp_, ci_, acx32_, n, stream_[0]}; }
 
 template <typename T>

@@ -178,6 +178,8 @@ class Engine {
     int *ap_, *ai_, *cp_, *ci_;
     double *ax_, *acx_;
     float *ax32_, *acx32_;
+    int *ap4_ = nullptr, *ai4_ = nullptr;  // A padded to rows of 4k entries (FP32 copy)
+    float* ax4_ = nullptr;
     Sched sA_, sAT_;
     Sched sRA_, sRAT_;  // default schedules (setup passes, cluster path)
     // warp schedules of A and A^T for every kTuneEntries value; sA_ / sAT_

@@ -414,6 +414,16 @@ __global__ void k_scale_matrix(int rows, const int* __restrict__ ptr, const int*
     }
 }
 
+// The FP32 copy of A into its padded layout (row r in [ptr4[r], ptr4[r+1]),
+// a multiple of 4 slots; pads hold 0).
+__global__ void k_pad4(int rows, const int* __restrict__ ptr, const float* __restrict__ val,
+                       const int* __restrict__ ptr4, float* __restrict__ val4) {
+    for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
+        const int b = ptr[r], len = ptr[r + 1] - b, b4 = ptr4[r], len4 = ptr4[r + 1] - b4;
+        for (int k = 0; k < len4; ++k) val4[b4 + k] = k < len ? val[b + k] : 0.f;
+    }
+}
+
 // s = v / d (bounds) or v * d (cost), elementwise, FP64 and FP32 copies.
 // out = a - b in FP64 (change between two restart points)
 template <typename T>
