@@ -138,6 +138,26 @@ static Sched upload_sched(Arena& ar, const int* ptr, int rows, int resident_ctas
 // entries in their original order (the same summation order).
 // The entries are gathered by the host's threads over row ranges of equal
 // size (the output does not depend on the split).
+// Padded layout of a CSR structure for 16-byte loads: row r gets
+// [P4[r], P4[r+1]), its length rounded up to a multiple of 4; pad slots
+// repeat the row's first index. Left empty when the pads would exceed
+// max_extra entries.
+static void pad4_layout(const int* P, const int* I, int rows, long long max_extra,
+                        std::vector<int>& P4, std::vector<int>& I4) {
+    P4.assign(rows + 1, 0);
+    for (int r = 0; r < rows; ++r) P4[r + 1] = P4[r] + ((P[r + 1] - P[r] + 3) & ~3);
+    if ((long long)P4[rows] - P[rows] > max_extra) {
+        P4.clear();
+        return;
+    }
+    I4.assign((size_t)P4[rows], 0);
+    for (int r = 0; r < rows; ++r) {
+        const int len = P[r + 1] - P[r];
+        for (int k = 0; k < P4[r + 1] - P4[r]; ++k)
+            I4[(size_t)P4[r] + k] = I[(size_t)P[r] + (k < len ? k : 0)];
+    }
+}
+
 static void permute_csr(int rows, const int* ptr, const int* idx, const double* val,
                         const std::vector<int>& rnew2old, const std::vector<int>& iold2new,
                         std::vector<int>& P, std::unique_ptr<int[]>& I,
@@ -186,6 +206,9 @@ static std::vector<int> inverse(const std::vector<int>& p) {
 }
 
 // IGX_PAD4=0 compiles out the padded FP32 copy of A (16-byte loads).
+// A^T is not padded: on the multicommodity LP (3-entry columns) the third
+// more bytes cost more than the fewer loads saved (FP32 attempt 67.6 ->
+// 69.3 us; 200k x 500k LP 53.9 -> 54.2 us).
 #ifndef IGX_PAD4
 #define IGX_PAD4 1
 #endif
@@ -246,18 +269,8 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         // (16-byte aligned rows, pads: value 0 and the row's first index) for
         // 16-byte vector loads (lane_products); built below when the LP runs
         // on the grid-wide kernels and the pads add at most nnz / 8 entries
-        std::vector<int> P4(m + 1), I4;
-        P4[0] = 0;
-        for (int r = 0; r < m; ++r) P4[r + 1] = P4[r] + ((P[r + 1] - P[r] + 3) & ~3);
-        const long long nnz4 = P4[m];
-        if (IGX_PAD4 && nnz4 - nnz <= nnz / 8) {
-            I4.assign((size_t)nnz4, 0);
-            for (int r = 0; r < m; ++r) {
-                const int len = P[r + 1] - P[r];
-                for (int k = 0; k < P4[r + 1] - P4[r]; ++k)
-                    I4[(size_t)P4[r] + k] = I[(size_t)P[r] + (k < len ? k : 0)];
-            }
-        }
+        std::vector<int> P4, I4;
+        if (IGX_PAD4) pad4_layout(P.data(), I.get(), m, nnz / 8, P4, I4);
         permute_csr(n, cp, ci, acx, pc_, ipr_, P, I, V);
         CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(ci_, I.get(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
@@ -295,10 +308,10 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         // copy for LPs it runs
         if (!I4.empty() && small_bytes_[0] == 0) {
             ap4_ = ar_.alloc<int>(m + 1);
-            ai4_ = ar_.alloc<int>((size_t)nnz4);
-            ax4_ = ar_.alloc<float>((size_t)nnz4);
+            ai4_ = ar_.alloc<int>(I4.size());
+            ax4_ = ar_.alloc<float>(I4.size());
             CU(cudaMemcpy(ap4_, P4.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
-            CU(cudaMemcpy(ai4_, I4.data(), sizeof(int) * nnz4, cudaMemcpyHostToDevice));
+            CU(cudaMemcpy(ai4_, I4.data(), sizeof(int) * I4.size(), cudaMemcpyHostToDevice));
         }
     }
     // vectors
