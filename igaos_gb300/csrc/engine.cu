@@ -138,24 +138,14 @@ static Sched upload_sched(Arena& ar, const int* ptr, int rows, int resident_ctas
 // entries in their original order (the same summation order).
 // The entries are gathered by the host's threads over row ranges of equal
 // size (the output does not depend on the split).
-// Padded layout of a CSR structure for 16-byte loads: row r gets
-// [P4[r], P4[r+1]), its length rounded up to a multiple of 4; pad slots
-// repeat the row's first index. Left empty when the pads would exceed
-// max_extra entries.
-static void pad4_layout(const int* P, const int* I, int rows, long long max_extra,
-                        std::vector<int>& P4, std::vector<int>& I4) {
+// Row pointers of a CSR structure padded for 16-byte loads: row r gets
+// [P4[r], P4[r+1]), its length rounded up to a multiple of 4 (k_pad4 fills
+// the slots on the device). Left empty when the pads would exceed max_extra
+// entries.
+static void pad4_layout(const int* P, int rows, long long max_extra, std::vector<int>& P4) {
     P4.assign(rows + 1, 0);
     for (int r = 0; r < rows; ++r) P4[r + 1] = P4[r] + ((P[r + 1] - P[r] + 3) & ~3);
-    if ((long long)P4[rows] - P[rows] > max_extra) {
-        P4.clear();
-        return;
-    }
-    I4.assign((size_t)P4[rows], 0);
-    for (int r = 0; r < rows; ++r) {
-        const int len = P[r + 1] - P[r];
-        for (int k = 0; k < P4[r + 1] - P4[r]; ++k)
-            I4[(size_t)P4[r] + k] = I[(size_t)P[r] + (k < len ? k : 0)];
-    }
+    if ((long long)P4[rows] - P[rows] > max_extra) P4.clear();
 }
 
 static void permute_csr(int rows, const int* ptr, const int* idx, const double* val,
@@ -205,6 +195,9 @@ static std::vector<int> inverse(const std::vector<int>& p) {
     return q;
 }
 
+#ifndef IGX_SETUP_TIMES
+#define IGX_SETUP_TIMES 0
+#endif
 // IGX_PAD4=0 compiles out the padded FP32 copy of A (16-byte loads).
 // A^T is not padded: on the multicommodity LP (3-entry columns) the third
 // more bytes cost more than the fewer loads saved (FP32 attempt 67.6 ->
@@ -227,6 +220,20 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
                double obj_const_, int device, int scaling)
     : m(m_), n(n_), nnz(nnz_), obj_const(obj_const_), scaling_(scaling) {
     auto t_setup = std::chrono::steady_clock::now();
+    auto t_mark = t_setup;
+    // IGX_SETUP_TIMES=1 builds print the setup's phases (stream synchronised)
+    auto mark = [&](const char* what) {
+#if IGX_SETUP_TIMES
+        CU(cudaStreamSynchronize(st_));
+        const auto now = std::chrono::steady_clock::now();
+        std::fprintf(stderr, "[pdhg-gb300 setup] %-28s %8.2f ms\n", what,
+                     std::chrono::duration<double, std::milli>(now - t_mark).count());
+        t_mark = now;
+#else
+        (void)what;
+        (void)t_mark;
+#endif
+    };
     if (device >= 0) CU(cudaSetDevice(device));
     CU(cudaGetDevice(&device_));
     CU(cudaStreamCreateWithFlags(&st_, cudaStreamNonBlocking));
@@ -238,6 +245,7 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
     pc_ = length_order(cp, n);
     ipr_ = inverse(pr_);
     ipc_ = inverse(pc_);
+    mark("stream, orderings");
     {
         std::vector<int> P;
         std::unique_ptr<int[]> I;
@@ -269,8 +277,9 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         // (16-byte aligned rows, pads: value 0 and the row's first index) for
         // 16-byte vector loads (lane_products); built below when the LP runs
         // on the grid-wide kernels and the pads add at most nnz / 8 entries
-        std::vector<int> P4, I4;
-        if (IGX_PAD4) pad4_layout(P.data(), I.get(), m, nnz / 8, P4, I4);
+        std::vector<int> P4;
+        if (IGX_PAD4) pad4_layout(P.data(), m, nnz / 8, P4);
+        mark("A: permute, upload, schedules");
         permute_csr(n, cp, ci, acx, pc_, ipr_, P, I, V);
         CU(cudaMemcpy(cp_, P.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
         CU(cudaMemcpy(ci_, I.get(), sizeof(int) * nnz, cudaMemcpyHostToDevice));
@@ -306,13 +315,13 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         }
         // the cluster path stages A by its unpadded row pointers: no padded
         // copy for LPs it runs
-        if (!I4.empty() && small_bytes_[0] == 0) {
+        if (!P4.empty() && small_bytes_[0] == 0) {
             ap4_ = ar_.alloc<int>(m + 1);
-            ai4_ = ar_.alloc<int>(I4.size());
-            ax4_ = ar_.alloc<float>(I4.size());
+            ai4_ = ar_.alloc<int>((size_t)P4[m]);
+            ax4_ = ar_.alloc<float>((size_t)P4[m]);
             CU(cudaMemcpy(ap4_, P4.data(), sizeof(int) * (m + 1), cudaMemcpyHostToDevice));
-            CU(cudaMemcpy(ai4_, I4.data(), sizeof(int) * I4.size(), cudaMemcpyHostToDevice));
         }
+        mark("A^T: permute, upload, sched.");
     }
     // vectors
     auto vec = [&](const double* h, const std::vector<int>& perm) {
@@ -394,8 +403,11 @@ Engine::Engine(int m_, int n_, long long nnz_, const int* ap, const int* ai, con
         }
         if (const char* e = std::getenv("IGAOS_PDHG_L2_STREAM")) stream_[0] = stream_[1] = std::atoi(e) ? 1 : 0;
     }
+    mark("vectors, scratch");
     setup_scaling();
+    mark("scaling");
     power_iteration();
+    mark("power iteration");
     // eta0, omega0 (src/pdhg/pdhg.cu:642-663), from the scaled cost and
     // row bounds, in the reference's summation order.
     eta0 = 1.2 / std::sqrt(lam2);
@@ -450,7 +462,7 @@ void Engine::setup_scaling() {
     k_fix_scale<<<grid_for(m), kThreads, 0, st_>>>(m, dr_);
     k_fix_scale<<<grid_for(n), kThreads, 0, st_>>>(n, dc_);
     k_scale_matrix<<<gr_full, kThreads, 0, st_>>>(m, ap_, ai_, ax_, ax32_, dr_, dc_, 1);
-    if (ax4_) k_pad4<<<grid_for(m), kThreads, 0, st_>>>(m, ap_, ax32_, ap4_, ax4_);
+    if (ax4_) k_pad4<<<grid_for(m), kThreads, 0, st_>>>(m, ap_, ai_, ax32_, ap4_, ai4_, ax4_);
     k_scale_matrix<<<gc_full, kThreads, 0, st_>>>(n, cp_, ci_, acx_, acx32_, dr_, dc_, 0);
     k_scale_vec<<<grid_for(m), kThreads, 0, st_>>>(m, base_.rmin, dr_, 0, base_.srmin, base_.frmin);
     k_scale_vec<<<grid_for(m), kThreads, 0, st_>>>(m, base_.rmax, dr_, 0, base_.srmax, base_.frmax);

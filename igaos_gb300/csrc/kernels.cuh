@@ -415,12 +415,16 @@ __global__ void k_scale_matrix(int rows, const int* __restrict__ ptr, const int*
 }
 
 // The FP32 copy of A into its padded layout (row r in [ptr4[r], ptr4[r+1]),
-// a multiple of 4 slots; pads hold 0).
-__global__ void k_pad4(int rows, const int* __restrict__ ptr, const float* __restrict__ val,
-                       const int* __restrict__ ptr4, float* __restrict__ val4) {
+// a multiple of 4 slots; pads hold value 0 and the row's first index).
+__global__ void k_pad4(int rows, const int* __restrict__ ptr, const int* __restrict__ idx,
+                       const float* __restrict__ val, const int* __restrict__ ptr4,
+                       int* __restrict__ idx4, float* __restrict__ val4) {
     for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < rows; r += gridDim.x * blockDim.x) {
         const int b = ptr[r], len = ptr[r + 1] - b, b4 = ptr4[r], len4 = ptr4[r + 1] - b4;
-        for (int k = 0; k < len4; ++k) val4[b4 + k] = k < len ? val[b + k] : 0.f;
+        for (int k = 0; k < len4; ++k) {
+            idx4[b4 + k] = idx[b + (k < len ? k : 0)];
+            val4[b4 + k] = k < len ? val[b + k] : 0.f;
+        }
     }
 }
 
