@@ -92,6 +92,31 @@ def test_spmv_fp64_and_fp32(case, orc):
         assert np.all(np.abs(y32 - ref) <= tol), np.max(np.abs(y32 - ref) / mag)
 
 
+@pytest.mark.parametrize("name", sorted(MATS))
+def test_spmv_grid_kernels_padded_rows(native, orc, monkeypatch, name):
+    """With the cluster path off, the FP32 copy of A has rows padded to 4k
+    entries and lanes read 4-entry chunks with 16-byte loads (dealt to the
+    G lanes of a row in turn; the long-row case has G = 32). Same bounds as
+    the unpadded products."""
+    from igaos_gb300 import capi
+    monkeypatch.setenv("IGAOS_PDHG_CLUSTER", "0")
+    lp = MATS[name]
+    olp = orc.lp_from(lp)
+    sd = orc.scale(olp, *orc.ruiz(olp))
+    rng = np.random.default_rng(5)
+    with capi.Problem(lp) as P:
+        for transpose in (False, True):
+            ptr, idx, val = (olp.cp, olp.ci, sd["sacx"]) if transpose else (olp.ap, olp.ai, sd["sax"])
+            x = rng.standard_normal(lp.m if transpose else lp.n)
+            ref = orc.spmv(ptr, idx, val, x)
+            mag = orc.spmv(ptr, idx, np.abs(val), np.abs(x)) + 1e-300
+            y32 = P.spmv(x, transpose=transpose, precision="fp32")
+            tol = 2.5 * 2.0 ** -24 * mag + 2.0 ** -24 * np.abs(ref)
+            assert np.all(np.abs(y32 - ref) <= tol), np.max(np.abs(y32 - ref) / mag)
+            y64 = P.spmv(x, transpose=transpose, precision="fp64")
+            assert np.all(np.abs(y64 - ref) <= 1e-14 * mag)
+
+
 def test_step_init(case, orc):
     _, lp, olp, P = case
     sd = orc.scale(olp, *orc.ruiz(olp))
