@@ -35,13 +35,18 @@ attempt_hbm_frac (this LP streams from HBM) and the distance of the 1e-8
 objectives to scipy-HiGHS's optimum (tests/golden/mcf_objectives.json).
 `time_to_tol_large_lp`: this workload to 1e-4 (FP32 + refinement with the
 opt-in Pock-Chambolle scaling; FP64 with the reference's scaling and with
-it), each within a stated budget, with the KKT reached. `vs_reference_gpu`: the reference's own GPU PDHG
-(cuSPARSE path, compiled from its sources into oracle/_ref, timed on this GPU
-in this process) beside this engine -- to 1e-4 and 1e-8 on the small LP, and
-over a fixed 4,992-iteration budget on the two large LPs (above 46,340 rows
-its dense dual repair, reached from iteration 5,000, overflows int32
-indices). Also `batched_small_lps` (4,096 uneven LPs to 1e-6 in one
-persistent launch vs sequential solves) and `differentiable_layer`.
+it), each within a stated budget, with the KKT reached. `vs_reference_gpu`:
+the reference's own GPU PDHG (cuSPARSE path, compiled from its sources into
+oracle/_ref, timed on this GPU in this process) beside this engine -- to
+1e-4 and 1e-8 on the small LP, and over a fixed 4,992-iteration budget on
+the two large LPs (above 46,340 rows its dense dual repair, reached from
+iteration 5,000, overflows int32 indices). Also `batched_small_lps` (4,096
+uneven LPs to 1e-6 in one persistent launch vs sequential solves) and
+`differentiable_layer`. Every
+single-LP solve of the bench (headline, e2e, time to tolerance, per-iteration
+comparison) runs the `--schedule` warp schedule (default: autotuned per
+problem and precision, the tuning timed with the solve where a fresh
+problem is created).
 """
 from __future__ import annotations
 
@@ -305,7 +310,7 @@ def rel_diff(a, b):
     return abs(a - b) / max(1.0, abs(b))
 
 
-def small_lp_probe(capi, G, local):
+def small_lp_probe(capi, G, local, sched):
     """Small random LP (m 2,000, n 5,000, seed 0): FP32 + refinement and FP64
     to 1e-4 and 1e-8 (device-resident), and the CPU oracle at 1e-8."""
     slp = G.config1(seed=0)
@@ -313,9 +318,9 @@ def small_lp_probe(capi, G, local):
     x_last = None
     with capi.Problem(slp, device=local) as P:
         for prec in ("fp64", "fp32-refine"):
-            P.solve(precision=prec, tolerance=1e-6, time_limit=60.0)  # warm
+            P.solve(precision=prec, tolerance=1e-6, time_limit=60.0, schedule=sched)  # warm
             for tol in (1e-4, 1e-8):
-                r = P.solve(precision=prec, tolerance=tol, time_limit=60.0)
+                r = P.solve(precision=prec, tolerance=tol, time_limit=60.0, schedule=sched)
                 out[f"{prec}@{tol:g}"] = tol_entry(r)
                 if prec == "fp32-refine" and tol == 1e-8:
                     x_last = r["x"]
@@ -339,7 +344,7 @@ def small_lp_probe(capi, G, local):
     return slp, out
 
 
-def c5_probe(capi, G, local):
+def c5_probe(capi, G, local, sched):
     """Multicommodity LP: both precisions to 1e-4 and 1e-8 (device-resident),
     with the attempt time against the HBM roofline (this LP's working set
     exceeds L2, so its attempts stream from HBM)."""
@@ -350,7 +355,7 @@ def c5_probe(capi, G, local):
         for prec in ("fp32-refine", "fp64"):
             cb = bytes_per_attempt(flp.m, flp.n, flp.nnz, 8 if prec == "fp64" else 4)
             for tol in (1e-4, 1e-8):
-                r = P.solve(precision=prec, tolerance=tol, time_limit=240.0)
+                r = P.solve(precision=prec, tolerance=tol, time_limit=240.0, schedule=sched)
                 e = tol_entry(r)
                 us = 1e3 * r["attempt_time_ms"] / max(1, r["attempts"])
                 e.update(attempt_us=us, attempt_bytes=cb,
@@ -373,21 +378,23 @@ def c5_probe(capi, G, local):
     return flp, out
 
 
-def c2_tol_probe(capi, lp, local, budget32, budget64):
+def c2_tol_probe(capi, lp, local, budget32, budget64, sched):
     """The large LP to 1e-4: FP32 + refinement with the opt-in Pock-Chambolle
     scaling; FP64 with it and with the reference's Ruiz scaling alone; each
     within its budget (seconds), reporting the KKT reached when it runs out."""
     out = {"tolerance": 1e-4, "budget_s": {"fp32-refine": budget32, "fp64": budget64}}
     with capi.Problem(lp, device=local, scaling="ruiz-pc") as P:
         out["fp32-refine+pc"] = tol_entry(P.solve(precision="fp32-refine", tolerance=1e-4,
-                                                  time_limit=budget32))
-        out["fp64+pc"] = tol_entry(P.solve(precision="fp64", tolerance=1e-4, time_limit=budget64))
+                                                  time_limit=budget32, schedule=sched))
+        out["fp64+pc"] = tol_entry(P.solve(precision="fp64", tolerance=1e-4, time_limit=budget64,
+                                           schedule=sched))
     with capi.Problem(lp, device=local) as P:
-        out["fp64"] = tol_entry(P.solve(precision="fp64", tolerance=1e-4, time_limit=budget64))
+        out["fp64"] = tol_entry(P.solve(precision="fp64", tolerance=1e-4, time_limit=budget64,
+                                        schedule=sched))
     return out
 
 
-def vs_reference_gpu(capi, local, slp, flp, lp):
+def vs_reference_gpu(capi, local, slp, flp, lp, sched):
     """The reference's GPU PDHG beside this engine on the same GPU. Small LP:
     both to 1e-4 and 1e-8 (loop time and whole-call wall time). Large LPs: a
     fixed budget of 4,992 iterations (seconds per iteration, KKT reached)."""
@@ -399,7 +406,8 @@ def vs_reference_gpu(capi, local, slp, flp, lp):
         row = {"reference": ref}
         for prec in ("fp64", "fp32-refine"):
             t0 = time.perf_counter()
-            r = capi.solve_lp(slp, precision=prec, tolerance=tol, time_limit=120.0, device=local)
+            r = capi.solve_lp(slp, precision=prec, tolerance=tol, time_limit=120.0, device=local,
+                              schedule=sched)
             row[prec] = tol_entry(r, wall_s=time.perf_counter() - t0)
             if ref["status"] == r["status_name"] == "near-optimal":
                 row[prec]["speedup_loop"] = ref["loop_s"] / row[prec]["loop_s"]
@@ -415,7 +423,8 @@ def vs_reference_gpu(capi, local, slp, flp, lp):
                "reference_s_per_iteration": ref["loop_s"] / max(1, ref["iterations"])}
         with capi.Problem(big, device=local) as P:
             for prec in ("fp64", "fp32-refine"):
-                r = P.solve(precision=prec, tolerance=1e-12, time_limit=1e9, max_iterations=4992)
+                r = P.solve(precision=prec, tolerance=1e-12, time_limit=1e9, max_iterations=4992,
+                            schedule=sched)
                 e = tol_entry(r)
                 e["s_per_iteration"] = e["loop_s"] / max(1, r["iterations"])
                 e["speedup_per_iteration"] = row["reference_s_per_iteration"] / e["s_per_iteration"]
@@ -565,15 +574,15 @@ def main():
                "schedule": args.schedule}
     slp = small = flp = c5 = c2tol = refg = None
     if rank == 0 and not args.no_small:
-        slp, small = small_lp_probe(capi, G, local)
+        slp, small = small_lp_probe(capi, G, local, args.schedule)
     if rank == 0 and not args.no_c5:
-        flp, c5 = c5_probe(capi, G, local)
+        flp, c5 = c5_probe(capi, G, local, args.schedule)
     if rank == 0 and not args.no_c2_tol:
-        c2tol = c2_tol_probe(capi, lp, local, args.c2_budget, 0.6 * args.c2_budget)
+        c2tol = c2_tol_probe(capi, lp, local, args.c2_budget, 0.6 * args.c2_budget, args.schedule)
     if rank == 0 and not args.no_ref_gpu:
         if ref_gpu_ready():
             slp = slp or G.config1(seed=0)
-            refg = vs_reference_gpu(capi, local, slp, flp, lp if s == 1.0 else None)
+            refg = vs_reference_gpu(capi, local, slp, flp, lp if s == 1.0 else None, args.schedule)
         else:
             refg = {"unavailable": "reference GPU PDHG not built here (oracle/_ref needs the "
                                    "reference sources or their staging in oracle/_ref/src)"}
