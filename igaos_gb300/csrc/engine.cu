@@ -127,6 +127,7 @@ static Sched upload_sched(Arena& ar, const int* ptr, int rows, int resident_ctas
     s.nwarps = (int)wl.size();
     s.ctas = std::max(1, std::min(resident_ctas, (s.nwarps + kWarps - 1) / kWarps));
     s.ctas64 = std::max(1, std::min(s.ctas, resident_ctas / kHotCtasPerSm * HotCtas<double>::value));
+    s.ctas64w = std::max(1, std::min(s.ctas, resident_ctas / kHotCtasPerSm * 4));
     s.row = ar.alloc<int>(wr.size());
     s.lg = ar.alloc<unsigned char>(wl.size());
     CU(cudaMemcpy(s.row, wr.data(), sizeof(int) * wr.size(), cudaMemcpyHostToDevice));
@@ -599,23 +600,52 @@ void Engine::attempt_args(const Vecs& v, PrimalArgs<T>& pa, DualArgs<T>& da) {
     }
     da.part = reinterpret_cast<Acc<T>*>(w.part_d);
     da.part_primal = reinterpret_cast<const Acc<T>*>(w.part_p);
-    const bool f64 = std::is_same<T, double>::value;
-    da.n_primal = f64 ? sAT_.ctas64 : sAT_.ctas;
+    da.n_primal = grid_primal<T>();
     da.yhat = VecSel<T>::yh(v);
     da.fac = fac_;
     da.n_fac = kFac;
     da.ctl = ctl_;
 }
 
+template <typename T>
+int Engine::grid_primal() const {
+    if constexpr (std::is_same<T, double>::value) return occ_[1] == 4 ? sAT_.ctas64w : sAT_.ctas64;
+    return sAT_.ctas;
+}
+template <typename T>
+int Engine::grid_dual() const {
+    if constexpr (std::is_same<T, double>::value) return occ_[0] == 4 ? sA_.ctas64w : sA_.ctas64;
+    return sA_.ctas;
+}
+template <typename T>
+void Engine::launch_primal(const PrimalArgs<T>& pa) {
+    const int gp = grid_primal<T>();
+    if constexpr (std::is_same<T, double>::value) {
+        if (occ_[1] == 4) k_primal<double, 4><<<gp, kThreads, 0, st_>>>(pa);
+        else k_primal<double, 3><<<gp, kThreads, 0, st_>>>(pa);
+    } else {
+        k_primal<T><<<gp, kThreads, 0, st_>>>(pa);
+    }
+}
+template <typename T>
+void Engine::launch_dual(const DualArgs<T>& da) {
+    const int gd = grid_dual<T>();
+    if constexpr (std::is_same<T, double>::value) {
+        if (occ_[0] == 4) k_dual<double, 4><<<gd, kThreads, 0, st_>>>(da);
+        else k_dual<double, 3><<<gd, kThreads, 0, st_>>>(da);
+    } else {
+        k_dual<T><<<gd, kThreads, 0, st_>>>(da);
+    }
+}
+
 // Enqueues `count` line-search attempts (2 launches each). With graphs the
-// sequence is captured once per (precision, count, vector set) and replayed.
+// sequence is captured once per (precision, count, vector set, schedules and
+// occupancies in use) and replayed.
 template <typename T>
 void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     PrimalArgs<T> pa;
     DualArgs<T> da;
     attempt_args<T>(v, pa, da);
-    const bool f64 = std::is_same<T, double>::value;
-    const int gp = f64 ? sAT_.ctas64 : sAT_.ctas, gd = f64 ? sA_.ctas64 : sA_.ctas;
     if (const int sb = small_bytes_[std::is_same<T, double>::value ? 1 : 0]) {
         // one cluster runs the whole chunk with the LP in shared memory (it
         // stages the default schedule)
@@ -629,10 +659,7 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     }
     launches_ += 2LL * count;
     auto enqueue = [&](int cnt) {
-        for (int a = 0; a < cnt; ++a) {
-            k_primal<T><<<gp, kThreads, 0, st_>>>(pa);
-            k_dual<T><<<gd, kThreads, 0, st_>>>(da);
-        }
+        for (int a = 0; a < cnt; ++a) enqueue_attempt<T>(pa, da);
     };
     if (!graphs) {
         enqueue(count);
@@ -641,7 +668,8 @@ void Engine::launch_attempts(int count, const Vecs& v, bool graphs) {
     }
     // key: precision, attempt count, vector set
     const GraphKey key{std::is_same<T, double>::value ? 1 : 2, count,
-                       (uintptr_t)VecSel<T>::c(v), kTuneCount * ia_ + iat_};
+                       (uintptr_t)VecSel<T>::c(v),
+                       4 * (kTuneCount * ia_ + iat_) + 2 * (occ_[0] == 4) + (occ_[1] == 4)};
     auto it = graphs_.find(key);
     if (it == graphs_.end()) {
         cudaGraph_t g;
@@ -702,35 +730,45 @@ void Engine::tune() {
     constexpr int kReps = 12;
     cudaEvent_t e[3];
     for (auto& ev : e) CU(cudaEventCreate(&ev));
-    const bool f64 = pi == 1;
-    for (int c = 0; c < kTuneCount; ++c) {
-        use_sched(c, c);
-        PrimalArgs<T> pa;
-        DualArgs<T> da;
-        attempt_args<T>(base_, pa, da);
-        const int gp = f64 ? sAT_.ctas64 : sAT_.ctas, gd = f64 ? sA_.ctas64 : sA_.ctas;
-        k_primal<T><<<gp, kThreads, 0, st_>>>(pa);
-        k_dual<T><<<gd, kThreads, 0, st_>>>(da);
-        CU(cudaEventRecord(e[0], st_));
-        for (int r = 0; r < kReps; ++r) k_primal<T><<<gp, kThreads, 0, st_>>>(pa);
-        CU(cudaEventRecord(e[1], st_));
-        for (int r = 0; r < kReps; ++r) k_dual<T><<<gd, kThreads, 0, st_>>>(da);
-        CU(cudaEventRecord(e[2], st_));
-        CU(cudaGetLastError());
-        CU(cudaEventSynchronize(e[2]));
-        float tp = 0.f, td = 0.f;
-        CU(cudaEventElapsedTime(&tp, e[0], e[1]));
-        CU(cudaEventElapsedTime(&td, e[1], e[2]));
-        tune_us_[pi][1][c] = 1e3f * tp / kReps;
-        tune_us_[pi][0][c] = 1e3f * td / kReps;
-        launches_ += 2 * (kReps + 1);
-    }
+    // FP64 attempts are also timed at 4 resident CTAs per SM (their 64
+    // registers hold without spills): more warps hide more gather latency on
+    // some LPs (multicommodity LP: 140 -> 134 us), fewer cost the FP64-pipe
+    // bound ones less (200k x 500k LP: 89 against 91 us)
+    const int nocc = pi == 1 ? 2 : 1;
+    for (int c = 0; c < kTuneCount; ++c)
+        for (int oi = 0; oi < nocc; ++oi) {
+            use_sched(c, c);
+            occ_[0] = occ_[1] = oi ? 4 : 3;
+            PrimalArgs<T> pa;
+            DualArgs<T> da;
+            attempt_args<T>(base_, pa, da);
+            enqueue_attempt<T>(pa, da);
+            CU(cudaEventRecord(e[0], st_));
+            for (int r = 0; r < kReps; ++r) launch_primal<T>(pa);
+            CU(cudaEventRecord(e[1], st_));
+            for (int r = 0; r < kReps; ++r) launch_dual<T>(da);
+            CU(cudaEventRecord(e[2], st_));
+            CU(cudaGetLastError());
+            CU(cudaEventSynchronize(e[2]));
+            float tp = 0.f, td = 0.f;
+            CU(cudaEventElapsedTime(&tp, e[0], e[1]));
+            CU(cudaEventElapsedTime(&td, e[1], e[2]));
+            tune_us_[pi][1][c][oi] = 1e3f * tp / kReps;
+            tune_us_[pi][0][c][oi] = 1e3f * td / kReps;
+            launches_ += 2 * (kReps + 1);
+        }
     for (auto& ev : e) cudaEventDestroy(ev);
+    occ_[0] = occ_[1] = 3;
     for (int o = 0; o < 2; ++o) {
-        int best = def;
+        int best = def, bo = 0;
         for (int c = 0; c < kTuneCount; ++c)
-            if (tune_us_[pi][o][c] < tune_us_[pi][o][best]) best = c;
+            for (int oi = 0; oi < nocc; ++oi)
+                if (tune_us_[pi][o][c][oi] < tune_us_[pi][o][best][bo]) {
+                    best = c;
+                    bo = oi;
+                }
         choice_[pi][o] = best;
+        if (pi == 1) choice_occ_[o] = bo ? 4 : 3;
     }
 }
 
@@ -1407,16 +1445,26 @@ void Engine::solve(const igaos_pdhg_options& o, igaos_pdhg_result& r, double* x,
         if (pi) tune<double>();
         else tune<float>();
         use_sched(choice_[pi][0], choice_[pi][1]);
-        if (o.verbosity > 0)
-            std::fprintf(stderr, "[pdhg-gb300] autotuned schedule (us per launch at 2/4/8/16/32 "
-                                 "entries per lane): A %.1f/%.1f/%.1f/%.1f/%.1f -> %d, A^T "
-                                 "%.1f/%.1f/%.1f/%.1f/%.1f -> %d\n",
-                         tune_us_[pi][0][0], tune_us_[pi][0][1], tune_us_[pi][0][2],
-                         tune_us_[pi][0][3], tune_us_[pi][0][4], sA_.entries, tune_us_[pi][1][0],
-                         tune_us_[pi][1][1], tune_us_[pi][1][2], tune_us_[pi][1][3],
-                         tune_us_[pi][1][4], sAT_.entries);
+        occ_[0] = pi ? choice_occ_[0] : 3;
+        occ_[1] = pi ? choice_occ_[1] : 3;
+        if (o.verbosity > 0) {
+            const char* name[2] = {"A", "A^T"};
+            const int chosen[2] = {sA_.entries, sAT_.entries};
+            for (int q = 0; q < 2; ++q) {
+                std::fprintf(stderr, "[pdhg-gb300] autotuned %s (us per launch at 2/4/8/16/32 entries "
+                                     "per lane):", name[q]);
+                for (int oi = 0; oi < (pi ? 2 : 1); ++oi) {
+                    std::fprintf(stderr, " %d CTAs/SM", oi ? 4 : (pi ? 3 : kHotCtasPerSm));
+                    for (int c = 0; c < kTuneCount; ++c)
+                        std::fprintf(stderr, "%s%.1f", c ? "/" : " ", tune_us_[pi][q][c][oi]);
+                }
+                std::fprintf(stderr, " -> %d entries, %d CTAs/SM\n", chosen[q],
+                             pi ? occ_[q] : kHotCtasPerSm);
+            }
+        }
     } else {
         use_sched(def, def);
+        occ_[0] = occ_[1] = 3;
     }
     if (o.precision == IGAOS_PDHG_FP32_REFINE) {
         solve_refine(o, r, x, y);

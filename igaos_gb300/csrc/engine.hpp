@@ -47,7 +47,8 @@ struct Sched {
     unsigned char* lg = nullptr;
     int nwarps = 0;
     int ctas = 0;  // kWarps warps per CTA
-    int ctas64 = 0;  // launch width of the FP64 attempt kernels
+    int ctas64 = 0;  // launch width of the FP64 attempt kernels (3 CTAs per SM)
+    int ctas64w = 0; // the same at 4 CTAs per SM
     int entries = 0; // entries per lane the schedule was built for
     WarpSched view() const { return WarpSched{row, lg, nwarps}; }
 };
@@ -187,8 +188,10 @@ class Engine {
     Sched candA_[kTuneCount], candAT_[kTuneCount];
     int cap_ctas_A_ = 0, cap_ctas_AT_ = 0;  // largest launch width of the candidates
     int ia_ = 2, iat_ = 2;                  // candidates in use as sA_ / sAT_ (8 entries)
+    int occ_[2] = {3, 3};                   // FP64 attempts: CTAs per SM of k_dual (A), k_primal (A^T)
     int choice_[2][2] = {{-1, -1}, {-1, -1}};  // autotuned (A, A^T) per FP32 / FP64
-    float tune_us_[2][2][kTuneCount] = {};  // per attempt-kernel launch, us
+    int choice_occ_[2] = {3, 3};            // autotuned FP64 occupancy (A, A^T)
+    float tune_us_[2][2][kTuneCount][2] = {};  // per attempt-kernel launch, us (occupancy 3, 4)
     void use_sched(int ia, int iat);
     template <typename T> void tune();
     template <typename T> void attempt_args(const Vecs& v, PrimalArgs<T>& pa, DualArgs<T>& da);
@@ -240,6 +243,16 @@ class Engine {
     template <typename T> Csr<T> csrAT() const;
     template <typename T> void ensure_work();
     template <typename T> void launch_attempts(int count, const Vecs& v, bool graphs);
+    // launch widths of the attempt kernels and one attempt's two launches at
+    // the occupancies in use
+    template <typename T> int grid_primal() const;
+    template <typename T> int grid_dual() const;
+    template <typename T> void launch_primal(const PrimalArgs<T>& pa);
+    template <typename T> void launch_dual(const DualArgs<T>& da);
+    template <typename T> void enqueue_attempt(const PrimalArgs<T>& pa, const DualArgs<T>& da) {
+        launch_primal<T>(pa);
+        launch_dual<T>(da);
+    }
     template <typename T> void run_until_stop(const Vecs& v, bool graphs, LoopOut& out);
     template <typename T> void kkt(const Vecs& v, const T* x0, const T* y0, const T* x1,
                                    const T* y1, int ncand);

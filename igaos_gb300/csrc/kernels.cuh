@@ -104,8 +104,10 @@ struct PrimalEpi {
     }
 };
 
-template <typename T>
-__global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_primal(PrimalArgs<T> a) {
+// OCC: resident CTAs per SM the kernel is compiled for (its register
+// budget); FP64 attempts come in two (3 and 4), chosen by the autotuner.
+template <typename T, int OCC = HotCtas<T>::value>
+__global__ void __launch_bounds__(kThreads, OCC) k_primal(PrimalArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;
@@ -241,8 +243,8 @@ __device__ inline void decide_step(DevCtl* c, double dx2, double dy2, double cro
 // kern_dots (:67-97), and -- in the last CTA to finish -- the fixed-order
 // reduction of all partials (kern_dotfin, :99-125) and the step decision that
 // the reference made on the host after a blocking copy (:768-794).
-template <typename T>
-__global__ void __launch_bounds__(kThreads, HotCtas<T>::value) k_dual(DualArgs<T> a) {
+template <typename T, int OCC = HotCtas<T>::value>
+__global__ void __launch_bounds__(kThreads, OCC) k_dual(DualArgs<T> a) {
     __shared__ __align__(16) double smred[kWarps * 4];
     const CtlView<T> cv = read_ctl<T>(a.ctl);
     if (cv.stop) return;

@@ -120,9 +120,10 @@ typedef struct igaos_pdhg_options {
      * IGAOS_PDHG_SCHEDULE_FIXED (0, default): about 8 entries per lane.
      * IGAOS_PDHG_SCHEDULE_AUTOTUNE (1): at the first solve of each precision
      * on a handle, the A and A^T attempt kernels are timed on schedules of 2, 4,
-     * 8, 16 and 32 entries per lane (a dozen launches each) and the fastest is
-     * kept for that handle and precision; the result's entries_a /
-     * entries_at report the choice. The schedule changes the order of each
+     * 8, 16 and 32 entries per lane (a dozen launches each; FP64 kernels
+     * also at 3 and 4 resident CTAs per SM) and the fastest is kept for that
+     * handle and precision; the result's entries_a / entries_at report the
+     * choice. The schedule changes the order of each
      * row's sum, so results match the fixed schedule's to rounding, not bit
      * for bit, and two handles may choose differently. Added in ABI 4. */
     int schedule;
