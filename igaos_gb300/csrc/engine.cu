@@ -727,7 +727,7 @@ void Engine::tune() {
     h_ctl_->k = 1;
     h_ctl_->k_stop = std::numeric_limits<long long>::max() / 2;
     upload_ctl();
-    constexpr int kReps = 12;
+    constexpr int kReps = 8;  // launches per timing (after a warming one)
     cudaEvent_t e[3];
     for (auto& ev : e) CU(cudaEventCreate(&ev));
     // FP64 attempts are also timed at 4 resident CTAs per SM (their 64

@@ -120,7 +120,7 @@ typedef struct igaos_pdhg_options {
      * IGAOS_PDHG_SCHEDULE_FIXED (0, default): about 8 entries per lane.
      * IGAOS_PDHG_SCHEDULE_AUTOTUNE (1): at the first solve of each precision
      * on a handle, the A and A^T attempt kernels are timed on schedules of 2, 4,
-     * 8, 16 and 32 entries per lane (a dozen launches each; FP64 kernels
+     * 8, 16 and 32 entries per lane (8 launches each; FP64 kernels
      * also at 3 and 4 resident CTAs per SM) and the fastest is kept for that
      * handle and precision; the result's entries_a / entries_at report the
      * choice. The schedule changes the order of each
