@@ -42,11 +42,15 @@ oracle/_ref, timed on this GPU in this process) beside this engine -- to
 the two large LPs (above 46,340 rows its dense dual repair, reached from
 iteration 5,000, overflows int32 indices). Also `batched_small_lps` (4,096
 uneven LPs to 1e-6 in one persistent launch vs sequential solves) and
-`differentiable_layer`. Every
-single-LP solve of the bench (headline, e2e, time to tolerance, per-iteration
-comparison) runs the `--schedule` warp schedule (default: autotuned per
-problem and precision, the tuning timed with the solve where a fresh
-problem is created).
+`differentiable_layer`. The speed measures (headline, e2e, the per-iteration
+comparison on the large LPs) run the `--schedule` warp schedule (default:
+autotuned per problem and precision, the tuning timed with the solve where
+a fresh problem is created). Time to tolerance runs the fixed schedule: the
+autotuner's choice depends on timing noise and changes the rounding of the
+products and of the step decision's dot products, and PDHG's trajectory
+with it (multicommodity LP in FP64 to 1e-8: 83,776 iterations on the fixed
+schedule, 140,800 on one tuned choice), so only the fixed schedule gives
+iteration counts that repeat from run to run.
 """
 from __future__ import annotations
 
@@ -407,7 +411,7 @@ def vs_reference_gpu(capi, local, slp, flp, lp, sched):
         for prec in ("fp64", "fp32-refine"):
             t0 = time.perf_counter()
             r = capi.solve_lp(slp, precision=prec, tolerance=tol, time_limit=120.0, device=local,
-                              schedule=sched)
+                              schedule="fixed")  # a time to tolerance: fixed schedule
             row[prec] = tol_entry(r, wall_s=time.perf_counter() - t0)
             if ref["status"] == r["status_name"] == "near-optimal":
                 row[prec]["speedup_loop"] = ref["loop_s"] / row[prec]["loop_s"]
@@ -574,11 +578,11 @@ def main():
                "schedule": args.schedule}
     slp = small = flp = c5 = c2tol = refg = None
     if rank == 0 and not args.no_small:
-        slp, small = small_lp_probe(capi, G, local, args.schedule)
+        slp, small = small_lp_probe(capi, G, local, "fixed")
     if rank == 0 and not args.no_c5:
-        flp, c5 = c5_probe(capi, G, local, args.schedule)
+        flp, c5 = c5_probe(capi, G, local, "fixed")
     if rank == 0 and not args.no_c2_tol:
-        c2tol = c2_tol_probe(capi, lp, local, args.c2_budget, 0.6 * args.c2_budget, args.schedule)
+        c2tol = c2_tol_probe(capi, lp, local, args.c2_budget, 0.6 * args.c2_budget, "fixed")
     if rank == 0 and not args.no_ref_gpu:
         if ref_gpu_ready():
             slp = slp or G.config1(seed=0)
