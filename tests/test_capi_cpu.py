@@ -90,6 +90,8 @@ def test_no_device_is_an_honest_error(native):
 def test_null_handles(native):
     from igaos_gb300 import capi
     assert native.igaos_pdhg_solve(None, None, None, None, None) == capi.ERR_INVALID
+    assert native.igaos_pdhg_set_start(None, None, None) == capi.ERR_INVALID
+    assert "NULL" in capi.last_error()
     native.igaos_pdhg_destroy(None)  # no-op
 
 
